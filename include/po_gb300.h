@@ -1,0 +1,202 @@
+/*
+ * po_gb300.h -- C-ABI of libpo_gb300.so, the GB300 (sm_103a) physical-optics
+ * surface-current integrator.
+ *
+ * The struct layouts below are identical to PyPO's (reference
+ * src/include/Structs.h:42-147, :243-348) so that the reference's ctypes
+ * structs (src/PyPO/Structs.py) bind to these entry points unchanged.
+ *
+ * Every entry point returns an int status: 0 on success, non-zero on error,
+ * with a message available from po_last_error() on the calling thread. No
+ * entry point calls exit() or cudaDeviceReset(); the CUDA context is shared
+ * with the caller (for example PyTorch).
+ *
+ * Mode numbers: 0 JM, 1 EH, 2 JMEH, 3 EHP, 4 FF, 5 scalar. The semantics are
+ * those of the reference's FP64 CPU path (src/CPU/Propagation.h): PEC
+ * currents J = 2 n x H, M = 0 for JM and JMEH; reflected H scaled by the
+ * medium conductance in EHP; exp(-t j k r) in scalar mode; the illumination
+ * test n_s . R_hat >= 0 for both time directions.
+ */
+#ifndef PO_GB300_H
+#define PO_GB300_H
+
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- ABI structs (same layout as the reference's) ---------------------- */
+
+typedef struct arrC1 { double *x, *y; } arrC1;
+typedef struct arrC1f { float *x, *y; } arrC1f;
+
+typedef struct c2Bundle {
+    double *r1x, *r1y, *r1z, *i1x, *i1y, *i1z;
+    double *r2x, *r2y, *r2z, *i2x, *i2y, *i2z;
+} c2Bundle;
+typedef struct c2Bundlef {
+    float *r1x, *r1y, *r1z, *i1x, *i1y, *i1z;
+    float *r2x, *r2y, *r2z, *i2x, *i2y, *i2z;
+} c2Bundlef;
+
+typedef struct c4Bundlef {
+    float *r1x, *r1y, *r1z, *i1x, *i1y, *i1z;
+    float *r2x, *r2y, *r2z, *i2x, *i2y, *i2z;
+    float *r3x, *r3y, *r3z, *i3x, *i3y, *i3z;
+    float *r4x, *r4y, *r4z, *i4x, *i4y, *i4z;
+} c4Bundlef;
+
+typedef struct c2rBundlef {
+    float *r1x, *r1y, *r1z, *i1x, *i1y, *i1z;
+    float *r2x, *r2y, *r2z, *i2x, *i2y, *i2z;
+    float *r3x, *r3y, *r3z;
+} c2rBundlef;
+
+typedef struct reflparams {
+    double *coeffs;
+    double *lxu;
+    double *lyv;
+    int *n_cells;
+    bool flip;
+    int gmode;
+    double *gcenter;
+    double ecc_uv;
+    double rot_uv;
+    int type;
+    double *transf;
+    double rms;
+    unsigned int rms_seed;
+} reflparams;
+
+typedef struct reflparamsf {
+    float *coeffs;
+    float *lxu;
+    float *lyv;
+    int *n_cells;
+    bool flip;
+    int gmode;
+    float *gcenter;
+    float ecc_uv;
+    float rot_uv;
+    int type;
+    float *transf;
+    float rms;
+    unsigned int rms_seed;
+} reflparamsf;
+
+typedef struct reflcontainer {
+    int size;
+    double *x, *y, *z, *nx, *ny, *nz, *area;
+} reflcontainer;
+
+typedef struct reflcontainerf {
+    int size;
+    float *x, *y, *z, *nx, *ny, *nz, *area;
+} reflcontainerf;
+
+/* ---- errors ------------------------------------------------------------- */
+
+/* Message of the last failed call on this thread ("" when none). */
+const char *po_last_error(void);
+
+/* ---- drop-in replacements for the reference's libpypogpu ----------------
+ * Same signatures as reference src/CUDA/InterfaceCUDA.h:31-64 (ctypes
+ * argtypes src/PyPO/BindGPU.py:34-74), called from BindGPU.PyPO_GPUf
+ * (src/PyPO/BindGPU.py:83-224). Like the reference they generate the source
+ * and target grids from the reflparamsf into cs / ct (here in FP64, then
+ * stored as float), and fill res. nBlocks / nThreads are accepted and
+ * ignored: the engine picks its own tiling. Computation is mixed precision
+ * (FP32 bulk, split hi/lo separation and phase). The reference returns void;
+ * these return the status (ctypes restype None ignores it).
+ */
+int callKernelf_JM(c2Bundlef *res, reflparamsf source, reflparamsf target,
+                   reflcontainerf *cs, reflcontainerf *ct, c2Bundlef *currents,
+                   float k, float epsilon, float t_direction, int nBlocks, int nThreads);
+    /* replaces Kernelsf.cu:1636-1706 */
+int callKernelf_EH(c2Bundlef *res, reflparamsf source, reflparamsf target,
+                   reflcontainerf *cs, reflcontainerf *ct, c2Bundlef *currents,
+                   float k, float epsilon, float t_direction, int nBlocks, int nThreads);
+    /* replaces Kernelsf.cu:1729-1797 */
+int callKernelf_JMEH(c4Bundlef *res, reflparamsf source, reflparamsf target,
+                     reflcontainerf *cs, reflcontainerf *ct, c2Bundlef *currents,
+                     float k, float epsilon, float t_direction, int nBlocks, int nThreads);
+    /* replaces Kernelsf.cu:1821-1895 */
+int callKernelf_EHP(c2rBundlef *res, reflparamsf source, reflparamsf target,
+                    reflcontainerf *cs, reflcontainerf *ct, c2Bundlef *currents,
+                    float k, float epsilon, float t_direction, int nBlocks, int nThreads);
+    /* replaces Kernelsf.cu:1919-2000 */
+int callKernelf_FF(c2Bundlef *res, reflparamsf source, reflparamsf target,
+                   reflcontainerf *cs, reflcontainerf *ct, c2Bundlef *currents,
+                   float k, float epsilon, float t_direction, int nBlocks, int nThreads);
+    /* replaces Kernelsf.cu:2023-2090 */
+int callKernelf_scalar(arrC1f *res, reflparamsf source, reflparamsf target,
+                       reflcontainerf *cs, reflcontainerf *ct, arrC1f *inp,
+                       float k, float epsilon, float t_direction, int nBlocks, int nThreads);
+    /* replaces Kernelsf.cu:2113-2175 */
+
+/* ---- FP64 grid generation ------------------------------------------------
+ * Same contract as the reference's generateGrid (src/common/InterfaceReflector.h:24-25,
+ * src/common/InterfaceReflector.cpp:882-972): fills container (size
+ * n_cells[0]*n_cells[1], row-major over (x/u, y/v)) with points, unit
+ * normals and area elements, applies the 4x4 transform when `transform`,
+ * maps AoE grids to (polar, azimuth) radians when `spheric`, and adds the
+ * uncorrelated normal-direction surface error when rms > 0.
+ */
+int po_generate_grid(reflparams refl, reflcontainer *container, int transform, int spheric);
+
+/* ---- explicit-grid, double-precision entry (host buffers) ---------------
+ * New; the reference has no equivalent (its C-ABI regenerates grids inside
+ * every call, Kernelsf.cu:1643-1644, so it cannot take perturbed surfaces or
+ * target subsets, and its float ABI rounds positions, BindUtils.py:277-328).
+ *
+ *   src7  7*ns doubles, rows x y z nx ny nz area (row-major over (ncx, ncy))
+ *   cur   12*ns doubles in c2Bundle row order (r1x r1y r1z i1x i1y i1z
+ *         r2x ... i2z: J then M), or 2*ns (re, im) for scalar mode
+ *   tgt7  7*nt doubles, rows x y z nx ny nz area; for FF x is the polar
+ *         angle and y the azimuth (radians), as the reference's AoE grid
+ *   out   po_n_out(mode)*nt doubles in bundle row order
+ *   precision  0 mixed (FP32 bulk + split hi/lo phase), 1 plain FP64
+ */
+int po_n_out(int mode);
+int po_run_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
+             const double *cur, long nt, const double *tgt7,
+             double k, double epsilon, double t_direction, int precision, double *out);
+
+/* ---- device-pointer entry ------------------------------------------------
+ * As po_run_d, but every array is device memory and the work is queued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream). The call returns
+ * once the work is queued; device scratch is stream-ordered.
+ * flags bit 0: caller guarantees M == 0 (JM outputs, PEC chains), which
+ * selects the kernel variant that skips the magnetic-current terms.
+ */
+int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
+               const double *cur, long nt, const double *tgt7,
+               double k, double epsilon, double t_direction, int precision, int flags,
+               double *out, void *stream);
+
+/* Number of kernel launches the last call on this thread queued. */
+int po_last_launches(void);
+
+/* Synchronises `stream`, then returns (and clears) the device error word in
+ * *code: 0 when every kernel finished normally, 101 when a kernel gave up a
+ * bounded wait for a tile copy (its results are then invalid). */
+int po_device_error(void *stream, int *code);
+
+/* ---- measurement support --------------------------------------------------
+ * po_timing_enable(n) arms n CUDA event pairs, recorded on the launching
+ * stream around each subsequent main-kernel launch (mixed or FP64);
+ * po_timing_collect copies up to `max` durations in ms (in launch order,
+ * synchronising on the events) and re-arms. n = 0 disables. */
+int po_timing_enable(int slots);
+int po_timing_collect(float *ms, int max);
+
+/* FP32 FFMA throughput probe: `blocks` x 256 threads, each running 8
+ * independent FMA chains for `iters` steps (16 flops per thread-step); out
+ * holds blocks*256 floats (device). Queued on `stream`. */
+int po_fp32_probe(int blocks, int iters, float *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PO_GB300_H */

@@ -1,0 +1,344 @@
+// po_capi.cu -- the extern "C" entry points of libpo_gb300 (include/po_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "po_internal.h"
+
+namespace {
+
+using po::fail;
+
+std::mutex g_stream_mu;
+cudaStream_t g_streams[64] = {};
+
+// Private non-blocking stream of the host-buffer entry points, one per device.
+int lib_stream(cudaStream_t *s)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(2, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) return fail(2, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_stream_mu);
+    if (!g_streams[dev]) {
+        e = cudaStreamCreateWithFlags(&g_streams[dev], cudaStreamNonBlocking);
+        if (e != cudaSuccess) return fail(2, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    *s = g_streams[dev];
+    return 0;
+}
+
+bool m_is_zero(const double *cur, long ns)
+{
+    for (long i = 6 * ns; i < 12 * ns; ++i)
+        if (cur[i] != 0.0) return false;
+    return true;
+}
+
+#define CK(expr)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            rc = fail(2, std::string(#expr) + ": " + cudaGetErrorString(e_));             \
+            goto done;                                                                    \
+        }                                                                                 \
+    } while (0)
+
+// Host buffers in, host buffers out; synchronous.
+int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
+             const double *tgt7, double k, double eps, double t, int precision, double *out)
+{
+    po::clear_error();
+    {
+        po::RunArgs v;
+        v.mode = mode;
+        v.ns = ns;
+        v.src7 = src7;
+        v.gmode = gmode;
+        v.ncx = ncx;
+        v.ncy = ncy;
+        v.cur = cur;
+        v.nt = nt;
+        v.tgt7 = tgt7;
+        v.k = k;
+        v.epsilon = eps;
+        v.t_dir = t;
+        v.precision = precision;
+        v.out = out;
+        if (int rc = po::validate(v)) return rc;
+    }
+    if (nt == 0) return 0;
+    const int ncur = mode == po::kScalar ? 2 : 12;
+    const int nout = po::n_out(mode);
+    cudaStream_t s = nullptr;
+    if (int rc = lib_stream(&s)) return rc;
+    double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_out = nullptr;
+    int rc = 0, code = 0;
+    po::RunArgs a;
+    CK(cudaMallocAsync(&d_src, sizeof(double) * 7 * std::max(ns, 1L), s));
+    CK(cudaMallocAsync(&d_cur, sizeof(double) * ncur * std::max(ns, 1L), s));
+    CK(cudaMallocAsync(&d_tgt, sizeof(double) * 7 * nt, s));
+    CK(cudaMallocAsync(&d_out, sizeof(double) * nout * nt, s));
+    if (ns > 0) {
+        CK(cudaMemcpyAsync(d_src, src7, sizeof(double) * 7 * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_cur, cur, sizeof(double) * ncur * ns, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(d_tgt, tgt7, sizeof(double) * 7 * nt, cudaMemcpyHostToDevice, s));
+    a.mode = mode;
+    a.ns = ns;
+    a.src7 = d_src;
+    a.gmode = gmode;
+    a.ncx = ncx;
+    a.ncy = ncy;
+    a.cur = d_cur;
+    a.nt = nt;
+    a.tgt7 = d_tgt;
+    a.k = k;
+    a.epsilon = eps;
+    a.t_dir = t;
+    a.precision = precision;
+    a.m_zero = mode != po::kScalar && ns > 0 && m_is_zero(cur, ns);
+    a.out = d_out;
+    a.stream = s;
+    rc = po::run_device(a);
+    if (rc) goto done;
+    CK(cudaMemcpyAsync(out, d_out, sizeof(double) * nout * nt, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    rc = po::read_device_error(s, &code);
+    if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
+                                      std::to_string(code) + "); results are invalid");
+done:
+    if (d_src) cudaFreeAsync(d_src, s);
+    if (d_cur) cudaFreeAsync(d_cur, s);
+    if (d_tgt) cudaFreeAsync(d_tgt, s);
+    if (d_out) cudaFreeAsync(d_out, s);
+    if (s) cudaStreamSynchronize(s);
+    return rc;
+}
+
+// reflparamsf -> reflparams with owned double arrays.
+struct Widened {
+    double coeffs[3], lxu[2], lyv[2], gcenter[2], transf[16];
+    reflparams r;
+};
+
+void widen(const reflparamsf &f, Widened &w)
+{
+    for (int i = 0; i < 3; ++i) w.coeffs[i] = f.coeffs ? f.coeffs[i] : 0.0;
+    for (int i = 0; i < 2; ++i) {
+        w.lxu[i] = f.lxu[i];
+        w.lyv[i] = f.lyv[i];
+        w.gcenter[i] = f.gcenter ? f.gcenter[i] : 0.0;
+    }
+    for (int i = 0; i < 16; ++i) w.transf[i] = f.transf ? f.transf[i] : (i % 5 == 0 ? 1.0 : 0.0);
+    w.r.coeffs = w.coeffs;
+    w.r.lxu = w.lxu;
+    w.r.lyv = w.lyv;
+    w.r.n_cells = f.n_cells;
+    w.r.flip = f.flip;
+    w.r.gmode = f.gmode;
+    w.r.gcenter = w.gcenter;
+    w.r.ecc_uv = f.ecc_uv;
+    w.r.rot_uv = f.rot_uv;
+    w.r.type = f.type;
+    w.r.transf = w.transf;
+    w.r.rms = f.rms;
+    w.r.rms_seed = f.rms_seed;
+}
+
+int make_grid(const reflparamsf &pf, std::vector<double> &g7, reflcontainerf *cf)
+{
+    if (!pf.n_cells || !pf.lxu || !pf.lyv) return fail(1, "reflparamsf has null arrays");
+    const long n = (long)pf.n_cells[0] * pf.n_cells[1];
+    if (n <= 0) return fail(1, "empty grid");
+    Widened w;
+    widen(pf, w);
+    g7.assign(7 * n, 0.0);
+    reflcontainer c;
+    c.size = (int)n;
+    c.x = g7.data();
+    c.y = c.x + n;
+    c.z = c.y + n;
+    c.nx = c.z + n;
+    c.ny = c.nx + n;
+    c.nz = c.ny + n;
+    c.area = c.nz + n;
+    if (po_grid_fill(w.r, &c, true, true)) return fail(1, "grid generation failed (bad gmode or sizes)");
+    if (cf && cf->x) {
+        float *dst[7] = {cf->x, cf->y, cf->z, cf->nx, cf->ny, cf->nz, cf->area};
+        for (int r = 0; r < 7; ++r)
+            if (dst[r])
+                for (long i = 0; i < n; ++i) dst[r][i] = (float)g7[r * n + i];
+    }
+    return 0;
+}
+
+// Shared body of the callKernelf_* drop-ins: FP64 grids, widened inputs,
+// mixed-precision run, float outputs into the caller's bundle rows.
+int drop_in(int mode, float *const *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
+            reflcontainerf *ct, float *const *inp, float k, float epsilon, float t)
+{
+    po::clear_error();
+    std::vector<double> s7, t7;
+    if (int rc = make_grid(source, s7, cs)) return rc;
+    if (int rc = make_grid(target, t7, ct)) return rc;
+    const long ns = (long)source.n_cells[0] * source.n_cells[1];
+    const long nt = (long)target.n_cells[0] * target.n_cells[1];
+    const int ncur = mode == po::kScalar ? 2 : 12;
+    std::vector<double> cur((size_t)ncur * ns);
+    for (int r = 0; r < ncur; ++r) {
+        if (!inp[r]) return fail(1, "null current array");
+        for (long i = 0; i < ns; ++i) cur[r * ns + i] = inp[r][i];
+    }
+    const int nout = po::n_out(mode);
+    std::vector<double> out((size_t)nout * nt);
+    int rc = run_host(mode, ns, s7.data(), source.gmode, source.n_cells[0], source.n_cells[1], cur.data(), nt,
+                      t7.data(), (double)k, (double)epsilon, (double)t, 0, out.data());
+    if (rc) return rc;
+    for (int r = 0; r < nout; ++r) {
+        if (!res[r]) return fail(1, "null result array");
+        for (long i = 0; i < nt; ++i) res[r][i] = (float)out[r * nt + i];
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *po_last_error(void) { return po::last_error(); }
+
+int po_n_out(int mode) { return po::n_out(mode); }
+
+int po_last_launches(void) { return po::last_launches(); }
+
+int po_generate_grid(reflparams refl, reflcontainer *container, int transform, int spheric)
+{
+    po::clear_error();
+    if (po_grid_fill(refl, container, transform != 0, spheric != 0))
+        return fail(1, "grid generation failed (bad gmode, sizes or null container)");
+    return 0;
+}
+
+int po_run_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
+             const double *tgt7, double k, double epsilon, double t_direction, int precision, double *out)
+{
+    return run_host(mode, ns, src7, gmode, ncx, ncy, cur, nt, tgt7, k, epsilon, t_direction, precision, out);
+}
+
+int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
+               const double *tgt7, double k, double epsilon, double t_direction, int precision, int flags,
+               double *out, void *stream)
+{
+    po::clear_error();
+    po::RunArgs a;
+    a.mode = mode;
+    a.ns = ns;
+    a.src7 = src7;
+    a.gmode = gmode;
+    a.ncx = ncx;
+    a.ncy = ncy;
+    a.cur = cur;
+    a.nt = nt;
+    a.tgt7 = tgt7;
+    a.k = k;
+    a.epsilon = epsilon;
+    a.t_dir = t_direction;
+    a.precision = precision;
+    a.m_zero = (flags & 1) != 0;
+    a.out = out;
+    a.stream = static_cast<cudaStream_t>(stream);
+    return po::run_device(a);
+}
+
+int po_timing_enable(int slots)
+{
+    po::clear_error();
+    return po::timing_enable(slots);
+}
+
+int po_timing_collect(float *ms, int max) { return po::timing_collect(ms, max); }
+
+int po_fp32_probe(int blocks, int iters, float *out, void *stream)
+{
+    po::clear_error();
+    if (blocks < 1 || iters < 1 || !out) return fail(1, "po_fp32_probe: bad arguments");
+    void *args[] = {&iters, nullptr, &out};
+    float seed = 1.0f;
+    args[1] = &seed;
+    cudaError_t e = cudaLaunchKernel(po::fp32_probe_kernel(), dim3(blocks), dim3(256), args, 0,
+                                     static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(2, std::string("po_fp32_probe: ") + cudaGetErrorString(e));
+    po::note_launches(1);
+    return 0;
+}
+
+int po_device_error(void *stream, int *code)
+{
+    po::clear_error();
+    return po::read_device_error(static_cast<cudaStream_t>(stream), code);
+}
+
+#define ROWS12(b) {b->r1x, b->r1y, b->r1z, b->i1x, b->i1y, b->i1z, b->r2x, b->r2y, b->r2z, b->i2x, b->i2y, b->i2z}
+
+int callKernelf_JM(c2Bundlef *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
+                   reflcontainerf *ct, c2Bundlef *currents, float k, float epsilon, float t_direction, int, int)
+{
+    if (!res || !currents) return fail(1, "null bundle");
+    float *r[12] = ROWS12(res);
+    float *c[12] = ROWS12(currents);
+    return drop_in(po::kJM, r, source, target, cs, ct, c, k, epsilon, t_direction);
+}
+
+int callKernelf_EH(c2Bundlef *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
+                   reflcontainerf *ct, c2Bundlef *currents, float k, float epsilon, float t_direction, int, int)
+{
+    if (!res || !currents) return fail(1, "null bundle");
+    float *r[12] = ROWS12(res);
+    float *c[12] = ROWS12(currents);
+    return drop_in(po::kEH, r, source, target, cs, ct, c, k, epsilon, t_direction);
+}
+
+int callKernelf_JMEH(c4Bundlef *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
+                     reflcontainerf *ct, c2Bundlef *currents, float k, float epsilon, float t_direction, int, int)
+{
+    if (!res || !currents) return fail(1, "null bundle");
+    float *r[24] = {res->r1x, res->r1y, res->r1z, res->i1x, res->i1y, res->i1z, res->r2x, res->r2y,
+                    res->r2z, res->i2x, res->i2y, res->i2z, res->r3x, res->r3y, res->r3z, res->i3x,
+                    res->i3y, res->i3z, res->r4x, res->r4y, res->r4z, res->i4x, res->i4y, res->i4z};
+    float *c[12] = ROWS12(currents);
+    return drop_in(po::kJMEH, r, source, target, cs, ct, c, k, epsilon, t_direction);
+}
+
+int callKernelf_EHP(c2rBundlef *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
+                    reflcontainerf *ct, c2Bundlef *currents, float k, float epsilon, float t_direction, int, int)
+{
+    if (!res || !currents) return fail(1, "null bundle");
+    float *r[15] = {res->r1x, res->r1y, res->r1z, res->i1x, res->i1y, res->i1z, res->r2x, res->r2y,
+                    res->r2z, res->i2x, res->i2y, res->i2z, res->r3x, res->r3y, res->r3z};
+    float *c[12] = ROWS12(currents);
+    return drop_in(po::kEHP, r, source, target, cs, ct, c, k, epsilon, t_direction);
+}
+
+int callKernelf_FF(c2Bundlef *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
+                   reflcontainerf *ct, c2Bundlef *currents, float k, float epsilon, float t_direction, int, int)
+{
+    if (!res || !currents) return fail(1, "null bundle");
+    float *r[12] = ROWS12(res);
+    float *c[12] = ROWS12(currents);
+    return drop_in(po::kFF, r, source, target, cs, ct, c, k, epsilon, t_direction);
+}
+
+int callKernelf_scalar(arrC1f *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
+                       reflcontainerf *ct, arrC1f *inp, float k, float epsilon, float t_direction, int, int)
+{
+    if (!res || !inp) return fail(1, "null array");
+    float *r[2] = {res->x, res->y};
+    float *c[2] = {inp->x, inp->y};
+    return drop_in(po::kScalar, r, source, target, cs, ct, c, k, epsilon, t_direction);
+}
+
+}  // extern "C"

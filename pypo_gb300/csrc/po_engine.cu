@@ -1,0 +1,346 @@
+// po_engine.cu -- host orchestration of one propagation on device buffers.
+//
+// Mixed precision (precision 0):
+//   bbox -> frame -> pack sources / targets -> main N-body kernel over a
+//   (target block, source chunk) grid -> FP64 epilogue summing the chunks.
+// Plain FP64 (precision 1):
+//   pack sources (double) -> one-thread-per-target FP64 direct sum -> epilogue.
+// Scratch is stream-ordered (cudaMallocAsync / cudaFreeAsync) on the caller's
+// stream; nothing here synchronises the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "po_internal.h"
+#include "po_kernels.cuh"
+
+namespace po {
+
+namespace {
+
+thread_local std::string t_err;
+thread_local int t_launches = 0;
+
+struct DeviceInfo {
+    bool ready = false;
+    int sms = 0;
+    int occ[3][2][2] = {};   // [kind][t>0][has_m] resident CTAs per SM
+};
+
+std::mutex g_mu;
+DeviceInfo g_dev[64];
+
+// Timing ring: CUDA event pairs recorded around each main-kernel launch.
+struct Timing {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;   // 2 per slot
+    int used = 0;
+};
+Timing g_timing;
+
+const char *err_str(cudaError_t e) { return cudaGetErrorString(e); }
+
+}  // namespace
+
+int fail(int code, const std::string &msg)
+{
+    t_err = msg;
+    return code;
+}
+
+void clear_error()
+{
+    t_err.clear();
+    t_launches = 0;
+}
+
+void note_launches(int n) { t_launches += n; }
+
+const char *last_error() { return t_err.c_str(); }
+int last_launches() { return t_launches; }
+
+int n_out(int mode)
+{
+    static const int n[6] = {12, 12, 24, 15, 12, 2};
+    return (mode >= 0 && mode < 6) ? n[mode] : -1;
+}
+
+#define PO_CK(expr)                                                                         \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess) return fail(2, std::string(#expr) + ": " + err_str(e_));     \
+    } while (0)
+
+static int device_info(DeviceInfo *&out)
+{
+    int dev = 0;
+    PO_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(2, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    DeviceInfo &di = g_dev[dev];
+    if (!di.ready) {
+        PO_CK(cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev));
+        for (int kind = 0; kind < 3; ++kind)
+            for (int ts = 0; ts < 2; ++ts)
+                for (int hm = 0; hm < 2; ++hm) {
+                    if (kind == kKindScalar && hm) continue;
+                    void *fn = main_kernel(kind, ts ? 1 : -1, hm != 0);
+                    const int smem = main_smem_bytes(kind);
+                    PO_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+                    int nb = 0;
+                    PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
+                    di.occ[kind][ts][hm] = std::max(nb, 1);
+                }
+        di.ready = true;
+    }
+    out = &di;
+    return 0;
+}
+
+// Number of source chunks: minimise waves * chunk length, given `slots`
+// resident CTAs, with a small cost per extra chunk (partials, prologue) and
+// the partial buffer capped near 1 GiB.
+static long choose_split(long ntb, long ns, long slots, long nt, int nacc)
+{
+    const long tiles = std::max(1L, (ns + kTile - 1) / kTile);
+    const long cap = std::max(1L, (1L << 30) / std::max(1L, nt * nacc * 8));
+    long best = 1;
+    double best_cost = 1e300;
+    for (long s = 1; s <= std::min(tiles, std::min(cap, 1024L)); ++s) {
+        const long chunk = (tiles + s - 1) / s;
+        const long real = (tiles + chunk - 1) / chunk;
+        if (real != s) continue;
+        const long waves = (ntb * real + slots - 1) / slots;
+        const double cost = (double)waves * chunk + 0.05 * real;
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            best = real;
+        }
+    }
+    return best;
+}
+
+template <typename T>
+static int salloc(T **p, size_t count, cudaStream_t s, std::vector<void *> &owned)
+{
+    void *q = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    cudaError_t e = cudaMallocAsync(&q, bytes, s);
+    if (e != cudaSuccess) return fail(3, std::string("device scratch allocation failed: ") + err_str(e));
+    owned.push_back(q);
+    *p = static_cast<T *>(q);
+    return 0;
+}
+
+static void sfree(std::vector<void *> &owned, cudaStream_t s)
+{
+    for (void *q : owned) cudaFreeAsync(q, s);
+    owned.clear();
+}
+
+static int launch(void *fn, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t s)
+{
+    if (grid.x == 0 || grid.y == 0) return 0;
+    PO_CK(cudaLaunchKernel(fn, grid, block, args, smem, s));
+    note_launches(1);
+    return 0;
+}
+
+static void timing_mark(cudaStream_t s, bool begin)
+{
+    if (!g_timing.on) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    const int slots = (int)g_timing.ev.size() / 2;
+    if (slots == 0) return;
+    if (begin) {
+        if (g_timing.used >= slots) return;
+        cudaEventRecord(g_timing.ev[2 * g_timing.used], s);
+    } else {
+        if (g_timing.used >= slots) return;
+        cudaEventRecord(g_timing.ev[2 * g_timing.used + 1], s);
+        ++g_timing.used;
+    }
+}
+
+int timing_enable(int slots)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (cudaEvent_t e : g_timing.ev) cudaEventDestroy(e);
+    g_timing.ev.clear();
+    g_timing.used = 0;
+    g_timing.on = slots > 0;
+    for (int i = 0; i < 2 * std::max(slots, 0); ++i) {
+        cudaEvent_t e;
+        PO_CK(cudaEventCreate(&e));
+        g_timing.ev.push_back(e);
+    }
+    return 0;
+}
+
+int timing_collect(float *ms, int max)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    int n = std::min(g_timing.used, max);
+    for (int i = 0; i < n; ++i) {
+        PO_CK(cudaEventSynchronize(g_timing.ev[2 * i + 1]));
+        PO_CK(cudaEventElapsedTime(&ms[i], g_timing.ev[2 * i], g_timing.ev[2 * i + 1]));
+    }
+    g_timing.used = 0;
+    return n;
+}
+
+// Persistent per-device error word, written by kernels that give up a wait.
+static int *error_word()
+{
+    static int *words[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!words[dev]) {
+        if (cudaMalloc(&words[dev], sizeof(int)) != cudaSuccess) return nullptr;
+        if (cudaMemset(words[dev], 0, sizeof(int)) != cudaSuccess) return nullptr;
+    }
+    return words[dev];
+}
+
+int read_device_error(cudaStream_t s, int *code)
+{
+    int *w = error_word();
+    if (!w) return fail(2, "no device error word");
+    PO_CK(cudaStreamSynchronize(s));
+    PO_CK(cudaMemcpy(code, w, sizeof(int), cudaMemcpyDeviceToHost));
+    PO_CK(cudaMemset(w, 0, sizeof(int)));
+    return 0;
+}
+
+int validate(const RunArgs &a)
+{
+    if (a.mode < 0 || a.mode > 5) return fail(1, "mode must be 0..5 (JM EH JMEH EHP FF scalar)");
+    if (a.ns < 0 || a.nt < 0) return fail(1, "negative size");
+    if (a.ns > 0 && a.gmode >= 0 && (a.ncx < 1 || a.ncy < 1)) return fail(1, "bad source grid shape");
+    if (a.ns > 0 && a.gmode >= 0 && (long)a.ncx * a.ncy != a.ns)
+        return fail(1, "ncx * ncy must equal the number of source points");
+    if (!(a.t_dir == 1.0 || a.t_dir == -1.0)) return fail(1, "t_direction must be -1 (fwd) or +1 (bwd)");
+    if (!(a.k > 0.0) || !std::isfinite(a.k)) return fail(1, "wavenumber k must be positive and finite");
+    if (a.precision != 0 && a.precision != 1) return fail(1, "precision must be 0 (mixed) or 1 (fp64)");
+    if (a.nt > 0 && ((a.ns > 0 && (!a.src7 || !a.cur)) || !a.tgt7 || !a.out)) return fail(1, "null buffer");
+    return 0;
+}
+
+int run_device(const RunArgs &a)
+{
+    if (int rc = validate(a)) return rc;
+    if (a.nt == 0) return 0;
+
+    DeviceInfo *di = nullptr;
+    if (int rc = device_info(di)) return rc;
+    int *err = error_word();
+    if (!err) return fail(2, "could not allocate the device error word");
+
+    const int kind = a.mode == kFF ? kKindFF : (a.mode == kScalar ? kKindScalar : kKindNF);
+    const int nacc = kind == kKindScalar ? 2 : kAcc;
+    const double pif = (double)3.14159265359f;   // the reference's float-literal pi
+    const double pref = a.k * a.k / (4.0 * pif);
+    const double kappa = a.k / (2.0 * 3.14159265358979323846);
+    const double c_l = (double)2.99792458e8f, mu0 = (double)1.2566370614e-6f;
+    const double eps = a.epsilon * (1.0 / (mu0 * c_l * c_l));
+    const double zeta_inv = 1.0 / std::sqrt(mu0 / eps);
+    const int ts = a.t_dir > 0 ? 1 : -1;
+    cudaStream_t s = a.stream;
+
+    // Complex factor folded into each source's weighted current.
+    double fac_re = pref, fac_im = 0.0;
+    if (kind == kKindFF) { fac_re = 0.0; fac_im = -pref; }
+    if (kind == kKindScalar) {
+        fac_re = -pref * (a.precision == 0 ? kappa : 1.0);
+        fac_im = 0.0;
+    }
+
+    std::vector<void *> owned;
+    int rc = 0;
+    const unsigned nblk_s = (unsigned)((a.ns + 255) / 256), nblk_t = (unsigned)((a.nt + 255) / 256);
+    long nt = a.nt, ns = a.ns;
+    int mode = a.mode;
+    double t = a.t_dir;
+    const int scalar = kind == kKindScalar;
+    const double *src7 = a.src7, *cur = a.cur, *tgt7 = a.tgt7;
+    int gmode = a.gmode, ncx = a.ncx, ncy = a.ncy;
+    double *out = a.out;
+
+    if (a.precision == 1) {
+        double *srcd = nullptr, *part = nullptr;
+        if ((rc = salloc(&srcd, (size_t)std::max(ns, 1L) * kRecD, s, owned)) ||
+            (rc = salloc(&part, (size_t)nacc * nt, s, owned))) {
+            sfree(owned, s);
+            return rc;
+        }
+        void *pargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &fac_re, &fac_im, (void *)&scalar, &srcd};
+        if (ns > 0) rc = launch(pack_src_d_kernel(), dim3(nblk_s), dim3(256), pargs, 0, s);
+        double k = a.k;
+        void *fargs[] = {&srcd, &ns, &tgt7, &nt, &k, &t, &part};
+        timing_mark(s, true);
+        if (!rc) rc = launch(fp64_kernel(kind), dim3((unsigned)((nt + kThreadsD - 1) / kThreadsD)),
+                             dim3(kThreadsD), fargs, 0, s);
+        timing_mark(s, false);
+        int one = 1;
+        double zi = zeta_inv;
+        void *eargs[] = {&mode, &one, &nt, &part, &tgt7, &t, &zi, &out};
+        if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
+        sfree(owned, s);
+        return rc;
+    }
+
+    // ---- mixed precision
+    double *bbox = nullptr;
+    Frame *frame = nullptr;
+    float4 *srcpk = nullptr, *tgtpk = nullptr;
+    double *part = nullptr;
+    const int rec = scalar ? kRecScalar : kRec;
+    const long ntb = (nt + (long)kThreads * kTPT - 1) / ((long)kThreads * kTPT);
+    const int occ = di->occ[kind][ts > 0][(kind != kKindScalar && !a.m_zero) ? 1 : 0];
+    const long nsplit = choose_split(ntb, ns, (long)di->sms * occ, nt, nacc);
+    const long tiles = std::max(1L, (ns + kTile - 1) / kTile);
+    long chunk = ((tiles + nsplit - 1) / nsplit) * kTile;
+    if ((rc = salloc(&bbox, (size_t)kBboxBlocks * 6, s, owned)) || (rc = salloc(&frame, 1, s, owned)) ||
+        (rc = salloc(&srcpk, (size_t)std::max(ns, 1L) * rec, s, owned)) ||
+        (rc = salloc(&tgtpk, (size_t)nt * 2, s, owned)) ||
+        (rc = salloc(&part, (size_t)nsplit * nacc * nt, s, owned))) {
+        sfree(owned, s);
+        return rc;
+    }
+    // Frame: far field keeps the coordinate origin (it is the phase reference).
+    const bool far = kind == kKindFF;
+    long nb = far ? 0 : nt;   // sources, plus targets for the near field
+    void *bargs[] = {&src7, &ns, &tgt7, &nb, &bbox};
+    rc = launch(bbox_kernel(), dim3(kBboxBlocks), dim3(kBboxThreads), bargs, 0, s);
+    int nbb = kBboxBlocks;
+    double kap = kappa;
+    int centred = far ? 0 : 1;
+    void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
+    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
+    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcpk};
+    if (!rc && ns > 0) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
+    int farflag = far ? 1 : 0;
+    void *ptargs[] = {&nt, &tgt7, &frame, &farflag, &tgtpk};
+    if (!rc) rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
+    const float4 *srcc = srcpk, *tgtc = tgtpk;
+    void *margs[] = {&srcc, &ns, &chunk, &tgtc, &nt, &part, &err};
+    timing_mark(s, true);
+    if (!rc)
+        rc = launch(main_kernel(kind, ts, kind != kKindScalar && !a.m_zero), dim3((unsigned)ntb, (unsigned)nsplit),
+                    dim3(kThreads), margs, main_smem_bytes(kind), s);
+    timing_mark(s, false);
+    int nspl = (int)nsplit;
+    double zi = zeta_inv;
+    void *eargs[] = {&mode, &nspl, &nt, &part, &tgt7, &t, &zi, &out};
+    if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
+    sfree(owned, s);
+    return rc;
+}
+
+}  // namespace po

@@ -1,0 +1,50 @@
+// po_internal.h -- shared declarations of libpo_gb300's host code.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/po_gb300.h"
+#include "po_kernels.cuh"
+
+namespace po {
+
+// One propagation on device buffers. All pointers are device memory.
+struct RunArgs {
+    int mode = kEH;
+    long ns = 0;
+    const double *src7 = nullptr;  // 7 rows x ns
+    int gmode = 0, ncx = 0, ncy = 0;
+    const double *cur = nullptr;   // 12 rows (or 2 for scalar) x ns
+    long nt = 0;
+    const double *tgt7 = nullptr;  // 7 rows x nt
+    double k = 1.0, epsilon = 1.0, t_dir = -1.0;
+    int precision = 0;             // 0 mixed, 1 plain FP64
+    bool m_zero = false;           // M == 0 on the source
+    double *out = nullptr;         // n_out(mode) rows x nt
+    cudaStream_t stream = nullptr;
+};
+
+int n_out(int mode);
+int validate(const RunArgs &a);   // argument checks only, no CUDA calls
+int run_device(const RunArgs &a);
+
+// Thread-local error reporting.
+int fail(int code, const std::string &msg);
+void clear_error();
+void note_launches(int n);
+
+const char *last_error();
+int last_launches();
+
+// Measurement hook: CUDA event pairs recorded on the launching stream around
+// every main-kernel launch, read back (synchronising) by timing_collect.
+int timing_enable(int slots);
+int timing_collect(float *ms, int max);
+
+// Synchronises `s`, returns and clears the device error word (wait timeouts).
+int read_device_error(cudaStream_t s, int *code);
+
+}  // namespace po
+
+int po_grid_fill(const reflparams &r, reflcontainer *c, bool transform, bool spheric);

@@ -1,0 +1,833 @@
+// po_kernels.cu -- sm_103a kernels of the physical-optics integrator.
+//
+// The O(Ns*Nt) radiation integral of reference src/CPU/Propagation.h:977-1144
+// (near field), :1656-1781 (far field) and :1279-1331 (scalar), written as an
+// N-body kernel:
+//
+//   * sources are packed once into 96-byte records (po_pack_src): positions
+//     in "turn" units (mm * k / 2 pi) relative to a frame origin, split into
+//     a hi part on a power-of-two quantum q (few significant bits, so that
+//     differences and squares of hi parts are exact in FP32) and a small lo
+//     part; the unit normal; and the currents pre-multiplied by the trapezoid
+//     weight, the area element and the Green's-function prefactor;
+//   * a CTA owns NTH*TPT targets held in registers and walks its share of the
+//     sources tile by tile; tiles are staged into shared memory by 1-D TMA
+//     bulk copies (cp.async.bulk) completing on mbarriers, STAGES deep;
+//   * per pair: exact hi separation + lo correction, R^2 exact-plus-small,
+//     R = Rh + Rl by one Newton step with an exact FMA residual, phase
+//     reduction mod 1 turn on (Rh, Rl), sin/cos of the reduced angle only,
+//     everything else in FP32;
+//   * each tile's FP32 partial is folded into a float-float total (two-sum),
+//     so long oscillatory sums stay compensated;
+//   * a source chunk (blockIdx.y) writes its totals as doubles; the epilogue
+//     kernel adds the chunks in a fixed order and applies the mode's physics
+//     (PEC current, EHP reflection, far-field projection) in FP64.
+//
+// The plain FP64 direct sum (po_fp64_kernel) is the comparison path: same
+// formulas, double everywhere, no splitting.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <cstdint>
+
+#include "po_kernels.cuh"
+
+namespace po {
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: gives up after kWaitLimit polls (each poll may itself block
+// for a bounded hardware time slice) and reports false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Error-free transformation: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Round-to-nearest integer of |x| < 2^22 without the conversion pipe.
+__device__ __forceinline__ float rint_magic(float x)
+{
+    return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+
+// ------------------------------------------------------------ pair kernels
+//
+// Packed source record, 6 float4 (kRec):
+//   r0 = (sh.x, sh.y, sh.z, n.x)     hi position (turns), normal x
+//   r1 = (sl.x, sl.y, sl.z, n.y)     lo position (turns), normal y
+//   r2 = (Jx.re, Jx.im, Jy.re, Jy.im)
+//   r3 = (Jz.re, Jz.im, Mx.re, Mx.im)
+//   r4 = (My.re, My.im, Mz.re, Mz.im)
+//   r5 = (n.z, 0, 0, 0)
+// Scalar record, 2 float4 (kRecScalar): (sh, S'.re), (sl, S'.im).
+//
+// Accumulators (kAcc = 12): E.re[3], E.im[3], H.re[3], H.im[3] for the near
+// field; for the far field the same slots hold S_J = sum G J' and S_M.
+
+template <int T, bool HAS_M>
+__device__ __forceinline__ void nf_pair(float *acc, const float4 &tA, const float4 &tB, const float4 *r)
+{
+    const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
+    // Exact hi differences (hi parts are multiples of q with < 12 bits).
+    const float dhx = __fsub_rn(tA.x, r0.x), dhy = __fsub_rn(tA.y, r0.y), dhz = __fsub_rn(tA.z, r0.z);
+    const float dlx = __fsub_rn(tA.w, r1.x), dly = __fsub_rn(tB.x, r1.y), dlz = __fsub_rn(tB.y, r1.z);
+    // R^2 = S0 (exact) + S1 (small).
+    const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
+    const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
+    const float R2 = __fadd_rn(S0, S1);
+    const float rinv = rsqrtf(R2);
+    const float Rh = __fmul_rn(R2, rinv);
+    const float p = __fmul_rn(Rh, Rh);
+    const float pe = fmaf(Rh, Rh, -p);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
+    const float Rl = __fmul_rn(res, __fmul_rn(0.5f, rinv));
+    // Phase in turns, reduced to [-1/2, 1/2].
+    const float f = __fadd_rn(__fsub_rn(Rh, rint_magic(Rh)), Rl);
+    float sn, cs;
+    __sincosf(f * 6.28318530717958647f, &sn, &cs);
+    // Unnormalised separation and the illumination test n . d >= 0.
+    const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
+    const float ndd = fmaf(r[5].x, dz, fmaf(r1.w, dy, r0.w * dx));
+    const bool lit = ndd >= 0.0f;
+    const float gc = lit ? cs : 0.0f;
+    const float gs = lit ? (T > 0 ? sn : -sn) : 0.0f;   // G = e^{t j theta}
+    // s1 = t u^2 + j (u^3 - u); s2 = -3 s1 - 2 j u; s3 = -u^2 + j t u; u = 1/(kR).
+    const float u = rinv * 0.159154943091895336f;
+    const float u2 = u * u;
+    const float s1r = T > 0 ? u2 : -u2;
+    const float s1i = fmaf(u2, u, -u);
+    const float c1r = gc * s1r - gs * s1i;
+    const float c1i = gc * s1i + gs * s1r;
+    const float rinv2 = rinv * rinv;
+    const float tu = 2.0f * u;
+    const float c2r = fmaf(-3.0f, c1r, tu * gs) * rinv2;    // G s2 / R^2
+    const float c2i = fmaf(-3.0f, c1i, -tu * gc) * rinv2;
+    const float s3r = -u2 * rinv;
+    const float s3i = (T > 0 ? u : -u) * rinv;
+    const float c3r = gc * s3r - gs * s3i;                    // G s3 / R
+    const float c3i = gc * s3i + gs * s3r;
+
+    const float jxr = r2.x, jxi = r2.y, jyr = r2.z, jyi = r2.w, jzr = r3.x, jzi = r3.y;
+    // J . d and P = c2 (J . d)
+    const float jdr = fmaf(jzr, dz, fmaf(jyr, dy, jxr * dx));
+    const float jdi = fmaf(jzi, dz, fmaf(jyi, dy, jxi * dx));
+    const float Pr = c2r * jdr - c2i * jdi;
+    const float Pi = c2r * jdi + c2i * jdr;
+    // J x d
+    const float axr = jyr * dz - jzr * dy, axi = jyi * dz - jzi * dy;
+    const float ayr = jzr * dx - jxr * dz, ayi = jzi * dx - jxi * dz;
+    const float azr = jxr * dy - jyr * dx, azi = jxi * dy - jyi * dx;
+    // E += c1 J + P d
+    acc[0] += c1r * jxr - c1i * jxi + Pr * dx;
+    acc[1] += c1r * jyr - c1i * jyi + Pr * dy;
+    acc[2] += c1r * jzr - c1i * jzi + Pr * dz;
+    acc[3] += c1r * jxi + c1i * jxr + Pi * dx;
+    acc[4] += c1r * jyi + c1i * jyr + Pi * dy;
+    acc[5] += c1r * jzi + c1i * jzr + Pi * dz;
+    // H -= c3 (J x d)
+    acc[6] -= c3r * axr - c3i * axi;
+    acc[7] -= c3r * ayr - c3i * ayi;
+    acc[8] -= c3r * azr - c3i * azi;
+    acc[9] -= c3r * axi + c3i * axr;
+    acc[10] -= c3r * ayi + c3i * ayr;
+    acc[11] -= c3r * azi + c3i * azr;
+    if (HAS_M) {
+        const float4 r4 = r[4];
+        const float mxr = r3.z, mxi = r3.w, myr = r4.x, myi = r4.y, mzr = r4.z, mzi = r4.w;
+        const float mdr = fmaf(mzr, dz, fmaf(myr, dy, mxr * dx));
+        const float mdi = fmaf(mzi, dz, fmaf(myi, dy, mxi * dx));
+        const float Qr = c2r * mdr - c2i * mdi;
+        const float Qi = c2r * mdi + c2i * mdr;
+        const float bxr = myr * dz - mzr * dy, bxi = myi * dz - mzi * dy;
+        const float byr = mzr * dx - mxr * dz, byi = mzi * dx - mxi * dz;
+        const float bzr = mxr * dy - myr * dx, bzi = mxi * dy - myi * dx;
+        // E += c3 (M x d)
+        acc[0] += c3r * bxr - c3i * bxi;
+        acc[1] += c3r * byr - c3i * byi;
+        acc[2] += c3r * bzr - c3i * bzi;
+        acc[3] += c3r * bxi + c3i * bxr;
+        acc[4] += c3r * byi + c3i * byr;
+        acc[5] += c3r * bzi + c3i * bzr;
+        // H += c1 M + Q d
+        acc[6] += c1r * mxr - c1i * mxi + Qr * dx;
+        acc[7] += c1r * myr - c1i * myi + Qr * dy;
+        acc[8] += c1r * mzr - c1i * mzi + Qr * dz;
+        acc[9] += c1r * mxi + c1i * mxr + Qi * dx;
+        acc[10] += c1r * myi + c1i * myr + Qi * dy;
+        acc[11] += c1r * mzi + c1i * mzr + Qi * dz;
+    }
+}
+
+// Far field: target record tA = (rh.x, rh.y, rh.z, rl.x), tB = (rl.y, rl.z, r.x?, -);
+// the full direction r = rh + rl is passed separately (per-target constant).
+template <int T, bool HAS_M>
+__device__ __forceinline__ void ff_pair(float *acc, const float4 &tA, const float4 &tB, const float3 &rr,
+                                        const float4 *r)
+{
+    const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
+    // r' . r_hat in turns: hi products are exact (hi parts have few bits).
+    const float Ph = fmaf(r0.z, tA.z, fmaf(r0.y, tA.y, __fmul_rn(r0.x, tA.x)));
+    const float Pl = fmaf(r1.z, rr.z, fmaf(r1.y, rr.y, fmaf(r1.x, rr.x,
+                     fmaf(r0.z, tB.y, fmaf(r0.y, tB.x, r0.x * tA.w)))));
+    const float f = __fadd_rn(__fsub_rn(Ph, rint_magic(Ph)), Pl);
+    float sn, cs;
+    __sincosf(f * 6.28318530717958647f, &sn, &cs);
+    const float ndr = fmaf(r[5].x, rr.z, fmaf(r1.w, rr.y, r0.w * rr.x));
+    const bool lit = ndr >= 0.0f;
+    const float gc = lit ? cs : 0.0f;
+    const float gs = lit ? (T > 0 ? -sn : sn) : 0.0f;   // G = e^{-t j theta}
+    acc[0] += gc * r2.x - gs * r2.y;
+    acc[3] += gc * r2.y + gs * r2.x;
+    acc[1] += gc * r2.z - gs * r2.w;
+    acc[4] += gc * r2.w + gs * r2.z;
+    acc[2] += gc * r3.x - gs * r3.y;
+    acc[5] += gc * r3.y + gs * r3.x;
+    if (HAS_M) {
+        const float4 r4 = r[4];
+        acc[6] += gc * r3.z - gs * r3.w;
+        acc[9] += gc * r3.w + gs * r3.z;
+        acc[7] += gc * r4.x - gs * r4.y;
+        acc[10] += gc * r4.y + gs * r4.x;
+        acc[8] += gc * r4.z - gs * r4.w;
+        acc[11] += gc * r4.w + gs * r4.z;
+    }
+}
+
+// Scalar: acc += S' e^{-t j k r} / r (prefactor, weights and k/2pi folded into S').
+template <int T>
+__device__ __forceinline__ void sc_pair(float *acc, const float4 &tA, const float4 &tB, const float4 *r)
+{
+    const float4 r0 = r[0], r1 = r[1];
+    const float dhx = __fsub_rn(tA.x, r0.x), dhy = __fsub_rn(tA.y, r0.y), dhz = __fsub_rn(tA.z, r0.z);
+    const float dlx = __fsub_rn(tA.w, r1.x), dly = __fsub_rn(tB.x, r1.y), dlz = __fsub_rn(tB.y, r1.z);
+    const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
+    const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
+    const float R2 = __fadd_rn(S0, S1);
+    const float rinv = rsqrtf(R2);
+    const float Rh = __fmul_rn(R2, rinv);
+    const float p = __fmul_rn(Rh, Rh);
+    const float pe = fmaf(Rh, Rh, -p);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
+    const float Rl = __fmul_rn(res, __fmul_rn(0.5f, rinv));
+    const float f = __fadd_rn(__fsub_rn(Rh, rint_magic(Rh)), Rl);
+    float sn, cs;
+    __sincosf(f * 6.28318530717958647f, &sn, &cs);
+    const float gr = cs * rinv;
+    const float gi = (T > 0 ? -sn : sn) * rinv;
+    acc[0] += gr * r0.w - gi * r1.w;
+    acc[1] += gr * r1.w + gi * r0.w;
+}
+
+// --------------------------------------------------------------- main kernel
+
+template <int KIND, int T, bool HAS_M, int TPT>
+__global__ void __launch_bounds__(kThreads)
+po_main_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt,
+               long nt, double *__restrict__ part, int *__restrict__ err)
+{
+    constexpr int REC = (KIND == kKindScalar) ? kRecScalar : kRec;
+    constexpr int NACC = (KIND == kKindScalar) ? 2 : kAcc;
+    extern __shared__ __align__(128) float4 stage[];   // kStages * kTile * REC
+    __shared__ __align__(8) uint64_t full[kStages];
+
+    // Targets of this thread (coalesced: target j sits kThreads apart).
+    const long tbase = (long)blockIdx.x * kThreads * TPT + threadIdx.x;
+    float4 tA[TPT], tB[TPT];
+    float3 rr[TPT];
+#pragma unroll
+    for (int j = 0; j < TPT; ++j) {
+        const long ti = tbase + (long)j * kThreads;
+        if (ti < nt) {
+            tA[j] = tgt[2 * ti];
+            tB[j] = tgt[2 * ti + 1];
+        } else {
+            tA[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+            tB[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (KIND != kKindFF) tA[j].z = 1.0f;  // keep R > 0 for idle lanes
+        }
+        rr[j] = make_float3(tA[j].x + tA[j].w, tA[j].y + tB[j].x, tA[j].z + tB[j].y);
+    }
+
+    float hi[TPT][NACC], lo[TPT][NACC];
+#pragma unroll
+    for (int j = 0; j < TPT; ++j)
+#pragma unroll
+        for (int a = 0; a < NACC; ++a) { hi[j][a] = 0.f; lo[j][a] = 0.f; }
+
+    const long s0 = (long)blockIdx.y * chunk;
+    const long s1 = min(ns, s0 + chunk);
+    const int ntiles = s1 > s0 ? (int)((s1 - s0 + kTile - 1) / kTile) : 0;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int it) {
+        const long first = s0 + (long)it * kTile;
+        const long cnt = min((long)kTile, s1 - first);
+        const uint32_t bytes = (uint32_t)(cnt * REC * sizeof(float4));
+        uint64_t *bar = &full[it % kStages];
+        fence_proxy_async();
+        mbar_expect_tx(bar, bytes);
+        tma_load_1d(stage + (size_t)(it % kStages) * kTile * REC, src + first * REC, bytes, bar);
+    };
+    if (threadIdx.x == 0)
+        for (int it = 0; it < ntiles && it < kStages; ++it) issue(it);
+
+    bool aborted = false;   // block-uniform: decided by __syncthreads_or
+    for (int it = 0; it < ntiles; ++it) {
+        const bool ok = mbar_wait_bounded(&full[it % kStages], (uint32_t)((it / kStages) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicExch(err, kErrWaitTimeout);
+            aborted = true;
+            break;
+        }
+        const float4 *tile = stage + (size_t)(it % kStages) * kTile * REC;
+        const int cnt = (int)min((long)kTile, s1 - (s0 + (long)it * kTile));
+        float acc[TPT][NACC];
+#pragma unroll
+        for (int j = 0; j < TPT; ++j)
+#pragma unroll
+            for (int a = 0; a < NACC; ++a) acc[j][a] = 0.f;
+
+#pragma unroll 2
+        for (int s = 0; s < cnt; ++s) {
+            float4 rec[REC];
+#pragma unroll
+            for (int q = 0; q < REC; ++q) rec[q] = tile[s * REC + q];
+#pragma unroll
+            for (int j = 0; j < TPT; ++j) {
+                if (KIND == kKindNF) nf_pair<T, HAS_M>(acc[j], tA[j], tB[j], rec);
+                else if (KIND == kKindFF) ff_pair<T, HAS_M>(acc[j], tA[j], tB[j], rr[j], rec);
+                else sc_pair<T>(acc[j], tA[j], tB[j], rec);
+            }
+        }
+        // Fold this tile's partial into the compensated totals.
+#pragma unroll
+        for (int j = 0; j < TPT; ++j)
+#pragma unroll
+            for (int a = 0; a < NACC; ++a) {
+                float s, e;
+                two_sum(hi[j][a], acc[j][a], s, e);
+                hi[j][a] = s;
+                lo[j][a] = __fadd_rn(lo[j][a], e);
+            }
+        __syncthreads();   // everyone is done reading this stage
+        if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
+    }
+
+    if (aborted) {
+        // Drain copies still in flight (bounded) before the CTA retires.
+        if (threadIdx.x == 0)
+            for (int s = 0; s < kStages; ++s) (void)mbar_wait_bounded(&full[s], 0);
+        return;
+    }
+
+#pragma unroll
+    for (int j = 0; j < TPT; ++j) {
+        const long ti = tbase + (long)j * kThreads;
+        if (ti >= nt) continue;
+#pragma unroll
+        for (int a = 0; a < NACC; ++a)
+            part[((long)blockIdx.y * NACC + a) * nt + ti] = (double)hi[j][a] + (double)lo[j][a];
+    }
+}
+
+// ----------------------------------------------------------- frame & packing
+
+__global__ void po_bbox_kernel(const double *__restrict__ a, long na, const double *__restrict__ b, long nb,
+                               double *__restrict__ partial)
+{
+    __shared__ double sm[6][kBboxThreads];
+    double v[6] = {CUDART_INF, CUDART_INF, CUDART_INF, -CUDART_INF, -CUDART_INF, -CUDART_INF};
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += stride) {
+        const double *p = i < na ? a : b;
+        const long n = i < na ? na : nb;
+        const long k = i < na ? i : i - na;
+        for (int c = 0; c < 3; ++c) {
+            const double x = p[c * n + k];
+            v[c] = fmin(v[c], x);
+            v[3 + c] = fmax(v[3 + c], x);
+        }
+    }
+    for (int c = 0; c < 6; ++c) sm[c][threadIdx.x] = v[c];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int c = 0; c < 6; ++c)
+                sm[c][threadIdx.x] = c < 3 ? fmin(sm[c][threadIdx.x], sm[c][threadIdx.x + w])
+                                           : fmax(sm[c][threadIdx.x], sm[c][threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 6; ++c) partial[blockIdx.x * 6 + c] = sm[c][0];
+}
+
+// One thread: reduce the block partials and fix origin, scale and quantum.
+// centred: origin at the bbox centre (near field, scalar); otherwise origin 0
+// (far field: the phase reference is the coordinate origin).
+__global__ void po_frame_kernel(const double *__restrict__ partial, int nblk, double kappa, int centred,
+                                Frame *__restrict__ fr)
+{
+    double lo[3] = {CUDART_INF, CUDART_INF, CUDART_INF}, hi[3] = {-CUDART_INF, -CUDART_INF, -CUDART_INF};
+    for (int b = 0; b < nblk; ++b)
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fmin(lo[c], partial[b * 6 + c]);
+            hi[c] = fmax(hi[c], partial[b * 6 + 3 + c]);
+        }
+    double m = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        double o = 0.0;
+        if (centred && lo[c] <= hi[c]) o = 0.5 * (lo[c] + hi[c]);
+        fr->o[c] = o;
+        if (lo[c] <= hi[c]) m = fmax(m, fmax(fabs(hi[c] - o), fabs(lo[c] - o)));
+    }
+    m *= kappa;
+    // Smallest power of two q with 2 m / q <= 2048, so |hi/q| <= 1024.5.
+    double need = 2.0 * m / 2048.0;
+    double q = 0x1p-40;
+    while (q < need) q *= 2.0;
+    fr->kappa = kappa;
+    fr->q = q;
+    fr->inv_q = 1.0 / q;
+}
+
+__device__ __forceinline__ double trap_weight(long i, int gmode, int ncx, int ncy)
+{
+    if (gmode < 0) return 1.0;
+    const long xu = i / ncy, yv = i - xu * ncy;
+    double w = (xu == 0 || xu == ncx - 1) ? 0.5 : 1.0;
+    if (gmode != 1 && (yv == 0 || yv == ncy - 1)) w *= 0.5;
+    return w;
+}
+
+__device__ __forceinline__ void split_hi_lo(double x, const Frame &fr, float &h, float &l)
+{
+    const double hd = rint(x * fr.inv_q) * fr.q;
+    h = (float)hd;
+    l = (float)(x - hd);
+}
+
+// fac: complex factor folded into the currents (times weight * area).
+__global__ void po_pack_src_kernel(long ns, const double *__restrict__ src7, const double *__restrict__ cur,
+                                   int gmode, int ncx, int ncy, const Frame *__restrict__ frp, double fac_re,
+                                   double fac_im, int scalar, float4 *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns) return;
+    const Frame fr = *frp;
+    float h[3], l[3];
+    for (int c = 0; c < 3; ++c) split_hi_lo((src7[c * ns + i] - fr.o[c]) * fr.kappa, fr, h[c], l[c]);
+    const double w = trap_weight(i, gmode, ncx, ncy) * src7[6 * ns + i];
+    const double fr_ = fac_re * w, fi_ = fac_im * w;
+    if (scalar) {
+        const double re = cur[i], im = cur[ns + i];
+        out[2 * i] = make_float4(h[0], h[1], h[2], (float)(fr_ * re - fi_ * im));
+        out[2 * i + 1] = make_float4(l[0], l[1], l[2], (float)(fr_ * im + fi_ * re));
+        return;
+    }
+    float c[12];   // J.re/im x y z interleaved, then M
+    for (int q = 0; q < 6; ++q) {
+        const int grp = q / 3, ax = q % 3;
+        const double re = cur[(grp * 6 + ax) * ns + i];
+        const double im = cur[(grp * 6 + 3 + ax) * ns + i];
+        c[2 * q] = (float)(fr_ * re - fi_ * im);
+        c[2 * q + 1] = (float)(fr_ * im + fi_ * re);
+    }
+    float4 *o = out + (size_t)kRec * i;
+    o[0] = make_float4(h[0], h[1], h[2], (float)src7[3 * ns + i]);
+    o[1] = make_float4(l[0], l[1], l[2], (float)src7[4 * ns + i]);
+    o[2] = make_float4(c[0], c[1], c[2], c[3]);
+    o[3] = make_float4(c[4], c[5], c[6], c[7]);
+    o[4] = make_float4(c[8], c[9], c[10], c[11]);
+    o[5] = make_float4((float)src7[5 * ns + i], 0.f, 0.f, 0.f);
+}
+
+// Near-field / scalar targets: hi/lo split positions in the same frame.
+// Far-field targets: direction r_hat from (polar, azimuth), hi part on 2^-11.
+__global__ void po_pack_tgt_kernel(long nt, const double *__restrict__ tgt7, const Frame *__restrict__ frp,
+                                   int far, float4 *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    float h[3], l[3];
+    if (far) {
+        const double th = tgt7[i], ph = tgt7[nt + i];
+        const double r[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
+        for (int c = 0; c < 3; ++c) {
+            const double hd = rint(r[c] * 2048.0) / 2048.0;
+            h[c] = (float)hd;
+            l[c] = (float)(r[c] - hd);
+        }
+    } else {
+        const Frame fr = *frp;
+        for (int c = 0; c < 3; ++c) split_hi_lo((tgt7[c * nt + i] - fr.o[c]) * fr.kappa, fr, h[c], l[c]);
+    }
+    out[2 * i] = make_float4(h[0], h[1], h[2], l[0]);
+    out[2 * i + 1] = make_float4(l[1], l[2], 0.f, 0.f);
+}
+
+// ---------------------------------------------------------------- FP64 path
+
+// Double record (kRecD doubles): x y z nx ny nz, J'(re,im)x3, M'(re,im)x3.
+__global__ void po_pack_src_d_kernel(long ns, const double *__restrict__ src7, const double *__restrict__ cur,
+                                     int gmode, int ncx, int ncy, double fac_re, double fac_im, int scalar,
+                                     double *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns) return;
+    double *o = out + (size_t)kRecD * i;
+    for (int c = 0; c < 6; ++c) o[c] = src7[c * ns + i];
+    const double w = trap_weight(i, gmode, ncx, ncy) * src7[6 * ns + i];
+    const double fr_ = fac_re * w, fi_ = fac_im * w;
+    if (scalar) {
+        const double re = cur[i], im = cur[ns + i];
+        o[6] = fr_ * re - fi_ * im;
+        o[7] = fr_ * im + fi_ * re;
+        for (int q = 8; q < kRecD; ++q) o[q] = 0.0;
+        return;
+    }
+    for (int q = 0; q < 6; ++q) {
+        const int grp = q / 3, ax = q % 3;
+        const double re = cur[(grp * 6 + ax) * ns + i];
+        const double im = cur[(grp * 6 + 3 + ax) * ns + i];
+        o[6 + 2 * q] = fr_ * re - fi_ * im;
+        o[7 + 2 * q] = fr_ * im + fi_ * re;
+    }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreadsD)
+po_fp64_kernel(const double *__restrict__ src, long ns, const double *__restrict__ tgt7, long nt, double k,
+               double t, double *__restrict__ part)
+{
+    __shared__ double tile[kTileD * kRecD];
+    const long ti = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double p[3] = {0, 0, 0};
+    if (ti < nt) {
+        if (KIND == kKindFF) {
+            const double th = tgt7[ti], ph = tgt7[nt + ti];
+            p[0] = cos(ph) * sin(th);
+            p[1] = sin(ph) * sin(th);
+            p[2] = cos(th);
+        } else {
+            for (int c = 0; c < 3; ++c) p[c] = tgt7[c * nt + ti];
+        }
+    }
+    double acc[kAcc];
+    for (int a = 0; a < kAcc; ++a) acc[a] = 0.0;
+    for (long base = 0; base < ns; base += kTileD) {
+        const int cnt = (int)min((long)kTileD, ns - base);
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt * kRecD; q += blockDim.x) tile[q] = src[base * kRecD + q];
+        __syncthreads();
+        if (ti >= nt) continue;
+        for (int s = 0; s < cnt; ++s) {
+            const double *r = tile + s * kRecD;
+            if (KIND == kKindNF) {
+                const double dx = p[0] - r[0], dy = p[1] - r[1], dz = p[2] - r[2];
+                const double R = sqrt(dx * dx + dy * dy + dz * dz);
+                const double rinv = 1.0 / R;
+                if (r[3] * dx + r[4] * dy + r[5] * dz < 0) continue;
+                double sn, cs;
+                sincos(k * R, &sn, &cs);
+                const double gc = cs, gs = t * sn;
+                const double u = rinv / k, u2 = u * u;
+                const double s1r = t * u2, s1i = u2 * u - u;
+                const double c1r = gc * s1r - gs * s1i, c1i = gc * s1i + gs * s1r;
+                const double rinv2 = rinv * rinv;
+                const double c2r = (-3.0 * c1r + 2.0 * u * gs) * rinv2;
+                const double c2i = (-3.0 * c1i - 2.0 * u * gc) * rinv2;
+                const double s3r = -u2 * rinv, s3i = t * u * rinv;
+                const double c3r = gc * s3r - gs * s3i, c3i = gc * s3i + gs * s3r;
+                const double d[3] = {dx, dy, dz};
+                const double *J = r + 6, *M = r + 12;
+                const double jdr = J[0] * dx + J[2] * dy + J[4] * dz, jdi = J[1] * dx + J[3] * dy + J[5] * dz;
+                const double mdr = M[0] * dx + M[2] * dy + M[4] * dz, mdi = M[1] * dx + M[3] * dy + M[5] * dz;
+                const double Pr = c2r * jdr - c2i * jdi, Pi = c2r * jdi + c2i * jdr;
+                const double Qr = c2r * mdr - c2i * mdi, Qi = c2r * mdi + c2i * mdr;
+                for (int c = 0; c < 3; ++c) {
+                    const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+                    // (J x d)_c and (M x d)_c
+                    const double jxr = J[2 * a1] * d[a2] - J[2 * a2] * d[a1];
+                    const double jxi = J[2 * a1 + 1] * d[a2] - J[2 * a2 + 1] * d[a1];
+                    const double mxr = M[2 * a1] * d[a2] - M[2 * a2] * d[a1];
+                    const double mxi = M[2 * a1 + 1] * d[a2] - M[2 * a2 + 1] * d[a1];
+                    acc[c] += c1r * J[2 * c] - c1i * J[2 * c + 1] + Pr * d[c] + c3r * mxr - c3i * mxi;
+                    acc[3 + c] += c1r * J[2 * c + 1] + c1i * J[2 * c] + Pi * d[c] + c3r * mxi + c3i * mxr;
+                    acc[6 + c] += c1r * M[2 * c] - c1i * M[2 * c + 1] + Qr * d[c] - (c3r * jxr - c3i * jxi);
+                    acc[9 + c] += c1r * M[2 * c + 1] + c1i * M[2 * c] + Qi * d[c] - (c3r * jxi + c3i * jxr);
+                }
+            } else if (KIND == kKindFF) {
+                if (r[3] * p[0] + r[4] * p[1] + r[5] * p[2] < 0) continue;
+                double sn, cs;
+                sincos(k * (r[0] * p[0] + r[1] * p[1] + r[2] * p[2]), &sn, &cs);
+                const double gc = cs, gs = -t * sn;
+                for (int c = 0; c < 6; ++c) {
+                    const double cr = r[6 + 2 * c], ci = r[7 + 2 * c];
+                    const int slot = (c < 3) ? c : 6 + (c - 3);
+                    acc[slot] += gc * cr - gs * ci;
+                    acc[slot + 3] += gc * ci + gs * cr;
+                }
+            } else {
+                const double dx = p[0] - r[0], dy = p[1] - r[1], dz = p[2] - r[2];
+                const double R = sqrt(dx * dx + dy * dy + dz * dz);
+                double sn, cs;
+                sincos(k * R, &sn, &cs);
+                const double gr = cs / R, gi = -t * sn / R;
+                acc[0] += gr * r[6] - gi * r[7];
+                acc[1] += gr * r[7] + gi * r[6];
+            }
+        }
+    }
+    if (ti < nt) {
+        const int nacc = (KIND == kKindScalar) ? 2 : kAcc;
+        for (int a = 0; a < nacc; ++a) part[(long)a * nt + ti] = acc[a];
+    }
+}
+
+// ------------------------------------------------------------------ epilogue
+
+__device__ __forceinline__ void cross_d(const double a[3], const double b[3], double o[3])
+{
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+__device__ __forceinline__ void normalize_d(const double v[3], double o[3])
+{
+    double n = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (n <= 4.9406564584124654e-324) n = 4.9406564584124654e-324;
+    for (int c = 0; c < 3; ++c) o[c] = v[c] / n;
+}
+
+// Sums the source chunks in order and writes the mode's outputs (FP64).
+// Output rows follow the reference's bundle order.
+__global__ void po_epilogue_kernel(int mode, int nsplit, long nt, const double *__restrict__ part,
+                                   const double *__restrict__ tgt7, double t, double zeta_inv,
+                                   double *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    if (mode == kScalar) {
+        double re = 0, im = 0;
+        for (int s = 0; s < nsplit; ++s) {
+            re += part[((long)s * 2 + 0) * nt + i];
+            im += part[((long)s * 2 + 1) * nt + i];
+        }
+        out[i] = re;
+        out[nt + i] = im;
+        return;
+    }
+    double a[kAcc];
+    for (int q = 0; q < kAcc; ++q) a[q] = 0.0;
+    for (int s = 0; s < nsplit; ++s)
+        for (int q = 0; q < kAcc; ++q) a[q] += part[((long)s * kAcc + q) * nt + i];
+    // a: E.re[3] E.im[3] H.re[3] H.im[3]
+    double er[3] = {a[0], a[1], a[2]}, ei[3] = {a[3], a[4], a[5]};
+    double hr[3] = {a[6], a[7], a[8]}, hi[3] = {a[9], a[10], a[11]};
+    auto put = [&](int row, double v) { out[(long)row * nt + i] = v; };
+    if (mode == kFF) {
+        // E = S_J - (S_J . r) r + t r x S_M ;  H = S_M - (S_M . r) r - t r x S_J
+        const double th = tgt7[i], ph = tgt7[nt + i];
+        const double r[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
+        const double jdr = er[0] * r[0] + er[1] * r[1] + er[2] * r[2];
+        const double jdi = ei[0] * r[0] + ei[1] * r[1] + ei[2] * r[2];
+        const double mdr = hr[0] * r[0] + hr[1] * r[1] + hr[2] * r[2];
+        const double mdi = hi[0] * r[0] + hi[1] * r[1] + hi[2] * r[2];
+        double rxmr[3], rxmi[3], rxjr[3], rxji[3];
+        cross_d(r, hr, rxmr);
+        cross_d(r, hi, rxmi);
+        cross_d(r, er, rxjr);
+        cross_d(r, ei, rxji);
+        for (int c = 0; c < 3; ++c) {
+            put(c, er[c] - jdr * r[c] + t * rxmr[c]);
+            put(3 + c, ei[c] - jdi * r[c] + t * rxmi[c]);
+            put(6 + c, hr[c] - mdr * r[c] - t * rxjr[c]);
+            put(9 + c, hi[c] - mdi * r[c] - t * rxji[c]);
+        }
+        return;
+    }
+    if (mode == kEH) {
+        for (int c = 0; c < 3; ++c) {
+            put(c, er[c]);
+            put(3 + c, ei[c]);
+            put(6 + c, hr[c]);
+            put(9 + c, hi[c]);
+        }
+        return;
+    }
+    const double n[3] = {tgt7[3 * nt + i], tgt7[4 * nt + i], tgt7[5 * nt + i]};
+    if (mode == kJM || mode == kJMEH) {
+        double jr[3], ji[3];
+        cross_d(n, hr, jr);
+        cross_d(n, hi, ji);
+        for (int c = 0; c < 3; ++c) {
+            put(c, 2.0 * jr[c]);
+            put(3 + c, 2.0 * ji[c]);
+            put(6 + c, 0.0);
+            put(9 + c, 0.0);
+        }
+        if (mode == kJMEH)
+            for (int c = 0; c < 3; ++c) {
+                put(12 + c, er[c]);
+                put(15 + c, ei[c]);
+                put(18 + c, hr[c]);
+                put(21 + c, hi[c]);
+            }
+        return;
+    }
+    // EHP: reflected field from the incident Poynting direction (Snell).
+    double s[3], si[3], tmp[3], pip[3], pia[3], sr[3], prp[3], pra[3];
+    for (int c = 0; c < 3; ++c) {
+        // Re(E x conj(H))_c
+        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+        s[c] = (er[a1] * hr[a2] + ei[a1] * hi[a2]) - (er[a2] * hr[a1] + ei[a2] * hi[a1]);
+    }
+    normalize_d(s, si);
+    cross_d(si, n, tmp);
+    normalize_d(tmp, pip);
+    cross_d(pip, si, pia);
+    const double f = 2.0 * (si[0] * n[0] + si[1] * n[1] + si[2] * n[2]);
+    for (int c = 0; c < 3; ++c) sr[c] = si[c] - n[c] * f;
+    cross_d(sr, n, tmp);
+    normalize_d(tmp, prp);
+    cross_d(sr, prp, pra);
+    const double epr = er[0] * prp[0] + er[1] * prp[1] + er[2] * prp[2];
+    const double epi = ei[0] * prp[0] + ei[1] * prp[1] + ei[2] * prp[2];
+    const double ear = er[0] * pra[0] + er[1] * pra[1] + er[2] * pra[2];
+    const double eai = ei[0] * pra[0] + ei[1] * pra[1] + ei[2] * pra[2];
+    double rr[3], ri[3];
+    for (int c = 0; c < 3; ++c) {
+        rr[c] = -epr * pip[c] - ear * pia[c];
+        ri[c] = -epi * pip[c] - eai * pia[c];
+    }
+    double xr[3], xi[3];
+    cross_d(sr, rr, xr);
+    cross_d(sr, ri, xi);
+    for (int c = 0; c < 3; ++c) {
+        put(c, rr[c]);
+        put(3 + c, ri[c]);
+        put(6 + c, xr[c] * zeta_inv);
+        put(9 + c, xi[c] * zeta_inv);
+        put(12 + c, sr[c]);
+    }
+}
+
+// ------------------------------------------------------------- FP32 probe
+// Eight independent FFMA chains per thread: the FP32 pipe's throughput on
+// this GPU, the roofline denominator of the pair kernels. The result is
+// stored so the chains cannot be optimised away.
+__global__ void __launch_bounds__(256) po_fp32_probe_kernel(int iters, float seed, float *__restrict__ out)
+{
+    float a[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = seed + q + threadIdx.x * 1e-3f;
+    const float b = 0.999999f, c = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = fmaf(a[q], b, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += a[q];
+    out[(long)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// ----------------------------------------------------------- instantiations
+
+template <int KIND, int T, bool HAS_M>
+static void *main_kernel_ptr()
+{
+    return reinterpret_cast<void *>(&po_main_kernel<KIND, T, HAS_M, kTPT>);
+}
+
+void *main_kernel(int kind, int t_sign, bool has_m)
+{
+    if (kind == kKindNF) {
+        if (t_sign < 0) return has_m ? main_kernel_ptr<kKindNF, -1, true>() : main_kernel_ptr<kKindNF, -1, false>();
+        return has_m ? main_kernel_ptr<kKindNF, 1, true>() : main_kernel_ptr<kKindNF, 1, false>();
+    }
+    if (kind == kKindFF) {
+        if (t_sign < 0) return has_m ? main_kernel_ptr<kKindFF, -1, true>() : main_kernel_ptr<kKindFF, -1, false>();
+        return has_m ? main_kernel_ptr<kKindFF, 1, true>() : main_kernel_ptr<kKindFF, 1, false>();
+    }
+    return t_sign < 0 ? main_kernel_ptr<kKindScalar, -1, false>() : main_kernel_ptr<kKindScalar, 1, false>();
+}
+
+void *fp64_kernel(int kind)
+{
+    if (kind == kKindNF) return reinterpret_cast<void *>(&po_fp64_kernel<kKindNF>);
+    if (kind == kKindFF) return reinterpret_cast<void *>(&po_fp64_kernel<kKindFF>);
+    return reinterpret_cast<void *>(&po_fp64_kernel<kKindScalar>);
+}
+
+void *bbox_kernel() { return reinterpret_cast<void *>(&po_bbox_kernel); }
+void *frame_kernel() { return reinterpret_cast<void *>(&po_frame_kernel); }
+void *pack_src_kernel() { return reinterpret_cast<void *>(&po_pack_src_kernel); }
+void *pack_tgt_kernel() { return reinterpret_cast<void *>(&po_pack_tgt_kernel); }
+void *pack_src_d_kernel() { return reinterpret_cast<void *>(&po_pack_src_d_kernel); }
+void *epilogue_kernel() { return reinterpret_cast<void *>(&po_epilogue_kernel); }
+void *fp32_probe_kernel() { return reinterpret_cast<void *>(&po_fp32_probe_kernel); }
+
+}  // namespace po

@@ -1,0 +1,61 @@
+// po_kernels.cuh -- constants and kernel handles shared by the PO kernels and
+// their host launcher.
+#pragma once
+#include <cstdint>
+
+namespace po {
+
+// Propagation modes (numbering of the reference's GpropagateBeam_0..5).
+enum Mode { kJM = 0, kEH = 1, kJMEH = 2, kEHP = 3, kFF = 4, kScalar = 5 };
+
+// Kernel families.
+constexpr int kKindNF = 0;      // near field (JM, EH, JMEH, EHP)
+constexpr int kKindFF = 1;      // far field
+constexpr int kKindScalar = 2;  // scalar Green's function
+
+// Mixed-precision N-body kernel geometry.
+constexpr int kThreads = 128;   // threads per CTA
+constexpr int kTPT = 2;         // targets per thread (registers)
+constexpr int kTile = 128;      // sources per shared-memory stage
+constexpr int kStages = 3;      // TMA pipeline depth
+constexpr int kRec = 6;         // float4 per packed source record (96 B)
+constexpr int kRecScalar = 2;   // float4 per packed scalar record (32 B)
+constexpr int kAcc = 12;        // accumulators per target (E, H re/im x y z)
+constexpr uint32_t kWaitLimit = 1u << 24;   // bounded mbarrier polls
+
+// FP64 comparison kernel.
+constexpr int kThreadsD = 128;
+constexpr int kTileD = 64;
+constexpr int kRecD = 18;       // x y z nx ny nz, J' 6, M' 6 (doubles)
+
+constexpr int kBboxThreads = 256;
+constexpr int kBboxBlocks = 152;
+
+// Device error codes (written to the call's error word).
+constexpr int kErrWaitTimeout = 101;
+
+// Frame of the split representation: positions in turns (mm * kappa),
+// relative to origin o, hi parts on multiples of q.
+struct Frame {
+    double o[3];
+    double kappa;
+    double q;
+    double inv_q;
+};
+
+inline int main_smem_bytes(int kind)
+{
+    return kStages * kTile * (kind == kKindScalar ? kRecScalar : kRec) * 16;
+}
+
+void *main_kernel(int kind, int t_sign, bool has_m);
+void *fp64_kernel(int kind);
+void *bbox_kernel();
+void *frame_kernel();
+void *pack_src_kernel();
+void *pack_tgt_kernel();
+void *pack_src_d_kernel();
+void *epilogue_kernel();
+void *fp32_probe_kernel();
+
+}  // namespace po

@@ -1,0 +1,120 @@
+"""Explicit-grid Python API over libpo_gb300.
+
+`propagate` runs one physical-optics propagation on host numpy buffers
+(po_run_d); `propagate_dev` on device buffers given as torch tensors
+(po_run_dev, queued on the current torch stream); `generate_grid` is the FP64
+grid generator (po_generate_grid).
+
+Array layouts (all float64):
+  src7 / tgt7 : (7, n) rows x y z nx ny nz area; row-major over the surface's
+                (ncx, ncy) grid. For far-field targets x is the polar angle
+                and y the azimuth in radians (the AoE grid's spheric form).
+  cur         : (12, ns) rows in c2Bundle order r1x r1y r1z i1x i1y i1z r2x
+                ... i2z (J then M), or (2, ns) (re, im) for scalar mode.
+  result      : (n_out(mode), nt) rows in the mode's bundle order.
+"""
+import ctypes
+
+import numpy as np
+
+from . import Structs as S
+from . import marshal as M
+from ._lib import MODE_ID, POError, check, load
+
+PRECISION = {"mixed": 0, "fp64": 1}
+
+
+def n_out(mode):
+    return S.N_OUT[mode]
+
+
+def generate_grid(refl, transform=True, spheric=True):
+    """(7, n) float64 grid of a reflector dict (FP64 generator)."""
+    lib = load()
+    rp, keep = M.fill_reflparams(refl, ctypes.c_double)
+    n = int(np.prod(refl["gridsize"]))
+    ct, block = M.alloc_container(n, ctypes.c_double)
+    check(lib.po_generate_grid(rp, ctypes.byref(ct), int(transform), int(spheric)))
+    return block
+
+
+def _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy):
+    if mode not in MODE_ID:
+        raise POError(f"unknown mode {mode!r}; expected one of {tuple(MODE_ID)}")
+    ns = src7.shape[1]
+    if src7.shape[0] != 7 or tgt7.shape[0] != 7:
+        raise POError("src7 and tgt7 must have 7 rows (x y z nx ny nz area)")
+    want = 2 if mode == "scalar" else 12
+    if cur.shape != (want, ns):
+        raise POError(f"cur must have shape ({want}, {ns}) for mode {mode}")
+    if gmode >= 0 and ncx * ncy != ns:
+        raise POError("ncx * ncy must equal the number of source points")
+
+
+def propagate(mode, src7, cur, gmode, ncx, ncy, tgt7, k, epsilon=1.0, t_dir=-1.0, precision="mixed",
+              out=None):
+    """Host-buffer propagation; returns (n_out(mode), nt) float64 (into `out` when given)."""
+    lib = load()
+    src7 = np.ascontiguousarray(src7, dtype=np.float64)
+    tgt7 = np.ascontiguousarray(tgt7, dtype=np.float64)
+    cur = np.ascontiguousarray(cur, dtype=np.float64)
+    _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy)
+    nt = tgt7.shape[1]
+    if out is None:
+        out = np.empty((n_out(mode), nt), dtype=np.float64)
+    elif out.shape != (n_out(mode), nt) or out.dtype != np.float64 or not out.flags.c_contiguous:
+        raise POError(f"out must be a C-contiguous float64 array of shape {(n_out(mode), nt)}")
+    check(lib.po_run_d(MODE_ID[mode], src7.shape[1], src7.ctypes.data, int(gmode), int(ncx), int(ncy),
+                       cur.ctypes.data, nt, tgt7.ctypes.data, float(k), float(epsilon), float(t_dir),
+                       PRECISION[precision], out.ctypes.data))
+    return out
+
+
+def propagate_dev(mode, src7, cur, gmode, ncx, ncy, tgt7, k, epsilon=1.0, t_dir=-1.0,
+                  precision="mixed", m_zero=False, out=None, stream=None):
+    """Device-buffer propagation on torch float64 CUDA tensors.
+
+    Queued on `stream` (default: torch's current stream); returns `out`.
+    """
+    import torch
+    lib = load()
+    for name, t in (("src7", src7), ("cur", cur), ("tgt7", tgt7)):
+        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+            raise POError(f"{name} must be a contiguous float64 CUDA tensor")
+    _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy)
+    nt = tgt7.shape[1]
+    if out is None:
+        out = torch.empty((n_out(mode), nt), dtype=torch.float64, device=tgt7.device)
+    if stream is None:
+        stream = torch.cuda.current_stream(tgt7.device)
+    check(lib.po_run_dev(MODE_ID[mode], src7.shape[1], src7.data_ptr(), int(gmode), int(ncx), int(ncy),
+                         cur.data_ptr(), nt, tgt7.data_ptr(), float(k), float(epsilon), float(t_dir),
+                         PRECISION[precision], 1 if m_zero else 0, out.data_ptr(), ctypes.c_void_p(stream.cuda_stream)))
+    return out
+
+
+def device_error(stream=None):
+    """Synchronise `stream` and return the device error word (0 = fine)."""
+    lib = load()
+    code = ctypes.c_int(0)
+    ptr = None
+    if stream is not None:
+        ptr = ctypes.c_void_p(stream.cuda_stream)
+    check(lib.po_device_error(ptr, ctypes.byref(code)))
+    return code.value
+
+
+def last_launches():
+    return load().po_last_launches()
+
+
+def timing_enable(slots):
+    check(load().po_timing_enable(int(slots)))
+
+
+def timing_collect(max_n=4096):
+    buf = (ctypes.c_float * max_n)()
+    n = load().po_timing_collect(buf, max_n)
+    if n < 0:
+        raise POError("po_timing_collect failed")
+    return [buf[i] for i in range(n)]

@@ -1,0 +1,103 @@
+"""Generate the golden vectors in tests/golden/ from the reference itself.
+
+Runs the reference's own FP64 CPU library (oracle/_ref/libpypo_ref.so,
+compiled from the reference sources by oracle/build_ref.sh) on small seeded
+cases shaped like the reference's test templates (reference
+tests/TestTemplates.py: 13x13 / 13x12 grids, xy, uv and AoE): every PO mode
+in both time directions, the grid generator for every surface type, and the
+vector Gaussian feed (makeGaussBeam). Outputs go to golden_*.npz beside this
+script. Needs the reference sources (this container); the fixtures then
+travel without them.
+
+Usage: python tests/golden/make_golden.py
+"""
+import json
+import pathlib
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle as O  # noqa: E402
+from pypo_gb300 import surfaces as SF  # noqa: E402
+
+
+def dict_to_json(d):
+    return json.dumps({k: (np.asarray(v).tolist() if isinstance(v, np.ndarray) else v) for k, v in d.items()})
+
+
+def cases():
+    par_uv = SF.paraboloid(0.25, [13, 12], gmode=1, lims_a=[0, 1])          # coeffs (1, 1), as the templates
+    par_xy = SF.paraboloid(0.25, [13, 13], gmode=0, lims_a=[-1, 1])
+    pl_tgt = SF.translate(SF.plane([13, 13], gmode=0, lims_a=[-1.5, 1.5]), dz=2.5)
+    hyp = SF.hyperboloid(2.0, 2.0, 3.0, [11, 10], gmode=1, lims_a=[0, 1.5])
+    ell = SF.translate(SF.ellipsoid(3.0, 3.0, 5.0, [9, 11], gmode=0, lims_a=[-1, 1]), dz=8.0)
+    ell = dict(ell, flip=True)
+    ff = SF.farfield([11, 9], [-8, 8], [-6, 6])
+    return [
+        ("paruv_to_plane", par_uv, pl_tgt, ["JM", "EH", "JMEH", "EHP", "scalar"]),
+        ("parxy_to_plane", par_xy, pl_tgt, ["EH", "JMEH"]),
+        ("paruv_to_ff", par_uv, ff, ["FF"]),
+        ("hyp_to_ell", hyp, ell, ["JM", "EH", "EHP"]),
+    ]
+
+
+def main():
+    if not O.REF_PATH.exists():
+        subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
+    ref = O.Reference()
+    rng = np.random.default_rng(20261203)
+    k = 2 * np.pi / 0.7
+    for name, src, tgt, modes in cases():
+        ns = int(np.prod(src["gridsize"]))
+        cur = rng.standard_normal((12, ns))
+        data = {"src_json": dict_to_json(src), "tgt_json": dict_to_json(tgt), "k": k, "epsilon": 1.7,
+                "cur": cur}
+        for mode in modes:
+            for t in (-1.0, 1.0):
+                c = cur[:2] if mode == "scalar" else cur
+                out, sg, tg = ref.propagate(mode, src, tgt, c, k=k, epsilon=1.7, t_dir=t, nthreads=4)
+                data[f"out_{mode}_{'fwd' if t < 0 else 'bwd'}"] = out
+        data["src_grid"] = sg
+        data["tgt_grid"] = tg
+        np.savez_compressed(HERE / f"golden_{name}.npz", **data)
+        print("wrote", name, modes)
+
+    # Grid generator, every surface type and grid mode.
+    grids = {
+        "par_xy": SF.paraboloid(0.25, [13, 13], gmode=0, lims_a=[-1, 1]),
+        "par_uv": SF.paraboloid(300.0, [11, 12], gmode=1, lims_a=[0, 150], ecc_uv=0.3, rot_uv=20.0,
+                                gcenter=np.array([3.0, -2.0])),
+        "hyp_xy": SF.hyperboloid(2.0, 3.0, 5.0, [9, 7], gmode=0, lims_a=[-1, 1], lims_b=[-2, 2],
+                                 gcenter=np.array([1.0, 2.0])),
+        "hyp_uv": SF.hyperboloid(2.0, 3.0, 5.0, [9, 8], gmode=1, lims_a=[0, 1], flip=True),
+        "ell_xy": SF.ellipsoid(4.0, 5.0, 6.0, [9, 7], gmode=0, lims_a=[-1, 1]),
+        "ell_uv": SF.ellipsoid(4.0, 5.0, 6.0, [9, 8], gmode=1, lims_a=[0, 1], ecc_uv=0.5),
+        "pl_xy": SF.rotate_x(SF.translate(SF.plane([7, 9], gmode=0, lims_a=[-3, 3]), 1, 2, 3), 30),
+        "pl_uv": SF.plane([7, 9], gmode=1, lims_a=[0, 3]),
+        "aoe": SF.farfield([11, 9], [-5, 5], [-4, 4]),
+        "par_rms": dict(SF.paraboloid(0.25, [13, 13], gmode=0, lims_a=[-1, 1]), rms=0.01, rms_seed=7),
+    }
+    gdata = {}
+    for name, d in grids.items():
+        gdata[f"{name}_json"] = dict_to_json(d)
+        gdata[f"{name}_grid"] = ref.grid(d)
+    np.savez_compressed(HERE / "golden_grids.npz", **gdata)
+    print("wrote grids")
+
+    # Vector Gaussian feed (reference makeGaussBeam), 3 mm, w0 10 mm on a plane.
+    plane = SF.plane([21, 21], gmode=0, lims_a=[-50, 50])
+    f, c = ref.gauss_beam(lam=3.0, w0=10.0, z=0.0, power=4 * np.pi, plane=plane)
+    f2, c2 = ref.gauss_beam(lam=1.0, w0=5.0, z=50.0, power=1.0,
+                            plane=SF.plane([15, 15], gmode=0, lims_a=[-20, 20]), mode=2)
+    np.savez_compressed(HERE / "golden_gauss.npz", plane_json=dict_to_json(plane), fields=f, currents=c,
+                        fields2=f2, currents2=c2)
+    print("wrote gauss")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,126 @@
+"""GPU edge cases against the oracle: single source / target, ragged tiles,
+multi-chunk source splits, empty sources, M = 0 kernels, large phases
+(kR ~ 1e3-1e4 rad, the regime of the benchmark configurations), determinism
+and the device error word."""
+import numpy as np
+import pytest
+
+from tests.common import PHASE_TOL, REL_L2_TOL, errors
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_case(rng, ns_shape, nt, z=3.0):
+    from pypo_gb300 import engine, surfaces as SF
+    src = SF.paraboloid(1.0, list(ns_shape), gmode=1, lims_a=[0.1, 2.0])
+    s7 = engine.generate_grid(src)
+    t7 = np.zeros((7, nt))
+    t7[0] = rng.uniform(-2, 2, nt)
+    t7[1] = rng.uniform(-2, 2, nt)
+    t7[2] = z + rng.uniform(-0.3, 0.3, nt)
+    t7[5] = -1.0
+    t7[6] = 1.0
+    cur = rng.standard_normal((12, s7.shape[1]))
+    return src, s7, t7, cur
+
+
+def _check(mode, s7, cur, gmode, ncx, ncy, t7, k, oracle_mod, t=-1.0):
+    from pypo_gb300 import engine
+    got = engine.propagate(mode, s7, cur, gmode, ncx, ncy, t7, k, 1.0, t)
+    ref = oracle_mod.run(mode, s7, cur, gmode, ncx, ncy, t7, k, 1.0, t)
+    e, p = errors(got, ref, mode)
+    assert e <= REL_L2_TOL and p <= PHASE_TOL, f"{mode}: rel L2 {e:.2e} phase {p:.2e}"
+    return got
+
+
+@pytest.mark.parametrize("ns_shape,nt", [((1, 1), 7), ((3, 4), 1), ((17, 23), 257), ((31, 33), 300),
+                                         ((64, 41), 5)])
+def test_sizes_against_oracle(cuda, lib, oracle_mod, ns_shape, nt):
+    rng = np.random.default_rng(sum(ns_shape) * 1000 + nt)
+    src, s7, t7, cur = _random_case(rng, ns_shape, nt)
+    for mode in ("EH", "JM", "EHP", "scalar"):
+        c = cur[:2] if mode == "scalar" else cur
+        _check(mode, s7, c, 1, *ns_shape, t7, 5.0, oracle_mod)
+
+
+def test_many_source_chunks(cuda, lib, oracle_mod):
+    """Few targets, many sources: the source axis is split over many CTAs."""
+    rng = np.random.default_rng(11)
+    src, s7, t7, cur = _random_case(rng, (120, 171), 40)
+    from pypo_gb300 import engine
+    engine.propagate("EH", s7, cur, 1, 120, 171, t7, 4.0)
+    assert engine.last_launches() >= 5
+    _check("EH", s7, cur, 1, 120, 171, t7, 4.0, oracle_mod)
+    _check("EH", s7, cur, 1, 120, 171, t7, 4.0, oracle_mod, t=1.0)
+
+
+def test_empty_source_gives_zero(cuda, lib):
+    from pypo_gb300 import engine
+    t7 = np.zeros((7, 10))
+    t7[2] = 1.0
+    for prec in ("mixed", "fp64"):
+        out = engine.propagate("EH", np.zeros((7, 0)), np.zeros((12, 0)), -1, 0, 0, t7, 1.0, precision=prec)
+        assert np.all(out == 0)
+
+
+def test_m_zero_kernel_matches_general_kernel(cuda, lib, oracle_mod):
+    """With M == 0 the host picks the kernel without magnetic terms."""
+    rng = np.random.default_rng(3)
+    src, s7, t7, cur = _random_case(rng, (29, 30), 200)
+    cur[6:] = 0.0
+    got = _check("EH", s7, cur, 1, 29, 30, t7, 6.0, oracle_mod)
+    assert np.abs(got[6:]).max() > 0   # H from J alone is not zero
+
+
+def test_far_field_far_off_origin(cuda, lib, oracle_mod):
+    """FF keeps the coordinate origin as phase reference; a displaced dish."""
+    from pypo_gb300 import engine, surfaces as SF
+    src = SF.translate(SF.paraboloid(100.0, [25, 24], gmode=1, lims_a=[0, 60]), 40.0, -30.0, 25.0)
+    s7 = engine.generate_grid(src)
+    ff = engine.generate_grid(SF.farfield([9, 7], [-3, 3], [-2, 2]))
+    rng = np.random.default_rng(8)
+    cur = rng.standard_normal((12, s7.shape[1]))
+    for t in (-1.0, 1.0):
+        _check("FF", s7, cur, 1, 25, 24, ff, 2 * np.pi / 1.0, oracle_mod, t)
+
+
+def test_large_phase_nearfield(cuda, lib, oracle_mod):
+    """Paraboloid D = 1000 mm, f = 500 mm at 1 mm wavelength (kR ~ 3e3 rad),
+    focal-plane targets: the benchmark's EH regime on a reduced grid."""
+    from pypo_gb300 import engine, surfaces as SF
+    src = SF.paraboloid(500.0, [61, 60], gmode=1, lims_a=[0, 500])
+    s7 = engine.generate_grid(src)
+    tgt = SF.translate(SF.plane([11, 11], gmode=0, lims_a=[-50, 50]), dz=500.0)
+    t7 = engine.generate_grid(tgt)
+    r = np.hypot(s7[0], s7[1])
+    amp = np.exp(-0.5 * np.log(10) * (r / 500.0) ** 2)
+    phase = np.random.default_rng(2).normal(0, 0.05, r.size)
+    cur = np.zeros((12, r.size))
+    cur[0] = amp * np.cos(phase)
+    cur[3] = amp * np.sin(phase)
+    k = 2 * np.pi / 1.0
+    for mode in ("EH", "JM"):
+        _check(mode, s7, cur, 1, 61, 60, t7, k, oracle_mod)
+
+
+def test_large_phase_farfield(cuda, lib, oracle_mod):
+    """Paraboloid D = 2000 mm, f = 800 mm at 1 mm wavelength (k r' ~ 6e3 rad)."""
+    from pypo_gb300 import engine, surfaces as SF
+    src = SF.paraboloid(800.0, [41, 40], gmode=1, lims_a=[0, 1000])
+    s7 = engine.generate_grid(src)
+    ff = engine.generate_grid(SF.farfield([9, 9], [-0.5, 0.5], [-0.5, 0.5]))
+    r = np.hypot(s7[0], s7[1])
+    cur = np.zeros((12, r.size))
+    cur[0] = np.exp(-0.5 * np.log(10) * (r / 1000.0) ** 2)
+    _check("FF", s7, cur, 1, 41, 40, ff, 2 * np.pi, oracle_mod)
+
+
+def test_deterministic_and_clean_error_word(cuda, lib):
+    import torch
+    from pypo_gb300 import engine
+    rng = np.random.default_rng(1)
+    src, s7, t7, cur = _random_case(rng, (40, 50), 333)
+    a = engine.propagate("JMEH", s7, cur, 1, 40, 50, t7, 3.0)
+    b = engine.propagate("JMEH", s7, cur, 1, 40, 50, t7, 3.0)
+    np.testing.assert_array_equal(a, b)
+    assert engine.device_error(torch.cuda.current_stream()) == 0

@@ -1,0 +1,113 @@
+"""GPU parity: libpo_gb300 against the reference's own FP64 outputs.
+
+Every mode, both time directions, both precisions, through the explicit-grid
+C-ABI (po_run_d), the device-pointer C-ABI (po_run_dev) and the drop-in
+float ABI (callKernelf_* via PyPO_GPUf). The bar: mixed precision within
+1e-5 relative L2 and 1e-4 rad phase (components within 20 dB of the peak);
+the plain FP64 path within 1e-10.
+"""
+import numpy as np
+import pytest
+
+from tests.common import FP64_TOL, PHASE_TOL, REL_L2_TOL, errors, load_case
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("paruv_to_plane", ["JM", "EH", "JMEH", "EHP", "scalar"]),
+         ("parxy_to_plane", ["EH", "JMEH"]),
+         ("paruv_to_ff", ["FF"]),
+         ("hyp_to_ell", ["JM", "EH", "EHP"])]
+
+
+def _run(c, mode, t, precision):
+    from pypo_gb300 import engine
+    src = c["src"]
+    cur = c["cur"][:2] if mode == "scalar" else c["cur"]
+    return engine.propagate(mode, c["src_grid"], cur, src["gmode"], *src["gridsize"], c["tgt_grid"],
+                            float(c["k"]), float(c["epsilon"]), t, precision)
+
+
+@pytest.mark.parametrize("name,modes", CASES)
+def test_mixed_precision_matches_reference(cuda, lib, name, modes):
+    c = load_case(name)
+    for mode in modes:
+        for tag, t in (("fwd", -1.0), ("bwd", 1.0)):
+            ref = c[f"out_{mode}_{tag}"]
+            got = _run(c, mode, t, "mixed")
+            e, p = errors(got, ref, mode)
+            assert e <= REL_L2_TOL, f"{name} {mode} {tag}: rel L2 {e:.3e}"
+            assert p <= PHASE_TOL, f"{name} {mode} {tag}: phase {p:.3e} rad"
+
+
+@pytest.mark.parametrize("name,modes", CASES)
+def test_fp64_path_matches_reference(cuda, lib, name, modes):
+    c = load_case(name)
+    for mode in modes:
+        for tag, t in (("fwd", -1.0), ("bwd", 1.0)):
+            ref = c[f"out_{mode}_{tag}"]
+            got = _run(c, mode, t, "fp64")
+            np.testing.assert_allclose(got, ref, rtol=0, atol=FP64_TOL * np.abs(ref).max(),
+                                       err_msg=f"{name} {mode} {tag}")
+
+
+def test_device_entry_equals_host_entry(cuda, lib):
+    import torch
+    from pypo_gb300 import engine
+    c = load_case("paruv_to_plane")
+    src = c["src"]
+    for mode in ("EH", "JMEH", "EHP", "scalar"):
+        cur = c["cur"][:2] if mode == "scalar" else c["cur"]
+        host = engine.propagate(mode, c["src_grid"], cur, src["gmode"], *src["gridsize"], c["tgt_grid"],
+                                float(c["k"]), float(c["epsilon"]), -1.0)
+        dev = engine.propagate_dev(mode, torch.tensor(c["src_grid"], device=cuda), torch.tensor(cur, device=cuda),
+                                   src["gmode"], *src["gridsize"], torch.tensor(c["tgt_grid"], device=cuda),
+                                   float(c["k"]), float(c["epsilon"]), -1.0)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(dev.cpu().numpy(), host)
+    assert engine.device_error(torch.cuda.current_stream()) == 0
+
+
+def _currents_obj(cur, shape, k):
+    from pypo_gb300 import PyPOTypes as PT
+    comps = [(cur[6 * g + a] + 1j * cur[6 * g + 3 + a]).reshape(shape) for g in range(2) for a in range(3)]
+    obj = PT.currents(*comps)
+    obj.setMeta("src", k)
+    return obj
+
+
+@pytest.mark.parametrize("name,modes", CASES)
+def test_drop_in_float_abi(cuda, lib, name, modes):
+    """PyPO_GPUf -> callKernelf_*: the reference's own binding call shape."""
+    from pypo_gb300 import BindGPU, PyPOTypes as PT
+    from pypo_gb300 import marshal as M
+    c = load_case(name)
+    src, tgt = c["src"], c["tgt"]
+    shape = tuple(int(v) for v in src["gridsize"])
+    for mode in modes:
+        for tag in ("fwd", "bwd"):
+            d = {"mode": mode, "exp": tag, "epsilon": float(c["epsilon"]), "k": float(c["k"])}
+            if mode == "scalar":
+                sf = PT.scalarfield((c["cur"][0] + 1j * c["cur"][1]).reshape(shape))
+                sf.setMeta("src", float(c["k"]))
+                d["s_scalarfield"] = sf
+            else:
+                d["s_current"] = _currents_obj(c["cur"], shape, float(c["k"]))
+            out = BindGPU.PyPO_GPUf(src, tgt, d)
+            if mode in ("JM", "EH", "FF"):
+                got = M.currents_block(out.stack())
+            elif mode == "JMEH":
+                got = np.concatenate([M.currents_block(out[0].stack()), M.currents_block(out[1].stack())])
+            elif mode == "EHP":
+                got = np.concatenate([M.currents_block(out[0].stack()), np.stack([out[1].x, out[1].y, out[1].z]).reshape(3, -1)])
+            else:
+                got = np.stack([out.S.real.ravel(), out.S.imag.ravel()])
+            ref = c[f"out_{mode}_{tag}"]
+            e, p = errors(got, ref, mode)
+            # float currents and float outputs add ~1e-7 on top of the kernel error
+            assert e <= REL_L2_TOL, f"{name} {mode} {tag}: rel L2 {e:.3e}"
+            assert p <= PHASE_TOL, f"{name} {mode} {tag}: phase {p:.3e}"
+            # PyPO_GPUd (FP64 inputs) too
+            got_d = BindGPU.PyPO_GPUd(src, tgt, d)
+            if mode == "EH":
+                e2, _ = errors(M.currents_block(got_d.stack()), ref, mode)
+                assert e2 <= REL_L2_TOL
