@@ -32,7 +32,7 @@ def build(quiet=True):
     import subprocess
     src = HERE / "po_oracle.c"
     tmp = str(LIB_PATH) + ".tmp"
-    cmd = ["gcc", "-O2", "-std=c11", "-shared", "-fPIC", "-pthread", str(src), "-o", tmp, "-lm"]
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-std=c11", "-shared", "-fPIC", "-pthread", str(src), "-o", tmp, "-lm"]
     subprocess.run(cmd, check=True, capture_output=quiet)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH

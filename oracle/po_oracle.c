@@ -53,6 +53,7 @@ typedef struct {
     const double *src;  /* 7*ns: x, y, z, nx, ny, nz, area */
     const double *cur;  /* 12*ns in c2Bundle order, or 2*ns (re, im) for scalar */
     int gmode, ncx, ncy;
+    int unit_w;         /* gmode < 0: explicit point cloud, unit weights */
     long nt;
     const double *tgt;  /* 7*nt: x, y, z, nx, ny, nz, area */
     const long *tidx;   /* optional subset of target indices */
@@ -67,9 +68,11 @@ typedef struct {
 
 static double or_half_weight(int gmode, int ncx, int ncy, int xu, int yv, int *yhalf)
 {
-    *yhalf = (gmode != 1) && (yv == 0 || yv == ncy - 1);
-    return (xu == 0 || xu == ncx - 1) ? 0.5 : 1.0;
+    *yhalf = (gmode >= 0) && (gmode != 1) && (yv == 0 || yv == ncy - 1);
+    return (gmode >= 0 && (xu == 0 || xu == ncx - 1)) ? 0.5 : 1.0;
 }
+
+static double or_x_weight(const void *job, int xu);
 
 /* Near-field E and H at one target point. Propagation.h:977-1144. */
 static void or_field_at_point(const or_job *jb, const double pt[3], cplx e[3], cplx h[3])
@@ -120,7 +123,7 @@ static void or_field_at_point(const or_job *jb, const double pt[3], cplx e[3], c
                 yh[q] += w * (ms[q] * s1 + mdr * rh[q] * s2 - jxr[q] * s3) * green;
             }
         }
-        double wx = (xu == 0 || xu == jb->ncx - 1) ? 0.5 : 1.0;
+        double wx = or_x_weight(jb, xu);
         for (int q = 0; q < 3; ++q) { e[q] += wx * ye[q]; h[q] += wx * yh[q]; }
     }
 }
@@ -163,7 +166,7 @@ static void or_farfield_at_point(const or_job *jb, const double rh[3], cplx e[3]
                 yh[q] += w * (ms[q] - mdr * rh[q] - t * rxj[q]) * green;
             }
         }
-        double wx = (xu == 0 || xu == jb->ncx - 1) ? 0.5 : 1.0;
+        double wx = or_x_weight(jb, xu);
         for (int q = 0; q < 3; ++q) { e[q] += wx * ye[q]; h[q] += wx * yh[q]; }
     }
 }
@@ -188,9 +191,16 @@ static cplx or_scalar_at_point(const or_job *jb, const double pt[3])
             (void)or_half_weight(jb->gmode, jb->ncx, jb->ncy, xu, yv, &yhalf);
             yf += yhalf ? 0.5 * term : term;
         }
-        out += (xu == 0 || xu == jb->ncx - 1) ? 0.5 * yf : yf;
+        out += or_x_weight(jb, xu) * yf;
     }
     return out;
+}
+
+static double or_x_weight(const void *job, int xu)
+{
+    const or_job *jb = (const or_job *)job;
+    if (jb->unit_w) return 1.0;
+    return (xu == 0 || xu == jb->ncx - 1) ? 0.5 : 1.0;
 }
 
 static void or_norm(const double v[3], double o[3])
@@ -318,7 +328,15 @@ int po_oracle_run(int mode, long ns, const double *src, const double *cur,
                   long nt, const double *tgt, const long *tidx, long nidx,
                   double k, double epsilon, double t_dir, int nthreads, double *out)
 {
-    if (mode < 0 || mode > 5 || ns < 0 || nt < 0 || (long)ncx * ncy != ns) return 1;
+    if (mode < 0 || mode > 5 || ns < 0 || nt < 0) return 1;
+    int unit_w = 0;
+    if (gmode < 0) {   /* point cloud: one row of ns points, unit weights (not a reference mode) */
+        unit_w = 1;
+        ncx = ns > 0 ? 1 : 0;
+        ncy = (int)ns;
+    } else if ((long)ncx * ncy != ns) {
+        return 1;
+    }
     if (nthreads < 1) nthreads = 1;
     /* Constants: float literals widened to double, Propagation.h:196-203. */
     const double pif = (double)3.14159265359f;
@@ -337,6 +355,7 @@ int po_oracle_run(int mode, long ns, const double *src, const double *cur,
     base.gmode = gmode;
     base.ncx = ncx;
     base.ncy = ncy;
+    base.unit_w = unit_w;
     base.nt = nt;
     base.tgt = tgt;
     base.tidx = tidx;

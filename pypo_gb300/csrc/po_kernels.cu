@@ -143,8 +143,10 @@ __device__ __forceinline__ void nf_pair(float *acc, const float4 &tA, const floa
     __sincosf(f * 6.28318530717958647f, &sn, &cs);
     // Unnormalised separation and the illumination test n . d >= 0.
     const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
+    // Pairs within rounding of exact tangency count as lit (the reference
+    // keeps n . R_hat == 0), so regular grids with tangent pairs agree.
     const float ndd = fmaf(r[5].x, dz, fmaf(r1.w, dy, r0.w * dx));
-    const bool lit = ndd >= 0.0f;
+    const bool lit = ndd >= -kTangentTol32 * Rh;
     const float gc = lit ? cs : 0.0f;
     const float gs = lit ? (T > 0 ? sn : -sn) : 0.0f;   // G = e^{t j theta}
     // s1 = t u^2 + j (u^3 - u); s2 = -3 s1 - 2 j u; s3 = -u^2 + j t u; u = 1/(kR).
@@ -229,7 +231,7 @@ __device__ __forceinline__ void ff_pair(float *acc, const float4 &tA, const floa
     float sn, cs;
     __sincosf(f * 6.28318530717958647f, &sn, &cs);
     const float ndr = fmaf(r[5].x, rr.z, fmaf(r1.w, rr.y, r0.w * rr.x));
-    const bool lit = ndr >= 0.0f;
+    const bool lit = ndr >= -kTangentTol32;
     const float gc = lit ? cs : 0.0f;
     const float gs = lit ? (T > 0 ? -sn : sn) : 0.0f;   // G = e^{-t j theta}
     acc[0] += gc * r2.x - gs * r2.y;
@@ -585,9 +587,16 @@ po_fp64_kernel(const double *__restrict__ src, long ns, const double *__restrict
             const double *r = tile + s * kRecD;
             if (KIND == kKindNF) {
                 const double dx = p[0] - r[0], dy = p[1] - r[1], dz = p[2] - r[2];
-                const double R = sqrt(dx * dx + dy * dy + dz * dz);
-                const double rinv = 1.0 / R;
-                if (r[3] * dx + r[4] * dy + r[5] * dz < 0) continue;
+                // Illumination test in the reference's own operation order and
+                // rounding (R_hat = d * (1/R), then n . R_hat summed left to
+                // right, no FMA), so tangent pairs are decided as it decides them.
+                const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                      __dmul_rn(dz, dz)));
+                const double rinv = __ddiv_rn(1.0, R);
+                const double ndr = __dadd_rn(__dadd_rn(__dmul_rn(r[3], __dmul_rn(dx, rinv)),
+                                                       __dmul_rn(r[4], __dmul_rn(dy, rinv))),
+                                             __dmul_rn(r[5], __dmul_rn(dz, rinv)));
+                if (ndr < 0.0) continue;
                 double sn, cs;
                 sincos(k * R, &sn, &cs);
                 const double gc = cs, gs = t * sn;
@@ -618,7 +627,9 @@ po_fp64_kernel(const double *__restrict__ src, long ns, const double *__restrict
                     acc[9 + c] += c1r * M[2 * c + 1] + c1i * M[2 * c] + Qi * d[c] - (c3r * jxi + c3i * jxr);
                 }
             } else if (KIND == kKindFF) {
-                if (r[3] * p[0] + r[4] * p[1] + r[5] * p[2] < 0) continue;
+                if (__dadd_rn(__dadd_rn(__dmul_rn(r[3], p[0]), __dmul_rn(r[4], p[1])), __dmul_rn(r[5], p[2])) <
+                    0.0)
+                    continue;
                 double sn, cs;
                 sincos(k * (r[0] * p[0] + r[1] * p[1] + r[2] * p[2]), &sn, &cs);
                 const double gc = cs, gs = -t * sn;

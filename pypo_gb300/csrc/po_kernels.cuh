@@ -31,6 +31,12 @@ constexpr int kRecD = 18;       // x y z nx ny nz, J' 6, M' 6 (doubles)
 constexpr int kBboxThreads = 256;
 constexpr int kBboxBlocks = 152;
 
+// Illumination test of the mixed-precision kernels: n . R_hat >= -tol, a
+// few FP32 ulps of slack so that pairs tangent in exact arithmetic (n . d == 0,
+// which the reference keeps when its FP64 rounding gives +0) are kept. The
+// FP64 kernel instead repeats the reference's own rounding.
+constexpr float kTangentTol32 = 5e-7f;
+
 // Device error codes (written to the call's error word).
 constexpr int kErrWaitTimeout = 101;
 

@@ -34,13 +34,18 @@ def cases():
     par_uv = SF.paraboloid(0.25, [13, 12], gmode=1, lims_a=[0, 1])          # coeffs (1, 1), as the templates
     par_xy = SF.paraboloid(0.25, [13, 13], gmode=0, lims_a=[-1, 1])
     pl_tgt = SF.translate(SF.plane([13, 13], gmode=0, lims_a=[-1.5, 1.5]), dz=2.5)
+    # Off-dyadic target: no source-target pair is tangent in exact arithmetic.
+    pl_off = SF.translate(SF.plane([13, 13], gmode=0, lims_a=[-1.45, 1.45]), dz=2.45)
     hyp = SF.hyperboloid(2.0, 2.0, 3.0, [11, 10], gmode=1, lims_a=[0, 1.5])
     ell = SF.translate(SF.ellipsoid(3.0, 3.0, 5.0, [9, 11], gmode=0, lims_a=[-1, 1]), dz=8.0)
     ell = dict(ell, flip=True)
     ff = SF.farfield([11, 9], [-8, 8], [-6, 6])
     return [
         ("paruv_to_plane", par_uv, pl_tgt, ["JM", "EH", "JMEH", "EHP", "scalar"]),
-        ("parxy_to_plane", par_xy, pl_tgt, ["EH", "JMEH"]),
+        ("parxy_to_plane", par_xy, pl_off, ["EH", "JMEH"]),
+        # Dyadic grids: 36 pairs are exactly tangent (n . d == 0); the reference
+        # skips the ones whose rounded n . R_hat comes out negative.
+        ("tangent", par_xy, pl_tgt, ["EH"]),
         ("paruv_to_ff", par_uv, ff, ["FF"]),
         ("hyp_to_ell", hyp, ell, ["JM", "EH", "EHP"]),
     ]

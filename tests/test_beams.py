@@ -1,0 +1,18 @@
+"""The vector Gaussian feed (pypo_gb300.beams) against the reference's
+makeGaussBeam outputs (golden vectors), full and PEC modes."""
+import numpy as np
+
+from tests.common import GOLDEN, from_json
+
+
+def test_gauss_beam_matches_reference(lib):
+    from pypo_gb300 import beams, engine, surfaces as SF
+    g = np.load(GOLDEN / "golden_gauss.npz")
+    s7 = engine.generate_grid(from_json(str(g["plane_json"])))
+    f, c = beams.gauss_beam(s7, 3.0, 10.0, 0.0, 4 * np.pi)
+    np.testing.assert_allclose(f, g["fields"], rtol=0, atol=1e-13 * np.abs(g["fields"]).max())
+    np.testing.assert_allclose(c, g["currents"], rtol=0, atol=1e-13 * np.abs(g["currents"]).max())
+    s7b = engine.generate_grid(SF.plane([15, 15], gmode=0, lims_a=[-20, 20]))
+    f2, c2 = beams.gauss_beam(s7b, 1.0, 5.0, 50.0, 1.0, mode=2)
+    np.testing.assert_allclose(c2, g["currents2"], rtol=0, atol=1e-13 * np.abs(g["currents2"]).max())
+    assert np.all(c2[6:] == 0)   # PEC mode: no magnetic current

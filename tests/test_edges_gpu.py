@@ -33,7 +33,7 @@ def _check(mode, s7, cur, gmode, ncx, ncy, t7, k, oracle_mod, t=-1.0):
     return got
 
 
-@pytest.mark.parametrize("ns_shape,nt", [((1, 1), 7), ((3, 4), 1), ((17, 23), 257), ((31, 33), 300),
+@pytest.mark.parametrize("ns_shape,nt", [((2, 2), 7), ((3, 4), 1), ((17, 23), 257), ((31, 33), 300),
                                          ((64, 41), 5)])
 def test_sizes_against_oracle(cuda, lib, oracle_mod, ns_shape, nt):
     rng = np.random.default_rng(sum(ns_shape) * 1000 + nt)
@@ -41,6 +41,20 @@ def test_sizes_against_oracle(cuda, lib, oracle_mod, ns_shape, nt):
     for mode in ("EH", "JM", "EHP", "scalar"):
         c = cur[:2] if mode == "scalar" else cur
         _check(mode, s7, c, 1, *ns_shape, t7, 5.0, oracle_mod)
+
+
+def test_single_source_point(cuda, lib, oracle_mod):
+    """One source element (explicit point, unit weight) against many targets."""
+    rng = np.random.default_rng(4)
+    s7 = np.array([[0.1], [-0.2], [0.05], [0.0], [0.0], [1.0], [0.01]])
+    t7 = np.zeros((7, 50))
+    t7[0:2] = rng.uniform(-1, 1, (2, 50))
+    t7[2] = rng.uniform(0.5, 2.0, 50)
+    t7[5] = 1.0
+    cur = rng.standard_normal((12, 1))
+    for mode in ("EH", "JMEH", "scalar"):
+        c = cur[:2] if mode == "scalar" else cur
+        _check(mode, s7, c, -1, 0, 0, t7, 7.0, oracle_mod)
 
 
 def test_many_source_chunks(cuda, lib, oracle_mod):

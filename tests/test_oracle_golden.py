@@ -14,7 +14,8 @@ from tests.common import load_case
 CASES = [("paruv_to_plane", ["JM", "EH", "JMEH", "EHP", "scalar"]),
          ("parxy_to_plane", ["EH", "JMEH"]),
          ("paruv_to_ff", ["FF"]),
-         ("hyp_to_ell", ["JM", "EH", "EHP"])]
+         ("hyp_to_ell", ["JM", "EH", "EHP"]),
+         ("tangent", ["EH"])]
 
 
 @pytest.mark.parametrize("name,modes", CASES)

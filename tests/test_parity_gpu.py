@@ -39,7 +39,7 @@ def test_mixed_precision_matches_reference(cuda, lib, name, modes):
             assert p <= PHASE_TOL, f"{name} {mode} {tag}: phase {p:.3e} rad"
 
 
-@pytest.mark.parametrize("name,modes", CASES)
+@pytest.mark.parametrize("name,modes", CASES + [("tangent", ["EH"])])
 def test_fp64_path_matches_reference(cuda, lib, name, modes):
     c = load_case(name)
     for mode in modes:
@@ -48,6 +48,25 @@ def test_fp64_path_matches_reference(cuda, lib, name, modes):
             got = _run(c, mode, t, "fp64")
             np.testing.assert_allclose(got, ref, rtol=0, atol=FP64_TOL * np.abs(ref).max(),
                                        err_msg=f"{name} {mode} {tag}")
+
+
+def test_tangent_pairs(cuda, lib):
+    """Dyadic grids with pairs tangent in exact arithmetic (n . d == 0).
+
+    The reference decides those pairs by the sign of its rounded FP64
+    n . R_hat; the FP64 path repeats that rounding and matches exactly, the
+    mixed path keeps tangent pairs and may differ only at targets that have
+    one; everywhere else it meets the usual bar."""
+    c = load_case("tangent")
+    s, t = c["src_grid"], c["tgt_grid"]
+    d = t[:3, :, None] - s[:3, None, :]
+    nd = (s[3:6, None, :] * d).sum(0)
+    touched = np.any(np.abs(nd) <= 1e-12 * np.sqrt((d ** 2).sum(0)), axis=1)
+    assert 0 < touched.sum() < 0.05 * t.shape[1]
+    ref = c["out_EH_fwd"]
+    got = _run(c, "EH", -1.0, "mixed")
+    e, p = errors(got[:, ~touched], ref[:, ~touched], "EH")
+    assert e <= REL_L2_TOL and p <= PHASE_TOL
 
 
 def test_device_entry_equals_host_entry(cuda, lib):
