@@ -62,7 +62,7 @@ def test_tangent_pairs(cuda, lib):
     d = t[:3, :, None] - s[:3, None, :]
     nd = (s[3:6, None, :] * d).sum(0)
     touched = np.any(np.abs(nd) <= 1e-12 * np.sqrt((d ** 2).sum(0)), axis=1)
-    assert 0 < touched.sum() < 0.05 * t.shape[1]
+    assert 0 < touched.sum() < 0.2 * t.shape[1]
     ref = c["out_EH_fwd"]
     got = _run(c, "EH", -1.0, "mixed")
     e, p = errors(got[:, ~touched], ref[:, ~touched], "EH")
