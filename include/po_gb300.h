@@ -175,6 +175,26 @@ int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int nc
                double k, double epsilon, double t_direction, int precision, int flags,
                double *out, void *stream);
 
+/* ---- allocation-free device entry ------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory: a framework that reserves the GPU's memory for its own pool (an
+ * allocation from inside it fails or fragments that pool), or a
+ * latency-critical loop that cannot take the device-wide synchronisation of
+ * cudaFree. Same arguments and results as po_run_dev in mixed precision, plus
+ * `status`: an optional device int, cleared at the start of the call and set
+ * to 101 if a kernel gave up a bounded wait (NULL: an internal word).
+ * The scratch is a fixed 64 MiB device array inside the library, held by
+ * every GPU that loads it until the process exits; problems needing more
+ * (about 96*ns + 128*nt bytes, plus 96*nt per extra source chunk) are
+ * rejected with status 5 and a message. The first call on a device looks up
+ * that array's address: make it before any stream capture. All calls share
+ * the array, so calls that overlap on the GPU race; the caller serialises
+ * them. Calls no cudaMalloc/cudaFree or other allocating routine. */
+int po_run_dev_static(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
+                      const double *cur, long nt, const double *tgt7,
+                      double k, double epsilon, double t_direction, int flags,
+                      double *out, int *status, void *stream);
+
 /* Number of kernel launches the last call on this thread queued. */
 int po_last_launches(void);
 
