@@ -12,7 +12,7 @@ LIB_PATH = pathlib.Path(__file__).resolve().parent / "libpo_gb300.so"
 
 #: every symbol declared in include/po_gb300.h
 EXPORTS = ("po_last_error", "po_n_out", "po_last_launches", "po_generate_grid", "po_run_d",
-           "po_run_dev", "po_run_dev_static", "po_device_error", "po_timing_enable", "po_timing_collect", "po_fp32_probe",
+           "po_run_dev", "po_run_dev_static", "po_adjoint_dev", "po_adjoint_d", "po_device_error", "po_timing_enable", "po_timing_collect", "po_fp32_probe",
            "callKernelf_JM", "callKernelf_EH", "callKernelf_JMEH", "callKernelf_EHP",
            "callKernelf_FF", "callKernelf_scalar")
 
@@ -58,6 +58,13 @@ def load():
     lib.po_run_dev_static.argtypes = [c_int, c_long, c_void_p, c_int, c_int, c_int, c_void_p, c_long,
                                       c_void_p, c_double, c_double, c_double, c_int, c_void_p, c_void_p,
                                       c_void_p]
+    lib.po_adjoint_dev.restype = c_int
+    lib.po_adjoint_dev.argtypes = [c_int, c_long, c_void_p, c_int, c_int, c_int, c_void_p, c_long, c_void_p,
+                                   c_double, c_double, c_double, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_void_p]
+    lib.po_adjoint_d.restype = c_int
+    lib.po_adjoint_d.argtypes = [c_int, c_long, c_void_p, c_int, c_int, c_int, c_void_p, c_long, c_void_p,
+                                 c_double, c_double, c_double, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
     lib.po_device_error.restype = c_int
     lib.po_device_error.argtypes = [c_void_p, P(c_int)]
     lib.po_timing_enable.restype = c_int

@@ -1,0 +1,818 @@
+// po_adjoint.cu -- adjoint (vector-Jacobian) kernels of the PO integrator.
+//
+// The reference has no derivatives; these kernels are new. For a real loss
+// L of the outputs with real cotangent rows y_bar, write gE = y_bar(E.re) +
+// j y_bar(E.im) and gH likewise (after mapping the mode's epilogue back onto
+// E and H). With d = r_t - r_s and the forward coefficients c1, c2' = G s2/R^2,
+// c3' = G s3/R of the near-field kernel (E = c1 J + c2'(J.d)d + c3'(M x d),
+// H = c1 M + c2'(M.d)d - c3'(J x d)):
+//
+//   currents      Jbar' = sum_t conj(c1) gE + conj(c2')(gE.d)d + conj(c3')(gH x d)
+//                 Mbar' = sum_t conj(c1) gH + conj(c2')(gH.d)d - conj(c3')(gE x d)
+//                 (primes: with respect to the folded currents; the epilogue
+//                 multiplies by conj(prefactor * weight * area))
+//   displacement  phi(d) = Re[a.F_E + b.F_H], a = conj(gE), b = conj(gH);
+//                 grad_d phi = Re[sigma d + c2' grad(beta) + c3' W] with
+//                 alpha = a.J + b.M, beta = (J.d)(a.d) + (M.d)(b.d),
+//                 W = a x M - b x J, sigma = dc1 alpha + dc2 beta + dc3 (W.d),
+//                 dc1 = G/R^2 [t(1-3u^2) + j(2u-3u^3)],
+//                 dc2 = G/R^4 [-t(1-15u^2) + j(-6u+15u^3)],
+//                 dc3 = G/R^3 [-(1-3u^2) - 3jtu]   (u = 1/kR)
+//                 dL/d delta_s = -n_s . sum_t grad_d phi, dL/d delta_t = n_t . sum_s grad_d phi
+//                 (normal-direction displacement with normals and areas frozen,
+//                 the reference's surface-error convention).
+//   far field     Jbar' = sum_t conj(G) gS_J, Mbar' = sum_t conj(G) gS_M with
+//                 gS_J = P gE + t r x gH, gS_M = P gH - t r x gE (P = I - r r^T);
+//                 dL/d delta_s = n_s . sum_t Re[-t j k G (conj(gS_J).J' + conj(gS_M).M')] r.
+// The illumination mask is piecewise constant: its derivative is dropped.
+//
+// Mixed precision: the same split hi/lo separation and phase as the forward
+// kernels, the same TMA tile pipeline, float-float totals per tile. The FP64
+// kernels are the plain comparison path.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <cstdint>
+
+#include "po_device.cuh"
+#include "po_kernels.cuh"
+
+namespace po {
+
+template <typename F>
+struct cx {
+    F r, i;
+};
+
+template <typename F>
+__device__ __forceinline__ cx<F> cmul(cx<F> a, cx<F> b)
+{
+    return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
+}
+template <typename F>
+__device__ __forceinline__ cx<F> cadd(cx<F> a, cx<F> b)
+{
+    return {a.r + b.r, a.i + b.i};
+}
+template <typename F>
+__device__ __forceinline__ cx<F> csub(cx<F> a, cx<F> b)
+{
+    return {a.r - b.r, a.i - b.i};
+}
+template <typename F>
+__device__ __forceinline__ cx<F> cconj(cx<F> a)
+{
+    return {a.r, -a.i};
+}
+// complex 3-vector . real 3-vector
+template <typename F>
+__device__ __forceinline__ cx<F> cdot_r(const cx<F> *v, F x, F y, F z)
+{
+    return {v[0].r * x + v[1].r * y + v[2].r * z, v[0].i * x + v[1].i * y + v[2].i * z};
+}
+// complex 3-vector . complex 3-vector (bilinear, no conjugation)
+template <typename F>
+__device__ __forceinline__ cx<F> cdot_c(const cx<F> *a, const cx<F> *b)
+{
+    return cadd(cadd(cmul(a[0], b[0]), cmul(a[1], b[1])), cmul(a[2], b[2]));
+}
+// complex 3-vector x real 3-vector
+template <typename F>
+__device__ __forceinline__ void ccross_r(const cx<F> *v, F x, F y, F z, cx<F> *o)
+{
+    o[0] = {v[1].r * z - v[2].r * y, v[1].i * z - v[2].i * y};
+    o[1] = {v[2].r * x - v[0].r * z, v[2].i * x - v[0].i * z};
+    o[2] = {v[0].r * y - v[1].r * x, v[0].i * y - v[1].i * x};
+}
+
+// Forward coefficients (and radial derivatives) of one lit pair, in the
+// units of d (turns for the mixed kernels, mm for FP64): rinv = 1/R,
+// u = 1/(kR) given, G = (gc, gs) = e^{t j k R} (zero when not lit).
+template <typename F, int T>
+struct Coef {
+    cx<F> c1, c2, c3, d1, d2, d3;
+};
+
+template <typename F, int T, bool WANT_C1, bool WANT_D>
+__device__ __forceinline__ Coef<F, T> coefficients(F rinv, F u, F gc, F gs)
+{
+    Coef<F, T> k;
+    const cx<F> G = {gc, gs};
+    const F u2 = u * u, u3 = u2 * u;
+    const F tf = (F)T;
+    const cx<F> s1 = {tf * u2, u3 - u};
+    const cx<F> c1 = cmul(G, s1);
+    if (WANT_C1) k.c1 = c1;
+    const F rinv2 = rinv * rinv;
+    // c2' = (-3 c1 - 2 j u G) / R^2
+    k.c2 = {(-(F)3 * c1.r + (F)2 * u * gs) * rinv2, (-(F)3 * c1.i - (F)2 * u * gc) * rinv2};
+    k.c3 = cmul(G, cx<F>{-u2 * rinv, tf * u * rinv});
+    if (WANT_D) {
+        const F rinv3 = rinv2 * rinv;
+        k.d1 = cmul(G, cx<F>{tf * ((F)1 - (F)3 * u2) * rinv2, ((F)2 * u - (F)3 * u3) * rinv2});
+        k.d2 = cmul(G, cx<F>{-tf * ((F)1 - (F)15 * u2) * rinv2 * rinv2, (-(F)6 * u + (F)15 * u3) * rinv2 * rinv2});
+        k.d3 = cmul(G, cx<F>{-((F)1 - (F)3 * u2) * rinv3, -(F)3 * tf * u * rinv3});
+    }
+    return k;
+}
+
+// Per-thread constants of one source (its folded currents and normal).
+template <typename F>
+struct SrcConst {
+    cx<F> J[3], M[3];
+    F n[3];
+    cx<F> Jn, Mn;        // J.n, M.n
+    cx<F> Jxn[3], Mxn[3];
+};
+
+template <typename F, bool HAS_M>
+__device__ __forceinline__ void src_const_finish(SrcConst<F> &s)
+{
+    s.Jn = cdot_r(s.J, s.n[0], s.n[1], s.n[2]);
+    ccross_r(s.J, s.n[0], s.n[1], s.n[2], s.Jxn);
+    if (HAS_M) {
+        s.Mn = cdot_r(s.M, s.n[0], s.n[1], s.n[2]);
+        ccross_r(s.M, s.n[0], s.n[1], s.n[2], s.Mxn);
+    }
+}
+
+// Near-field source-side pair: adjoint currents (acc[0..11]) and the source
+// displacement term n_s . grad_d phi (acc[12]).
+template <typename F, int T, bool HAS_M, bool WANT_D>
+__device__ __forceinline__ void nf_adj_src_algebra(F *acc, F dx, F dy, F dz, F rinv, F u, F gc, F gs, F ndn,
+                                                   const cx<F> *gE, const cx<F> *gH, const SrcConst<F> &sc)
+{
+    const Coef<F, T> k = coefficients<F, T, true, WANT_D>(rinv, u, gc, gs);
+    const cx<F> c1c = cconj(k.c1), c2c = cconj(k.c2), c3c = cconj(k.c3);
+    const cx<F> ged = cdot_r(gE, dx, dy, dz), ghd = cdot_r(gH, dx, dy, dz);
+    const cx<F> P = cmul(c2c, ged), Q = cmul(c2c, ghd);
+    cx<F> ghxd[3], gexd[3];
+    ccross_r(gH, dx, dy, dz, ghxd);
+    ccross_r(gE, dx, dy, dz, gexd);
+    const F dv[3] = {dx, dy, dz};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const cx<F> jb = cadd(cadd(cmul(c1c, gE[c]), cx<F>{P.r * dv[c], P.i * dv[c]}), cmul(c3c, ghxd[c]));
+        const cx<F> mb = csub(cadd(cmul(c1c, gH[c]), cx<F>{Q.r * dv[c], Q.i * dv[c]}), cmul(c3c, gexd[c]));
+        acc[c] += jb.r;
+        acc[3 + c] += jb.i;
+        acc[6 + c] += mb.r;
+        acc[9 + c] += mb.i;
+    }
+    if (WANT_D) {
+        // a = conj(gE), b = conj(gH)
+        cx<F> a[3], b[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            a[c] = cconj(gE[c]);
+            b[c] = cconj(gH[c]);
+        }
+        const cx<F> ad = cconj(ged), bd = cconj(ghd);
+        const cx<F> Jd = cdot_r(sc.J, dx, dy, dz);
+        cx<F> alpha = cdot_c(a, sc.J);
+        cx<F> beta = cmul(Jd, ad);
+        cx<F> Jxd[3];
+        ccross_r(sc.J, dx, dy, dz, Jxd);
+        cx<F> Wd = {-cdot_c(b, Jxd).r, -cdot_c(b, Jxd).i};
+        cx<F> Wn = {-cdot_c(b, sc.Jxn).r, -cdot_c(b, sc.Jxn).i};
+        const cx<F> an = cdot_r(a, sc.n[0], sc.n[1], sc.n[2]);
+        cx<F> gbn = cadd(cmul(ad, sc.Jn), cmul(Jd, an));
+        if (HAS_M) {
+            const cx<F> Md = cdot_r(sc.M, dx, dy, dz);
+            alpha = cadd(alpha, cdot_c(b, sc.M));
+            beta = cadd(beta, cmul(Md, bd));
+            cx<F> Mxd[3];
+            ccross_r(sc.M, dx, dy, dz, Mxd);
+            Wd = cadd(Wd, cdot_c(a, Mxd));
+            Wn = cadd(Wn, cdot_c(a, sc.Mxn));
+            const cx<F> bn = cdot_r(b, sc.n[0], sc.n[1], sc.n[2]);
+            gbn = cadd(gbn, cadd(cmul(bd, sc.Mn), cmul(Md, bn)));
+        }
+        const cx<F> sig = cadd(cadd(cmul(k.d1, alpha), cmul(k.d2, beta)), cmul(k.d3, Wd));
+        acc[12] += sig.r * ndn + cmul(k.c2, gbn).r + cmul(k.c3, Wn).r;
+    }
+}
+
+// Near-field target-side pair: n_t . grad_d phi for one source (J, M, d).
+template <typename F, int T, bool HAS_M>
+__device__ __forceinline__ F nf_adj_tgt_algebra(F dx, F dy, F dz, F rinv, F u, F gc, F gs, F ndn,
+                                                const cx<F> *a, const cx<F> *b, const cx<F> *nxa,
+                                                const cx<F> *nxb, cx<F> an, cx<F> bn, const F *n,
+                                                const cx<F> *J, const cx<F> *M)
+{
+    const Coef<F, T> k = coefficients<F, T, false, true>(rinv, u, gc, gs);
+    const cx<F> Jd = cdot_r(J, dx, dy, dz);
+    const cx<F> ad = cdot_r(a, dx, dy, dz);
+    cx<F> alpha = cdot_c(a, J);
+    cx<F> beta = cmul(Jd, ad);
+    // W.d = M.(d x a) - J.(d x b);  W.n = M.(n x a) - J.(n x b)
+    cx<F> dxb[3];
+    {
+        cx<F> t3[3];
+        ccross_r(b, dx, dy, dz, t3);   // b x d = -(d x b)
+        dxb[0] = {-t3[0].r, -t3[0].i};
+        dxb[1] = {-t3[1].r, -t3[1].i};
+        dxb[2] = {-t3[2].r, -t3[2].i};
+    }
+    cx<F> Wd = {-cdot_c(J, dxb).r, -cdot_c(J, dxb).i};
+    cx<F> Wn = {-cdot_c(J, nxb).r, -cdot_c(J, nxb).i};
+    const cx<F> Jn = cdot_r(J, n[0], n[1], n[2]);
+    cx<F> gbn = cadd(cmul(ad, Jn), cmul(Jd, an));
+    if (HAS_M) {
+        const cx<F> Md = cdot_r(M, dx, dy, dz);
+        const cx<F> bd = cdot_r(b, dx, dy, dz);
+        alpha = cadd(alpha, cdot_c(b, M));
+        beta = cadd(beta, cmul(Md, bd));
+        cx<F> dxa[3];
+        {
+            cx<F> t3[3];
+            ccross_r(a, dx, dy, dz, t3);
+            dxa[0] = {-t3[0].r, -t3[0].i};
+            dxa[1] = {-t3[1].r, -t3[1].i};
+            dxa[2] = {-t3[2].r, -t3[2].i};
+        }
+        Wd = cadd(Wd, cdot_c(M, dxa));
+        Wn = cadd(Wn, cdot_c(M, nxa));
+        const cx<F> Mn = cdot_r(M, n[0], n[1], n[2]);
+        gbn = cadd(gbn, cadd(cmul(bd, Mn), cmul(Md, bn)));
+    }
+    const cx<F> sig = cadd(cadd(cmul(k.d1, alpha), cmul(k.d2, beta)), cmul(k.d3, Wd));
+    return sig.r * ndn + cmul(k.c2, gbn).r + cmul(k.c3, Wn).r;
+}
+
+// ------------------------------------------------------------- tile driver
+
+// Streams records [s0, s1) of `rec` (REC float4 each) through shared memory,
+// calling body(acc, record) for each and folding tile partials into hi/lo.
+// Returns false (after setting *err) if a tile wait timed out.
+template <int REC, int NACC, class Body>
+__device__ __forceinline__ bool stream_tiles(const float4 *__restrict__ rec, long s0, long s1, float4 *stage,
+                                             uint64_t *full, float (&hi)[NACC], float (&lo)[NACC], int *err,
+                                             Body &&body)
+{
+    const int ntiles = s1 > s0 ? (int)((s1 - s0 + kTile - 1) / kTile) : 0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int it) {
+        const long first = s0 + (long)it * kTile;
+        const long cnt = min((long)kTile, s1 - first);
+        const uint32_t bytes = (uint32_t)(cnt * REC * sizeof(float4));
+        uint64_t *bar = &full[it % kStages];
+        fence_proxy_async();
+        mbar_expect_tx(bar, bytes);
+        tma_load_1d(stage + (size_t)(it % kStages) * kTile * REC, rec + first * REC, bytes, bar);
+    };
+    if (threadIdx.x == 0)
+        for (int it = 0; it < ntiles && it < kStages; ++it) issue(it);
+    for (int it = 0; it < ntiles; ++it) {
+        const bool ok = mbar_wait_bounded(&full[it % kStages], (uint32_t)((it / kStages) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicExch(err, kErrWaitTimeout);
+                for (int s = 0; s < kStages; ++s) (void)mbar_wait_bounded(&full[s], 0);
+            }
+            return false;
+        }
+        const float4 *tile = stage + (size_t)(it % kStages) * kTile * REC;
+        const int cnt = (int)min((long)kTile, s1 - (s0 + (long)it * kTile));
+        float acc[NACC];
+#pragma unroll
+        for (int a = 0; a < NACC; ++a) acc[a] = 0.f;
+#pragma unroll 1
+        for (int s = 0; s < cnt; ++s) body(acc, tile + s * REC);
+#pragma unroll
+        for (int a = 0; a < NACC; ++a) {
+            float sm, e;
+            two_sum(hi[a], acc[a], sm, e);
+            hi[a] = sm;
+            lo[a] = __fadd_rn(lo[a], e);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
+    }
+    return true;
+}
+
+// Split-precision separation of the mixed kernels: from hi/lo target and
+// source positions (turns) to d, 1/R, the reduced phase (turns) and R.
+struct Sep {
+    float dx, dy, dz, rinv, Rh, f;
+};
+
+__device__ __forceinline__ Sep separation(float thx, float thy, float thz, float tlx, float tly, float tlz, float shx,
+                                          float shy, float shz, float slx, float sly, float slz)
+{
+    const float dhx = __fsub_rn(thx, shx), dhy = __fsub_rn(thy, shy), dhz = __fsub_rn(thz, shz);
+    const float dlx = __fsub_rn(tlx, slx), dly = __fsub_rn(tly, sly), dlz = __fsub_rn(tlz, slz);
+    const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
+    const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
+    const float R2 = __fadd_rn(S0, S1);
+    Sep s;
+    s.rinv = rsqrtf(R2);
+    s.Rh = __fmul_rn(R2, s.rinv);
+    const float p = __fmul_rn(s.Rh, s.Rh);
+    const float pe = fmaf(s.Rh, s.Rh, -p);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
+    const float Rl = __fmul_rn(res, __fmul_rn(0.5f, s.rinv));
+    s.f = __fadd_rn(__fsub_rn(s.Rh, rint_magic(s.Rh)), Rl);
+    s.dx = dhx + dlx;
+    s.dy = dhy + dly;
+    s.dz = dhz + dlz;
+    return s;
+}
+
+// ------------------------------------------------------------ mixed kernels
+
+// Source-side adjoint. Thread = one source (forward-packed record). Streams
+// the cotangent target records (kRec float4):
+//   near field: (th, 0), (tl, 0), (gEx, gEy), (gEz, gHx), (gHy, gHz), (0)
+//   far field:  (rh, rl.x), (rl.y, rl.z, 0, 0), (gSJ ...), ..., (r, 0)
+// Writes 13 accumulators per source per target chunk.
+template <int KIND, int T, bool HAS_M, bool WANT_D>
+__global__ void __launch_bounds__(kThreadsA)
+po_adj_src_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
+                  double *__restrict__ part, int *__restrict__ err)
+{
+    constexpr int NACC = kAccAdj;
+    extern __shared__ __align__(128) float4 stage[];
+    __shared__ __align__(8) uint64_t full[kStages];
+    const long si = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    float4 q[kRec];
+#pragma unroll
+    for (int c = 0; c < kRec; ++c) q[c] = si < ns ? srcpk[(size_t)kRec * si + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (si >= ns) q[0].z = 1e3f;   // idle lanes: keep R > 0
+    SrcConst<float> sc;
+    sc.n[0] = q[0].w;
+    sc.n[1] = q[1].w;
+    sc.n[2] = q[5].x;
+    sc.J[0] = {q[2].x, q[2].y};
+    sc.J[1] = {q[2].z, q[2].w};
+    sc.J[2] = {q[3].x, q[3].y};
+    sc.M[0] = {q[3].z, q[3].w};
+    sc.M[1] = {q[4].x, q[4].y};
+    sc.M[2] = {q[4].z, q[4].w};
+    if (WANT_D) src_const_finish<float, HAS_M>(sc);
+    float hi[NACC], lo[NACC];
+#pragma unroll
+    for (int a = 0; a < NACC; ++a) { hi[a] = 0.f; lo[a] = 0.f; }
+    const long t0 = (long)blockIdx.y * chunk;
+    const long t1 = min(nt, t0 + chunk);
+    const bool ok = stream_tiles<kRec, NACC>(trec, t0, t1, stage, full, hi, lo, err, [&](float *acc, const float4 *r) {
+        const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4];
+        const cx<float> gE[3] = {{r2.x, r2.y}, {r2.z, r2.w}, {r3.x, r3.y}};
+        const cx<float> gH[3] = {{r3.z, r3.w}, {r4.x, r4.y}, {r4.z, r4.w}};
+        if (KIND == kKindNF) {
+            const Sep g = separation(r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, q[0].x, q[0].y, q[0].z, q[1].x, q[1].y,
+                                     q[1].z);
+            float sn, cs;
+            __sincosf(g.f * 6.28318530717958647f, &sn, &cs);
+            const float ndd = fmaf(sc.n[2], g.dz, fmaf(sc.n[1], g.dy, sc.n[0] * g.dx));
+            const bool lit = ndd >= -kTangentTol32 * g.Rh;
+            const float gc = lit ? cs : 0.f, gs = lit ? (T > 0 ? sn : -sn) : 0.f;
+            nf_adj_src_algebra<float, T, HAS_M, WANT_D>(acc, g.dx, g.dy, g.dz, g.rinv,
+                                                       g.rinv * 0.159154943091895336f, gc, gs, ndd, gE, gH, sc);
+        } else {
+            const float4 r5 = r[5];
+            const float Ph = fmaf(q[0].z, r0.z, fmaf(q[0].y, r0.y, __fmul_rn(q[0].x, r0.x)));
+            const float Pl = fmaf(q[1].z, r5.z, fmaf(q[1].y, r5.y, fmaf(q[1].x, r5.x,
+                             fmaf(q[0].z, r1.y, fmaf(q[0].y, r1.x, q[0].x * r0.w)))));
+            const float f = __fadd_rn(__fsub_rn(Ph, rint_magic(Ph)), Pl);
+            float sn, cs;
+            __sincosf(f * 6.28318530717958647f, &sn, &cs);
+            const float ndr = fmaf(sc.n[2], r5.z, fmaf(sc.n[1], r5.y, sc.n[0] * r5.x));
+            const bool lit = ndr >= -kTangentTol32;
+            const cx<float> G = {lit ? cs : 0.f, lit ? (T > 0 ? -sn : sn) : 0.f};   // e^{-t j theta}
+            const cx<float> Gc = cconj(G);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const cx<float> jb = cmul(Gc, gE[c]), mb = cmul(Gc, gH[c]);
+                acc[c] += jb.r;
+                acc[3 + c] += jb.i;
+                acc[6 + c] += mb.r;
+                acc[9 + c] += mb.i;
+            }
+            if (WANT_D) {
+                // sigma = Re(-t j 2pi G X), X = conj(gSJ).J' + conj(gSM).M'
+                cx<float> gEc[3] = {cconj(gE[0]), cconj(gE[1]), cconj(gE[2])};
+                cx<float> X = cdot_c(gEc, sc.J);
+                if (HAS_M) {
+                    cx<float> gHc[3] = {cconj(gH[0]), cconj(gH[1]), cconj(gH[2])};
+                    X = cadd(X, cdot_c(gHc, sc.M));
+                }
+                const cx<float> Z = cmul(G, X);
+                acc[12] += (T > 0 ? 6.28318530717958647f : -6.28318530717958647f) * Z.i * ndr;
+            }
+        }
+    });
+    if (!ok || si >= ns) return;
+#pragma unroll
+    for (int a = 0; a < NACC; ++a)
+        part[((long)blockIdx.y * NACC + a) * ns + si] = (double)hi[a] + (double)lo[a];
+}
+
+// Target-side displacement adjoint (near field). Thread = one target; per
+// thread a = conj(gE), b = conj(gH) from the cotangent rows; streams the
+// forward-packed source records. One accumulator: n_t . sum_s grad_d phi.
+template <int T, bool HAS_M>
+__global__ void __launch_bounds__(kThreadsA)
+po_adj_tgt_kernel(const float4 *__restrict__ srcpk, long ns, long chunk, const float4 *__restrict__ tgtpk,
+                  const double *__restrict__ gam, const double *__restrict__ tgt7, long nt,
+                  double *__restrict__ part, int *__restrict__ err)
+{
+    extern __shared__ __align__(128) float4 stage[];
+    __shared__ __align__(8) uint64_t full[kStages];
+    const long ti = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    float4 tA = make_float4(0.f, 0.f, 1e3f, 0.f), tB = make_float4(0.f, 0.f, 0.f, 0.f);
+    float n[3] = {0.f, 0.f, 0.f};
+    cx<float> a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, b[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    if (ti < nt) {
+        tA = tgtpk[2 * ti];
+        tB = tgtpk[2 * ti + 1];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            n[c] = (float)tgt7[(3 + c) * nt + ti];
+            a[c] = {(float)gam[c * nt + ti], -(float)gam[(3 + c) * nt + ti]};
+            b[c] = {(float)gam[(6 + c) * nt + ti], -(float)gam[(9 + c) * nt + ti]};
+        }
+    }
+    cx<float> nxa[3], nxb[3];
+    {
+        // n x v = -(v x n)
+        cx<float> t3[3];
+        ccross_r(a, n[0], n[1], n[2], t3);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nxa[c] = {-t3[c].r, -t3[c].i};
+        ccross_r(b, n[0], n[1], n[2], t3);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nxb[c] = {-t3[c].r, -t3[c].i};
+    }
+    const cx<float> an = cdot_r(a, n[0], n[1], n[2]), bn = cdot_r(b, n[0], n[1], n[2]);
+    float hi[1] = {0.f}, lo[1] = {0.f};
+    const long s0 = (long)blockIdx.y * chunk;
+    const long s1 = min(ns, s0 + chunk);
+    const bool ok = stream_tiles<kRec, 1>(srcpk, s0, s1, stage, full, hi, lo, err, [&](float *acc, const float4 *r) {
+        const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4];
+        const Sep g = separation(tA.x, tA.y, tA.z, tA.w, tB.x, tB.y, r0.x, r0.y, r0.z, r1.x, r1.y, r1.z);
+        float sn, cs;
+        __sincosf(g.f * 6.28318530717958647f, &sn, &cs);
+        const float nsd = fmaf(r[5].x, g.dz, fmaf(r1.w, g.dy, r0.w * g.dx));
+        const bool lit = nsd >= -kTangentTol32 * g.Rh;
+        const float gc = lit ? cs : 0.f, gs = lit ? (T > 0 ? sn : -sn) : 0.f;
+        const cx<float> J[3] = {{r2.x, r2.y}, {r2.z, r2.w}, {r3.x, r3.y}};
+        const cx<float> M[3] = {{r3.z, r3.w}, {r4.x, r4.y}, {r4.z, r4.w}};
+        const float ndn = fmaf(n[2], g.dz, fmaf(n[1], g.dy, n[0] * g.dx));
+        acc[0] += nf_adj_tgt_algebra<float, T, HAS_M>(g.dx, g.dy, g.dz, g.rinv, g.rinv * 0.159154943091895336f, gc,
+                                                      gs, ndn, a, b, nxa, nxb, an, bn, n, J, M);
+    });
+    if (!ok || ti >= nt) return;
+    part[(long)blockIdx.y * nt + ti] = (double)hi[0] + (double)lo[0];
+}
+
+// ------------------------------------------------------- cotangent mapping
+
+// Cotangents of the mode's output rows -> (gE, gH) per target (near field)
+// or (gS_J, gS_M) (far field), as 12 double rows (re xyz, im xyz, ...).
+__global__ void po_adj_cot_kernel(int mode, long nt, const double *__restrict__ cot, const double *__restrict__ tgt7,
+                                  double t, double *__restrict__ gam)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    double ge[6] = {0, 0, 0, 0, 0, 0}, gh[6] = {0, 0, 0, 0, 0, 0};
+    auto row = [&](int r) { return cot[(long)r * nt + i]; };
+    if (mode == kEH || mode == kFF) {
+        for (int c = 0; c < 6; ++c) {
+            ge[c] = row(c);
+            gh[c] = row(6 + c);
+        }
+    }
+    if (mode == kJMEH) {
+        for (int c = 0; c < 6; ++c) {
+            ge[c] = row(12 + c);
+            gh[c] = row(18 + c);
+        }
+    }
+    if (mode == kJM || mode == kJMEH) {
+        // J = 2 n x H  ->  gH += 2 gJ x n
+        const double n[3] = {tgt7[3 * nt + i], tgt7[4 * nt + i], tgt7[5 * nt + i]};
+        for (int part_ = 0; part_ < 2; ++part_) {
+            const double g[3] = {row(3 * part_ + 0), row(3 * part_ + 1), row(3 * part_ + 2)};
+            gh[3 * part_ + 0] += 2.0 * (g[1] * n[2] - g[2] * n[1]);
+            gh[3 * part_ + 1] += 2.0 * (g[2] * n[0] - g[0] * n[2]);
+            gh[3 * part_ + 2] += 2.0 * (g[0] * n[1] - g[1] * n[0]);
+        }
+    }
+    if (mode == kFF) {
+        // gS_J = P gE + t r x gH ; gS_M = P gH - t r x gE
+        const double th = tgt7[i], ph = tgt7[nt + i];
+        const double r[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
+        double sj[6], sm[6];
+        for (int part_ = 0; part_ < 2; ++part_) {
+            const double *e = ge + 3 * part_, *h = gh + 3 * part_;
+            const double ed = e[0] * r[0] + e[1] * r[1] + e[2] * r[2];
+            const double hd = h[0] * r[0] + h[1] * r[1] + h[2] * r[2];
+            const double rxh[3] = {r[1] * h[2] - r[2] * h[1], r[2] * h[0] - r[0] * h[2], r[0] * h[1] - r[1] * h[0]};
+            const double rxe[3] = {r[1] * e[2] - r[2] * e[1], r[2] * e[0] - r[0] * e[2], r[0] * e[1] - r[1] * e[0]};
+            for (int c = 0; c < 3; ++c) {
+                sj[3 * part_ + c] = e[c] - ed * r[c] + t * rxh[c];
+                sm[3 * part_ + c] = h[c] - hd * r[c] - t * rxe[c];
+            }
+        }
+        for (int c = 0; c < 6; ++c) {
+            ge[c] = sj[c];
+            gh[c] = sm[c];
+        }
+    }
+    for (int c = 0; c < 6; ++c) {
+        gam[(long)c * nt + i] = ge[c];
+        gam[(long)(6 + c) * nt + i] = gh[c];
+    }
+}
+
+// Streamed cotangent records of the mixed source-side kernel (layout above).
+__global__ void po_adj_pack_tgt_kernel(long nt, const double *__restrict__ tgt7, const double *__restrict__ gam,
+                                       const Frame *__restrict__ frp, int far, float4 *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    float h[3], l[3], rf[3] = {0.f, 0.f, 0.f};
+    if (far) {
+        const double th = tgt7[i], ph = tgt7[nt + i];
+        const double r[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
+        for (int c = 0; c < 3; ++c) {
+            const double hd = rint(r[c] * 2048.0) / 2048.0;
+            h[c] = (float)hd;
+            l[c] = (float)(r[c] - hd);
+            rf[c] = h[c] + l[c];
+        }
+    } else {
+        const Frame fr = *frp;
+        for (int c = 0; c < 3; ++c) {
+            const double x = (tgt7[c * nt + i] - fr.o[c]) * fr.kappa;
+            const double hd = rint(x * fr.inv_q) * fr.q;
+            h[c] = (float)hd;
+            l[c] = (float)(x - hd);
+        }
+    }
+    float g[12];
+    for (int c = 0; c < 3; ++c) {
+        g[2 * c] = (float)gam[c * nt + i];
+        g[2 * c + 1] = (float)gam[(3 + c) * nt + i];
+        g[6 + 2 * c] = (float)gam[(6 + c) * nt + i];
+        g[7 + 2 * c] = (float)gam[(9 + c) * nt + i];
+    }
+    float4 *o = out + (size_t)kRec * i;
+    if (far) {
+        o[0] = make_float4(h[0], h[1], h[2], l[0]);
+        o[1] = make_float4(l[1], l[2], 0.f, 0.f);
+    } else {
+        o[0] = make_float4(h[0], h[1], h[2], 0.f);
+        o[1] = make_float4(l[0], l[1], l[2], 0.f);
+    }
+    o[2] = make_float4(g[0], g[1], g[2], g[3]);
+    o[3] = make_float4(g[4], g[5], g[6], g[7]);
+    o[4] = make_float4(g[8], g[9], g[10], g[11]);
+    o[5] = make_float4(rf[0], rf[1], rf[2], 0.f);
+}
+
+// ------------------------------------------------------------- FP64 kernels
+
+// The forward FP64 kernel's illumination test: the reference's operation
+// order and rounding (R_hat = d * (1/R), n . R_hat left to right, no FMA).
+__device__ __forceinline__ bool lit_fp64(const double *n, double dx, double dy, double dz, double rinv)
+{
+    const double ndr = __dadd_rn(__dadd_rn(__dmul_rn(n[0], __dmul_rn(dx, rinv)), __dmul_rn(n[1], __dmul_rn(dy, rinv))),
+                                 __dmul_rn(n[2], __dmul_rn(dz, rinv)));
+    return !(ndr < 0.0);
+}
+
+// Plain FP64 source-side adjoint: thread = source, loop over every target.
+template <int KIND, int T>
+__global__ void __launch_bounds__(kThreadsD)
+po_adj_src_fp64_kernel(const double *__restrict__ srcd, long ns, const double *__restrict__ tgt7,
+                       const double *__restrict__ gam, long nt, double k, double *__restrict__ part)
+{
+    __shared__ double tile[kTileD * 15];
+    const long si = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const double *q = srcd + (size_t)kRecD * (si < ns ? si : 0);
+    const double sp[3] = {q[0], q[1], q[2]};
+    SrcConst<double> sc;
+    for (int c = 0; c < 3; ++c) {
+        sc.n[c] = q[3 + c];
+        sc.J[c] = {q[6 + 2 * c], q[7 + 2 * c]};
+        sc.M[c] = {q[12 + 2 * c], q[13 + 2 * c]};
+    }
+    src_const_finish<double, true>(sc);
+    double acc[kAccAdj];
+    for (int a = 0; a < kAccAdj; ++a) acc[a] = 0.0;
+    for (long base = 0; base < nt; base += kTileD) {
+        const int cnt = (int)min((long)kTileD, nt - base);
+        __syncthreads();
+        for (int w = threadIdx.x; w < cnt * 15; w += blockDim.x) {
+            const int s = w / 15, c = w % 15;
+            const long ti = base + s;
+            double v;
+            if (c < 3) {
+                if (KIND == kKindFF) {
+                    const double th = tgt7[ti], ph = tgt7[nt + ti];
+                    v = c == 0 ? cos(ph) * sin(th) : (c == 1 ? sin(ph) * sin(th) : cos(th));
+                } else {
+                    v = tgt7[c * nt + ti];
+                }
+            } else {
+                v = gam[(long)(c - 3) * nt + ti];
+            }
+            tile[s * 15 + c] = v;
+        }
+        __syncthreads();
+        if (si >= ns) continue;
+        for (int s = 0; s < cnt; ++s) {
+            const double *r = tile + s * 15;
+            const cx<double> gE[3] = {{r[3], r[6]}, {r[4], r[7]}, {r[5], r[8]}};
+            const cx<double> gH[3] = {{r[9], r[12]}, {r[10], r[13]}, {r[11], r[14]}};
+            if (KIND == kKindNF) {
+                const double dx = r[0] - sp[0], dy = r[1] - sp[1], dz = r[2] - sp[2];
+                const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                      __dmul_rn(dz, dz)));
+                const double rinv = __ddiv_rn(1.0, R);
+                if (lit_fp64(sc.n, dx, dy, dz, rinv) == false) continue;
+                const double ndd = sc.n[0] * dx + sc.n[1] * dy + sc.n[2] * dz;
+                double sn, cs;
+                sincos(k * R, &sn, &cs);
+                nf_adj_src_algebra<double, T, true, true>(acc, dx, dy, dz, rinv, rinv / k, cs, T * sn, ndd, gE, gH,
+                                                          sc);
+            } else {
+                const double ndr = sc.n[0] * r[0] + sc.n[1] * r[1] + sc.n[2] * r[2];
+                if (__dadd_rn(__dadd_rn(__dmul_rn(sc.n[0], r[0]), __dmul_rn(sc.n[1], r[1])),
+                              __dmul_rn(sc.n[2], r[2])) < 0.0)
+                    continue;
+                double sn, cs;
+                sincos(k * (sp[0] * r[0] + sp[1] * r[1] + sp[2] * r[2]), &sn, &cs);
+                const cx<double> G = {cs, -T * sn};
+                const cx<double> Gc = cconj(G);
+                for (int c = 0; c < 3; ++c) {
+                    const cx<double> jb = cmul(Gc, gE[c]), mb = cmul(Gc, gH[c]);
+                    acc[c] += jb.r;
+                    acc[3 + c] += jb.i;
+                    acc[6 + c] += mb.r;
+                    acc[9 + c] += mb.i;
+                }
+                cx<double> gEc[3] = {cconj(gE[0]), cconj(gE[1]), cconj(gE[2])};
+                cx<double> gHc[3] = {cconj(gH[0]), cconj(gH[1]), cconj(gH[2])};
+                const cx<double> Z = cmul(G, cadd(cdot_c(gEc, sc.J), cdot_c(gHc, sc.M)));
+                acc[12] += T * k * Z.i * ndr;
+            }
+        }
+    }
+    if (si < ns)
+        for (int a = 0; a < kAccAdj; ++a) part[(long)a * ns + si] = acc[a];
+}
+
+// Plain FP64 target-side displacement adjoint (near field).
+template <int T>
+__global__ void __launch_bounds__(kThreadsD)
+po_adj_tgt_fp64_kernel(const double *__restrict__ srcd, long ns, const double *__restrict__ tgt7,
+                       const double *__restrict__ gam, long nt, double k, double *__restrict__ part)
+{
+    __shared__ double tile[kTileD * kRecD];
+    const long ti = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double p[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+    cx<double> a[3] = {{0, 0}, {0, 0}, {0, 0}}, b[3] = {{0, 0}, {0, 0}, {0, 0}};
+    if (ti < nt)
+        for (int c = 0; c < 3; ++c) {
+            p[c] = tgt7[c * nt + ti];
+            n[c] = tgt7[(3 + c) * nt + ti];
+            a[c] = {gam[c * nt + ti], -gam[(3 + c) * nt + ti]};
+            b[c] = {gam[(6 + c) * nt + ti], -gam[(9 + c) * nt + ti]};
+        }
+    cx<double> nxa[3], nxb[3], t3[3];
+    ccross_r(a, n[0], n[1], n[2], t3);
+    for (int c = 0; c < 3; ++c) nxa[c] = {-t3[c].r, -t3[c].i};
+    ccross_r(b, n[0], n[1], n[2], t3);
+    for (int c = 0; c < 3; ++c) nxb[c] = {-t3[c].r, -t3[c].i};
+    const cx<double> an = cdot_r(a, n[0], n[1], n[2]), bn = cdot_r(b, n[0], n[1], n[2]);
+    double acc = 0.0;
+    for (long base = 0; base < ns; base += kTileD) {
+        const int cnt = (int)min((long)kTileD, ns - base);
+        __syncthreads();
+        for (int w = threadIdx.x; w < cnt * kRecD; w += blockDim.x) tile[w] = srcd[base * kRecD + w];
+        __syncthreads();
+        if (ti >= nt) continue;
+        for (int s = 0; s < cnt; ++s) {
+            const double *r = tile + s * kRecD;
+            const double dx = p[0] - r[0], dy = p[1] - r[1], dz = p[2] - r[2];
+            const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                  __dmul_rn(dz, dz)));
+            const double rinv = __ddiv_rn(1.0, R);
+            if (lit_fp64(r + 3, dx, dy, dz, rinv) == false) continue;
+            double sn, cs;
+            sincos(k * R, &sn, &cs);
+            const cx<double> J[3] = {{r[6], r[7]}, {r[8], r[9]}, {r[10], r[11]}};
+            const cx<double> M[3] = {{r[12], r[13]}, {r[14], r[15]}, {r[16], r[17]}};
+            const double ndn = n[0] * dx + n[1] * dy + n[2] * dz;
+            acc += nf_adj_tgt_algebra<double, T, true>(dx, dy, dz, rinv, rinv / k, cs, T * sn, ndn, a, b, nxa, nxb,
+                                                       an, bn, n, J, M);
+        }
+    }
+    if (ti < nt) part[ti] = acc;
+}
+
+// ---------------------------------------------------------------- epilogues
+
+// Sums the chunks of the source-side partials; unfolds the currents by
+// conj(fac * weight * area); scales the displacement term to mm.
+__global__ void po_adj_src_epilogue_kernel(int kind, int nsplit, long ns, const double *__restrict__ part,
+                                           const double *__restrict__ src7, int gmode, int ncx, int ncy,
+                                           double fac_re, double fac_im, double dscale,
+                                           double *__restrict__ grad_cur, double *__restrict__ grad_ds)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns) return;
+    double a[kAccAdj];
+    for (int q = 0; q < kAccAdj; ++q) a[q] = 0.0;
+    for (int s = 0; s < nsplit; ++s)
+        for (int q = 0; q < kAccAdj; ++q) a[q] += part[((long)s * kAccAdj + q) * ns + i];
+    double w = src7[6 * ns + i];
+    if (gmode >= 0) {
+        const long xu = i / ncy, yv = i - xu * ncy;
+        if (xu == 0 || xu == ncx - 1) w *= 0.5;
+        if (gmode != 1 && (yv == 0 || yv == ncy - 1)) w *= 0.5;
+    }
+    const double fr = fac_re * w, fi = fac_im * w;
+    if (grad_cur)
+        for (int g = 0; g < 2; ++g)
+            for (int c = 0; c < 3; ++c) {
+                const double re = a[6 * g + c], im = a[6 * g + 3 + c];
+                // conj(f) * (re + j im)
+                grad_cur[(long)(6 * g + c) * ns + i] = fr * re + fi * im;
+                grad_cur[(long)(6 * g + 3 + c) * ns + i] = fr * im - fi * re;
+            }
+    (void)kind;
+    if (grad_ds) grad_ds[i] = dscale * a[12];
+}
+
+__global__ void po_adj_tgt_epilogue_kernel(int nsplit, long nt, const double *__restrict__ part, double dscale,
+                                           double *__restrict__ grad_dt)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    double s = 0.0;
+    for (int c = 0; c < nsplit; ++c) s += part[(long)c * nt + i];
+    grad_dt[i] = dscale * s;
+}
+
+// ----------------------------------------------------------- instantiations
+
+template <int KIND, int T, bool HAS_M, bool WANT_D>
+static void *adj_src_ptr()
+{
+    return reinterpret_cast<void *>(&po_adj_src_kernel<KIND, T, HAS_M, WANT_D>);
+}
+
+void *adj_src_kernel(int kind, int t_sign, bool has_m, bool want_d)
+{
+#define PO_ADJ_SEL(K)                                                                                       \
+    if (t_sign < 0) {                                                                                       \
+        if (has_m) return want_d ? adj_src_ptr<K, -1, true, true>() : adj_src_ptr<K, -1, true, false>();    \
+        return want_d ? adj_src_ptr<K, -1, false, true>() : adj_src_ptr<K, -1, false, false>();             \
+    }                                                                                                       \
+    if (has_m) return want_d ? adj_src_ptr<K, 1, true, true>() : adj_src_ptr<K, 1, true, false>();          \
+    return want_d ? adj_src_ptr<K, 1, false, true>() : adj_src_ptr<K, 1, false, false>();
+    if (kind == kKindNF) {
+        PO_ADJ_SEL(kKindNF)
+    }
+    PO_ADJ_SEL(kKindFF)
+#undef PO_ADJ_SEL
+}
+
+void *adj_tgt_kernel(int t_sign, bool has_m)
+{
+    if (t_sign < 0)
+        return has_m ? reinterpret_cast<void *>(&po_adj_tgt_kernel<-1, true>)
+                     : reinterpret_cast<void *>(&po_adj_tgt_kernel<-1, false>);
+    return has_m ? reinterpret_cast<void *>(&po_adj_tgt_kernel<1, true>)
+                 : reinterpret_cast<void *>(&po_adj_tgt_kernel<1, false>);
+}
+
+void *adj_src_fp64_kernel(int kind, int t_sign)
+{
+    if (kind == kKindNF)
+        return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindNF, -1>)
+                          : reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindNF, 1>);
+    return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindFF, -1>)
+                      : reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindFF, 1>);
+}
+
+void *adj_tgt_fp64_kernel(int t_sign)
+{
+    return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<-1>)
+                      : reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<1>);
+}
+
+void *adj_cot_kernel() { return reinterpret_cast<void *>(&po_adj_cot_kernel); }
+void *adj_pack_tgt_kernel() { return reinterpret_cast<void *>(&po_adj_pack_tgt_kernel); }
+void *adj_src_epilogue_kernel() { return reinterpret_cast<void *>(&po_adj_src_epilogue_kernel); }
+void *adj_tgt_epilogue_kernel() { return reinterpret_cast<void *>(&po_adj_tgt_epilogue_kernel); }
+
+}  // namespace po

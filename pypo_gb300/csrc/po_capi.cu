@@ -254,6 +254,82 @@ int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int nc
     return po::run_device(a);
 }
 
+int po_adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
+                   const double *tgt7, double k, double epsilon, double t_direction, int precision, int flags,
+                   const double *cot, double *grad_cur, double *grad_ds, double *grad_dt, void *stream)
+{
+    po::clear_error();
+    po::AdjArgs a;
+    a.mode = mode;
+    a.ns = ns;
+    a.src7 = src7;
+    a.gmode = gmode;
+    a.ncx = ncx;
+    a.ncy = ncy;
+    a.cur = cur;
+    a.nt = nt;
+    a.tgt7 = tgt7;
+    a.k = k;
+    a.epsilon = epsilon;
+    a.t_dir = t_direction;
+    a.precision = precision;
+    a.m_zero = (flags & 1) != 0;
+    a.out = grad_cur ? grad_cur : (grad_ds ? grad_ds : grad_dt);   // validate() wants an output
+    a.cot = cot;
+    a.grad_cur = grad_cur;
+    a.grad_ds = grad_ds;
+    a.grad_dt = grad_dt;
+    a.stream = static_cast<cudaStream_t>(stream);
+    if (!grad_cur && !grad_ds && !grad_dt) return fail(1, "no gradient requested");
+    return po::run_adjoint(a);
+}
+
+int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
+                 const double *tgt7, double k, double epsilon, double t_direction, int precision, const double *cot,
+                 double *grad_cur, double *grad_ds, double *grad_dt)
+{
+    po::clear_error();
+    if (mode < 0 || mode > 5) return fail(1, "mode must be 0..5");
+    if (ns < 0 || nt < 0) return fail(1, "negative size");
+    const int nout = po::n_out(mode);
+    cudaStream_t s = nullptr;
+    if (int rc = lib_stream(&s)) return rc;
+    double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_cot = nullptr;
+    double *d_gc = nullptr, *d_gs = nullptr, *d_gt = nullptr;
+    int rc = 0, code = 0;
+    const size_t ns1 = std::max(ns, 1L), nt1 = std::max(nt, 1L);
+    CK(cudaMallocAsync(&d_src, sizeof(double) * 7 * ns1, s));
+    CK(cudaMallocAsync(&d_cur, sizeof(double) * 12 * ns1, s));
+    CK(cudaMallocAsync(&d_tgt, sizeof(double) * 7 * nt1, s));
+    CK(cudaMallocAsync(&d_cot, sizeof(double) * nout * nt1, s));
+    if (grad_cur) CK(cudaMallocAsync(&d_gc, sizeof(double) * 12 * ns1, s));
+    if (grad_ds) CK(cudaMallocAsync(&d_gs, sizeof(double) * ns1, s));
+    if (grad_dt) CK(cudaMallocAsync(&d_gt, sizeof(double) * nt1, s));
+    if (ns > 0) {
+        CK(cudaMemcpyAsync(d_src, src7, sizeof(double) * 7 * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_cur, cur, sizeof(double) * 12 * ns, cudaMemcpyHostToDevice, s));
+    }
+    if (nt > 0) {
+        CK(cudaMemcpyAsync(d_tgt, tgt7, sizeof(double) * 7 * nt, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_cot, cot, sizeof(double) * nout * nt, cudaMemcpyHostToDevice, s));
+    }
+    rc = po_adjoint_dev(mode, ns, d_src, gmode, ncx, ncy, d_cur, nt, d_tgt, k, epsilon, t_direction, precision,
+                        (ns > 0 && m_is_zero(cur, ns)) ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s);
+    if (rc) goto done;
+    if (grad_cur && ns > 0) CK(cudaMemcpyAsync(grad_cur, d_gc, sizeof(double) * 12 * ns, cudaMemcpyDeviceToHost, s));
+    if (grad_ds && ns > 0) CK(cudaMemcpyAsync(grad_ds, d_gs, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+    if (grad_dt && nt > 0) CK(cudaMemcpyAsync(grad_dt, d_gt, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    rc = po::read_device_error(s, &code);
+    if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
+                                      std::to_string(code) + "); results are invalid");
+done:
+    for (double *p : {d_src, d_cur, d_tgt, d_cot, d_gc, d_gs, d_gt})
+        if (p) cudaFreeAsync(p, s);
+    if (s) cudaStreamSynchronize(s);
+    return rc;
+}
+
 int po_timing_enable(int slots)
 {
     po::clear_error();

@@ -343,4 +343,164 @@ int run_device(const RunArgs &a)
     return rc;
 }
 
+
+// ---------------------------------------------------------------- adjoint
+
+int run_adjoint(const AdjArgs &a)
+{
+    if (int rc = validate(a)) return rc;
+    if (a.mode == kEHP || a.mode == kScalar)
+        return fail(1, "the adjoint covers modes JM, EH, JMEH and FF (EHP is nonlinear, scalar not built)");
+    if (a.mode == kFF && a.grad_dt) return fail(1, "far-field targets are directions: no target displacement");
+    if (a.nt > 0 && !a.cot) return fail(1, "null cotangent buffer");
+    if (a.ns == 0) return 0;
+    if (a.nt == 0) {
+        // no targets: every gradient is zero
+        if (a.grad_cur) PO_CK(cudaMemsetAsync(a.grad_cur, 0, sizeof(double) * 12 * a.ns, a.stream));
+        if (a.grad_ds) PO_CK(cudaMemsetAsync(a.grad_ds, 0, sizeof(double) * a.ns, a.stream));
+        return 0;
+    }
+    DeviceInfo *di = nullptr;
+    if (int rc = device_info(di)) return rc;
+    int *err = error_word();
+    if (!err) return fail(2, "could not allocate the device error word");
+
+    const int kind = a.mode == kFF ? kKindFF : kKindNF;
+    const double pif = (double)3.14159265359f;
+    const double pref = a.k * a.k / (4.0 * pif);
+    const double kappa = a.k / (2.0 * 3.14159265358979323846);
+    double fac_re = pref, fac_im = 0.0;
+    if (kind == kKindFF) { fac_re = 0.0; fac_im = -pref; }
+    const int ts = a.t_dir > 0 ? 1 : -1;
+    const bool far = kind == kKindFF;
+    const bool has_m = !a.m_zero;
+    const bool want_d = a.grad_ds != nullptr;
+    cudaStream_t s = a.stream;
+    long ns = a.ns, nt = a.nt;
+    int mode = a.mode, gmode = a.gmode, ncx = a.ncx, ncy = a.ncy;
+    double t = a.t_dir, k = a.k;
+    const double *src7 = a.src7, *cur = a.cur, *tgt7 = a.tgt7, *cot = a.cot;
+    double *grad_cur = a.grad_cur, *grad_ds = a.grad_ds, *grad_dt = a.grad_dt;
+    const unsigned nblk_s = (unsigned)((ns + 255) / 256), nblk_t = (unsigned)((nt + 255) / 256);
+    std::vector<void *> owned;
+    int rc = 0;
+    double *gam = nullptr;
+    if ((rc = salloc(&gam, (size_t)12 * nt, s, owned))) { sfree(owned, s); return rc; }
+    void *cargs[] = {&mode, &nt, &cot, &tgt7, &t, &gam};
+    rc = launch(adj_cot_kernel(), dim3(nblk_t), dim3(256), cargs, 0, s);
+    const int zero_scalar = 0;
+
+    if (a.precision == 1) {
+        double *srcd = nullptr, *part = nullptr, *partt = nullptr;
+        if (!rc && ((rc = salloc(&srcd, (size_t)ns * kRecD, s, owned)) ||
+                    (rc = salloc(&part, (size_t)kAccAdj * ns, s, owned)) ||
+                    (rc = salloc(&partt, (size_t)std::max(nt, 1L), s, owned)))) {
+            sfree(owned, s);
+            return rc;
+        }
+        void *pargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &fac_re, &fac_im, (void *)&zero_scalar, &srcd};
+        if (!rc) rc = launch(pack_src_d_kernel(), dim3(nblk_s), dim3(256), pargs, 0, s);
+        void *sargs[] = {&srcd, &ns, &tgt7, &gam, &nt, &k, &part};
+        timing_mark(s, true);
+        if (!rc) rc = launch(adj_src_fp64_kernel(kind, ts), dim3((unsigned)((ns + kThreadsD - 1) / kThreadsD)),
+                             dim3(kThreadsD), sargs, 0, s);
+        timing_mark(s, false);
+        int one = 1;
+        double dsc = far ? 1.0 : -1.0;
+        void *eargs[] = {(void *)&kind, &one, &ns, &part, &src7, &gmode, &ncx, &ncy, &fac_re, &fac_im, &dsc,
+                         &grad_cur, &grad_ds};
+        if (!rc) rc = launch(adj_src_epilogue_kernel(), dim3(nblk_s), dim3(256), eargs, 0, s);
+        if (!rc && grad_dt) {
+            void *targs[] = {&srcd, &ns, &tgt7, &gam, &nt, &k, &partt};
+            rc = launch(adj_tgt_fp64_kernel(ts), dim3((unsigned)((nt + kThreadsD - 1) / kThreadsD)), dim3(kThreadsD),
+                        targs, 0, s);
+            double one_d = 1.0;
+            void *teargs[] = {&one, &nt, &partt, &one_d, &grad_dt};
+            if (!rc) rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
+        }
+        sfree(owned, s);
+        return rc;
+    }
+
+    // ---- mixed precision
+    double *bbox = nullptr;
+    Frame *frame = nullptr;
+    float4 *srcpk = nullptr, *trec = nullptr;
+    if (!rc && ((rc = salloc(&bbox, (size_t)kBboxBlocks * 6, s, owned)) || (rc = salloc(&frame, 1, s, owned)) ||
+                (rc = salloc(&srcpk, (size_t)ns * kRec, s, owned)) ||
+                (rc = salloc(&trec, (size_t)nt * kRec, s, owned)))) {
+        sfree(owned, s);
+        return rc;
+    }
+    long nb = far ? 0 : nt;
+    void *bargs[] = {&src7, &ns, &tgt7, &nb, &bbox};
+    if (!rc) rc = launch(bbox_kernel(), dim3(kBboxBlocks), dim3(kBboxThreads), bargs, 0, s);
+    int nbb = kBboxBlocks;
+    double kap = kappa;
+    int centred = far ? 0 : 1;
+    void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
+    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
+    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&zero_scalar, &srcpk};
+    if (!rc) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
+    int farflag = far ? 1 : 0;
+    void *paargs[] = {&nt, &tgt7, &gam, &frame, &farflag, &trec};
+    if (!rc) rc = launch(adj_pack_tgt_kernel(), dim3(nblk_t), dim3(256), paargs, 0, s);
+
+    // source side: sources in registers, targets streamed
+    void *fsrc = adj_src_kernel(kind, ts, has_m, want_d);
+    const int smem = kStages * kTile * kRec * 16;
+    int occ = 1;
+    if (!rc) {
+        PO_CK(cudaFuncSetAttribute(fsrc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fsrc, kThreadsA, smem));
+        occ = std::max(occ, 1);
+    }
+    const long nsb = (ns + kThreadsA - 1) / kThreadsA;
+    const long splitA = choose_split(nsb, nt, (long)di->sms * occ, ns, kAccAdj);
+    const long tilesA = std::max(1L, (nt + kTile - 1) / kTile);
+    long chunkA = ((tilesA + splitA - 1) / splitA) * kTile;
+    double *part = nullptr;
+    if (!rc && (rc = salloc(&part, (size_t)splitA * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
+    const float4 *srcc = srcpk, *trc = trec;
+    void *aargs[] = {&srcc, &ns, &trc, &nt, &chunkA, &part, &err};
+    timing_mark(s, true);
+    if (!rc) rc = launch(fsrc, dim3((unsigned)nsb, (unsigned)splitA), dim3(kThreadsA), aargs, smem, s);
+    timing_mark(s, false);
+    int nspl = (int)splitA;
+    double dsc = far ? kappa : -kappa;
+    void *eargs[] = {(void *)&kind, &nspl, &ns, &part, &src7, &gmode, &ncx, &ncy, &fac_re, &fac_im, &dsc, &grad_cur,
+                     &grad_ds};
+    if (!rc) rc = launch(adj_src_epilogue_kernel(), dim3(nblk_s), dim3(256), eargs, 0, s);
+
+    // target side (near field): targets in registers, sources streamed
+    if (!rc && grad_dt) {
+        float4 *tgtpk = nullptr;
+        if ((rc = salloc(&tgtpk, (size_t)nt * 2, s, owned))) { sfree(owned, s); return rc; }
+        int zero_far = 0;
+        void *ptargs[] = {&nt, &tgt7, &frame, &zero_far, &tgtpk};
+        rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
+        void *ftgt = adj_tgt_kernel(ts, has_m);
+        if (!rc) {
+            PO_CK(cudaFuncSetAttribute(ftgt, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ftgt, kThreadsA, smem));
+            occ = std::max(occ, 1);
+        }
+        const long ntb = (nt + kThreadsA - 1) / kThreadsA;
+        const long splitB = choose_split(ntb, ns, (long)di->sms * occ, nt, 1);
+        const long tilesB = std::max(1L, (ns + kTile - 1) / kTile);
+        long chunkB = ((tilesB + splitB - 1) / splitB) * kTile;
+        double *partt = nullptr;
+        if (!rc && (rc = salloc(&partt, (size_t)splitB * nt, s, owned))) { sfree(owned, s); return rc; }
+        const float4 *tgc = tgtpk;
+        void *targs[] = {&srcc, &ns, &chunkB, &tgc, &gam, &tgt7, &nt, &partt, &err};
+        if (!rc) rc = launch(ftgt, dim3((unsigned)ntb, (unsigned)splitB), dim3(kThreadsA), targs, smem, s);
+        int nsplB = (int)splitB;
+        double dsct = kappa;
+        void *teargs[] = {&nsplB, &nt, &partt, &dsct, &grad_dt};
+        if (!rc) rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
+    }
+    sfree(owned, s);
+    return rc;
+}
+
 }  // namespace po

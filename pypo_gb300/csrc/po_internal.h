@@ -25,7 +25,17 @@ struct RunArgs {
     cudaStream_t stream = nullptr;
 };
 
+// Adjoint of one propagation: cotangents of the outputs in, gradients with
+// respect to the source currents and the normal displacements out.
+struct AdjArgs : RunArgs {
+    const double *cot = nullptr;   // n_out(mode) rows x nt
+    double *grad_cur = nullptr;    // 12 rows x ns, or null
+    double *grad_ds = nullptr;     // ns, or null
+    double *grad_dt = nullptr;     // nt, or null (near field only)
+};
+
 int n_out(int mode);
+int run_adjoint(const AdjArgs &a);
 int validate(const RunArgs &a);   // argument checks only, no CUDA calls
 int run_device(const RunArgs &a);
 

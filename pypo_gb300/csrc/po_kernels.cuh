@@ -23,6 +23,11 @@ constexpr int kRecScalar = 2;   // float4 per packed scalar record (32 B)
 constexpr int kAcc = 12;        // accumulators per target (E, H re/im x y z)
 constexpr uint32_t kWaitLimit = 1u << 24;   // bounded mbarrier polls
 
+// Adjoint kernels: one source (or target) per thread; 12 current
+// accumulators + 1 displacement accumulator.
+constexpr int kThreadsA = 128;
+constexpr int kAccAdj = 13;
+
 // FP64 comparison kernel.
 constexpr int kThreadsD = 128;
 constexpr int kTileD = 64;
@@ -63,5 +68,13 @@ void *pack_tgt_kernel();
 void *pack_src_d_kernel();
 void *epilogue_kernel();
 void *fp32_probe_kernel();
+void *adj_src_kernel(int kind, int t_sign, bool has_m, bool want_d);
+void *adj_tgt_kernel(int t_sign, bool has_m);
+void *adj_src_fp64_kernel(int kind, int t_sign);
+void *adj_tgt_fp64_kernel(int t_sign);
+void *adj_cot_kernel();
+void *adj_pack_tgt_kernel();
+void *adj_src_epilogue_kernel();
+void *adj_tgt_epilogue_kernel();
 
 }  // namespace po

@@ -118,3 +118,55 @@ def timing_collect(max_n=4096):
     if n < 0:
         raise POError("po_timing_collect failed")
     return [buf[i] for i in range(n)]
+
+
+def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-1.0, precision="mixed",
+            want=("cur", "ds", "dt")):
+    """Host-buffer adjoint (po_adjoint_d).
+
+    cot: (n_out(mode), nt) float64, dL/d(output rows). Returns a dict with the
+    requested gradients: "cur" (12, ns), "ds" (ns,) and "dt" (nt,) (near field).
+    """
+    lib = load()
+    src7 = np.ascontiguousarray(src7, dtype=np.float64)
+    tgt7 = np.ascontiguousarray(tgt7, dtype=np.float64)
+    cur = np.ascontiguousarray(cur, dtype=np.float64)
+    cot = np.ascontiguousarray(cot, dtype=np.float64)
+    _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy)
+    ns, nt = src7.shape[1], tgt7.shape[1]
+    if cot.shape != (n_out(mode), nt):
+        raise POError(f"cot must have shape {(n_out(mode), nt)}")
+    out = {}
+    gc = np.zeros((12, ns)) if "cur" in want else None
+    gs = np.zeros(ns) if "ds" in want else None
+    gt = np.zeros(nt) if ("dt" in want and mode != "FF") else None
+    ptr = lambda a: a.ctypes.data if a is not None else None
+    check(lib.po_adjoint_d(MODE_ID[mode], ns, src7.ctypes.data, int(gmode), int(ncx), int(ncy), cur.ctypes.data,
+                           nt, tgt7.ctypes.data, float(k), float(epsilon), float(t_dir), PRECISION[precision],
+                           cot.ctypes.data, ptr(gc), ptr(gs), ptr(gt)))
+    if gc is not None:
+        out["cur"] = gc
+    if gs is not None:
+        out["ds"] = gs
+    if gt is not None:
+        out["dt"] = gt
+    return out
+
+
+def adjoint_dev(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-1.0, precision="mixed",
+                m_zero=False, grad_cur=None, grad_ds=None, grad_dt=None, stream=None):
+    """Device-buffer adjoint (po_adjoint_dev) on torch float64 CUDA tensors; queued on `stream`."""
+    import torch
+    lib = load()
+    for name, t in (("src7", src7), ("cur", cur), ("tgt7", tgt7), ("cot", cot)):
+        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+            raise POError(f"{name} must be a contiguous float64 CUDA tensor")
+    _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy)
+    if stream is None:
+        stream = torch.cuda.current_stream(tgt7.device)
+    ptr = lambda t: t.data_ptr() if t is not None else None
+    check(lib.po_adjoint_dev(MODE_ID[mode], src7.shape[1], src7.data_ptr(), int(gmode), int(ncx), int(ncy),
+                             cur.data_ptr(), tgt7.shape[1], tgt7.data_ptr(), float(k), float(epsilon), float(t_dir),
+                             PRECISION[precision], 1 if m_zero else 0, cot.data_ptr(), ptr(grad_cur), ptr(grad_ds),
+                             ptr(grad_dt), ctypes.c_void_p(stream.cuda_stream)))
+    return grad_cur, grad_ds, grad_dt

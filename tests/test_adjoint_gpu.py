@@ -1,0 +1,156 @@
+"""GPU adjoint: gradients of a real loss of the outputs with respect to the
+source currents and to normal-direction displacements of source and target
+points, checked against central finite differences of the FP64 oracle
+(forward restatement of the reference) and against the plain FP64 GPU
+adjoint. The bar: 1e-4 relative to the finite differences (mixed), 1e-6
+(FP64)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(rng, mode):
+    from pypo_gb300 import engine, surfaces as SF
+    src = SF.paraboloid(3.0, [9, 10], gmode=1, lims_a=[0.2, 2.0])
+    s7 = engine.generate_grid(src)
+    if mode == "FF":
+        t7 = engine.generate_grid(SF.farfield([6, 5], [-20, 20], [-15, 15]))
+    else:
+        t7 = engine.generate_grid(SF.translate(SF.plane([6, 5], gmode=0, lims_a=[-1, 1]), dz=3.0))
+        t7[3:6] *= -1.0
+    cur = rng.standard_normal((12, s7.shape[1]))
+    cot = rng.standard_normal((engine.n_out(mode), t7.shape[1]))
+    return s7, cur, t7, cot, (1, 9, 10)
+
+
+def _loss(oracle_mod, mode, s7, cur, t7, cot, grid, k, t):
+    out = oracle_mod.run(mode, s7, cur, grid[0], grid[1], grid[2], t7, k, 1.0, t)
+    return float((cot * out).sum())
+
+
+def _fd(oracle_mod, mode, s7, cur, t7, cot, grid, k, t, rng, nsamp=6):
+    """Central FD of the oracle loss: current entries, source and target displacements."""
+    f = lambda s, c, tt: _loss(oracle_mod, mode, s, c, tt, cot, grid, k, t)
+    h_c, h_d = 1e-3, 1e-6 * (2 * np.pi / k)
+    rows = rng.integers(0, 12, nsamp)
+    cols = rng.integers(0, s7.shape[1], nsamp)
+    fc = []
+    for r, c in zip(rows, cols):
+        cp, cm = cur.copy(), cur.copy()
+        cp[r, c] += h_c
+        cm[r, c] -= h_c
+        fc.append((f(s7, cp, t7) - f(s7, cm, t7)) / (2 * h_c))
+    si = rng.choice(s7.shape[1], nsamp, replace=False)
+    fs = []
+    for i in si:
+        sp, sm = s7.copy(), s7.copy()
+        sp[:3, i] += h_d * s7[3:6, i]
+        sm[:3, i] -= h_d * s7[3:6, i]
+        fs.append((f(sp, cur, t7) - f(sm, cur, t7)) / (2 * h_d))
+    ti = rng.choice(t7.shape[1], nsamp, replace=False)
+    ft = []
+    if mode != "FF":
+        for j in ti:
+            tp, tm = t7.copy(), t7.copy()
+            tp[:3, j] += h_d * t7[3:6, j]
+            tm[:3, j] -= h_d * t7[3:6, j]
+            ft.append((f(s7, cur, tp) - f(s7, cur, tm)) / (2 * h_d))
+    return (rows, cols, np.array(fc)), (si, np.array(fs)), (ti, np.array(ft))
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("mode", ["EH", "JM", "JMEH", "FF"])
+@pytest.mark.parametrize("t", [-1.0, 1.0])
+def test_adjoint_matches_finite_differences(cuda, lib, oracle_mod, mode, t):
+    from pypo_gb300 import engine
+    rng = np.random.default_rng({"EH": 10, "JM": 20, "JMEH": 30, "FF": 40}[mode] + (t > 0))
+    s7, cur, t7, cot, grid = _case(rng, mode)
+    k = 2 * np.pi / 0.9
+    (rows, cols, fc), (si, fs), (ti, ft) = _fd(oracle_mod, mode, s7, cur, t7, cot, grid, k, t, rng)
+    for prec, tol in (("mixed", 1e-4), ("fp64", 1e-6)):
+        g = engine.adjoint(mode, s7, cur, *grid, t7, k, cot, 1.0, t, prec)
+        assert _rel(g["cur"][rows, cols], fc) <= tol, (prec, "cur", g["cur"][rows, cols], fc)
+        assert _rel(g["ds"][si], fs) <= tol, (prec, "ds", g["ds"][si], fs)
+        if mode != "FF":
+            assert _rel(g["dt"][ti], ft) <= tol, (prec, "dt", g["dt"][ti], ft)
+
+
+def test_mixed_adjoint_matches_fp64_adjoint_at_scale(cuda, lib):
+    """A reduced dish_eh (kR ~ 3e3 rad): the mixed adjoint against the FP64 one."""
+    from pypo_gb300 import configs, engine
+    w = configs.dish_eh(scale=0.12)
+    rng = np.random.default_rng(4)
+    cot = rng.standard_normal((12, w["t7"].shape[1]))
+    args = (w["mode"], w["s7"], w["cur"], w["gmode"], w["ncx"], w["ncy"], w["t7"], w["k"], cot)
+    gm = engine.adjoint(*args, precision="mixed")
+    gd = engine.adjoint(*args, precision="fp64")
+    assert _rel(gm["cur"], gd["cur"]) <= 1e-5
+    assert _rel(gm["ds"], gd["ds"]) <= 1e-4
+    assert _rel(gm["dt"], gd["dt"]) <= 1e-4
+
+
+def test_autograd_chain_feed_dish_farfield(cuda, lib, oracle_mod):
+    """feed plane --JM--> dish --FF--> far field; loss sum |E_ff - E_ideal|^2 with
+    E_ideal the unperturbed result. Gradients with respect to the feed currents
+    and the dish's normal displacement against FD of the oracle chain."""
+    import torch
+    from pypo_gb300 import autograd as A, beams, engine, surfaces as SF
+    lam = 2.0
+    k = 2 * np.pi / lam
+    feed = SF.plane([9, 9], gmode=0, lims_a=[-6, 6])
+    f7 = engine.generate_grid(feed)
+    _, fcur = beams.gauss_beam(f7, lam, 4.0, 0.0, 1.0)
+    # dish opening downwards with its focus on the feed: the reflected beam goes to -z
+    dish = SF.translate(SF.rotate_x(SF.paraboloid(40.0, [10, 12], gmode=1, lims_a=[0, 30]), 180.0), dz=40.0)
+    d7 = engine.generate_grid(dish)
+    aoe = engine.generate_grid(SF.farfield([5, 5], [-10, 10], [-10, 10]))
+    ff7 = aoe.copy()
+    ff7[0] = np.pi - aoe[0]          # polar angles around -z
+    dev = cuda
+    T = lambda a: torch.tensor(a, device=dev)
+    fcur_t = T(fcur).requires_grad_(True)
+    dd = torch.zeros(d7.shape[1], dtype=torch.float64, device=dev, requires_grad=True)
+    jm = A.propagate("JM", T(f7), fcur_t, 0, 9, 9, T(d7), k, dt=dd)
+    ff = A.propagate("FF", T(d7), jm, 1, 10, 12, T(ff7), k, ds=dd)
+    ideal = torch.tensor(oracle_mod.run("FF", d7, oracle_mod.run("JM", f7, fcur, 0, 9, 9, d7, k), 1, 10, 12, ff7, k),
+                         device=dev)
+    # perturb the dish a little so that the loss is not at its minimum
+    rng = np.random.default_rng(0)
+    pert = rng.normal(0, lam / 40, d7.shape[1])
+    with torch.no_grad():
+        dd.copy_(T(pert))
+    jm = A.propagate("JM", T(f7), fcur_t, 0, 9, 9, T(d7), k, dt=dd)
+    ff = A.propagate("FF", T(d7), jm, 1, 10, 12, T(ff7), k, ds=dd)
+    loss = ((ff - ideal) ** 2).sum()
+    loss.backward()
+    g_dd = dd.grad.cpu().numpy()
+    g_cur = fcur_t.grad.cpu().numpy()
+
+    def chain_loss(disp, c):
+        dm = d7.copy()
+        dm[:3] += disp[None, :] * d7[3:6]
+        j = oracle_mod.run("JM", f7, c, 0, 9, 9, dm, k)
+        o = oracle_mod.run("FF", dm, j, 1, 10, 12, ff7, k)
+        return float(((o - ideal.cpu().numpy()) ** 2).sum())
+
+    h = 1e-6 * lam
+    nodes = rng.choice(d7.shape[1], 8, replace=False)
+    fd = []
+    for i in nodes:
+        p, m = pert.copy(), pert.copy()
+        p[i] += h
+        m[i] -= h
+        fd.append((chain_loss(p, fcur) - chain_loss(m, fcur)) / (2 * h))
+    assert _rel(g_dd[nodes], np.array(fd)) <= 1e-4, (g_dd[nodes], fd)
+    ent = [(0, 10), (3, 40), (7, 22)]
+    fdc = []
+    for r, c in ent:
+        cp, cm = fcur.copy(), fcur.copy()
+        cp[r, c] += 1e-3
+        cm[r, c] -= 1e-3
+        fdc.append((chain_loss(pert, cp) - chain_loss(pert, cm)) / 2e-3)
+    assert _rel(np.array([g_cur[r, c] for r, c in ent]), np.array(fdc)) <= 1e-4
