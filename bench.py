@@ -3,20 +3,26 @@
 
 Workload (default `dish_eh`): paraboloid D 1000 mm, f 500 mm, uv 501x501
 (251,001 source points, lambda 1 mm) radiating to a 301x301 focal-plane grid
-(90,601 targets), mode EH: 2.27e10 source-target pairs per step. Inputs are
-seeded synthetic currents with the configuration's taper and phase noise.
+(90,601 targets), mode EH: 2.27e10 source-target pairs. Inputs are seeded
+synthetic currents with the configuration's taper and phase noise (M = 0).
 
-A step is one mixed-precision forward propagation of the whole workload.
-  value  pairs / s with inputs resident on the device (po_run_dev)
-  e2e    the same through the host-buffer C-ABI (po_run_d): H2D of the
-         step's inputs from pinned memory, the propagation, D2H of the fields
-Also reported: accuracy of the step's output against the plain FP64 GPU sum
-(sampled targets), the FP64 GPU sum's own pair rate, the FP32 roofline of the
-main kernel (CUDA events around every launch on its stream), the clocks seen
-during the timed region, and the FP64 CPU oracle on a bounded sample.
+A step is one forward propagation of the whole workload plus its adjoint:
+the gradient of a loss on the output fields (a fixed random cotangent) with
+respect to the source currents and to the normal displacement of every
+source and target point. value = pairs per step / step time (each pair
+counted once per forward+adjoint step).
+  value  inputs resident on the device (po_run_dev + po_adjoint_dev)
+  e2e    the same through the host-buffer C-ABI (po_run_d + po_adjoint_d):
+         H2D of each call's inputs from pinned memory and D2H of its outputs
+         inside the timed region
+Also reported: the forward and adjoint accuracy against the plain FP64 GPU
+path, the FP64 GPU path's own step rate, the FP32 roofline of each kernel
+(CUDA events around every launch on its stream), the clocks during the timed
+region, and the FP64 CPU oracle on a bounded sample.
 
 `--impl reference` times the reference's CPU path (its compiled library when
 it loads here, else the oracle's C restatement of it) on the same workload.
+The reference has no adjoint, so that arm times the forward pass.
 
 Multi-GPU: one process per GPU (torchrun); each rank runs its own replica of
 the workload (targets are independent, no collective on the data path);
@@ -37,8 +43,10 @@ ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Gpairs/s fwd+adjoint, mixed-prec vs FP64 sum, 1 GB300 at ≤1e-5 rel err vs FP64"
-#: algorithmic FP32 flops per pair (FMA = 2), split-precision overhead not counted
-FLOPS_PER_PAIR = {("EH", True): 234, ("EH", False): 140, ("FF", True): 61, ("FF", False): 37}
+#: algorithmic FP32 flops per pair (FMA = 2; split-precision overhead not counted)
+FWD_FLOPS = {("EH", True): 234, ("EH", False): 140, ("FF", True): 61, ("FF", False): 37}
+ADJ_SRC_FLOPS = {("EH", False): 416, ("FF", False): 99}   # currents + source displacement, M = 0 sources
+ADJ_TGT_FLOPS = {("EH", False): 245}                       # target displacement, M = 0 sources
 
 
 def dist_env():
@@ -105,8 +113,8 @@ def gpu_index(local):
     return local
 
 
-def cpu_oracle_rate(w, seconds, threads, impl_ref=False):
-    """Pairs/s of the FP64 CPU path on a target subsample sized to ~`seconds`."""
+def cpu_oracle_rate(w, seconds, threads):
+    """Pairs/s of the FP64 CPU oracle (forward) on a random target sample sized to ~`seconds`."""
     from oracle import oracle as O
     rng = np.random.default_rng(123)
     nt = w["t7"].shape[1]
@@ -170,10 +178,10 @@ def run_reference(args):
     for i in range(args.warmup + args.steps):
         if kind == "reference":
             rate, n, dt = reference_lib_rate(w, per_step, threads)
-            sample = f"{n} targets (leading grid rows) x {w['s7'].shape[1]} sources per step"
+            sample = f"{n} targets (leading grid rows) x {w['s7'].shape[1]} sources per step, forward only"
         else:
             rate, n, dt = cpu_oracle_rate(w, per_step, threads)
-            sample = f"{n} random targets x {w['s7'].shape[1]} sources per step"
+            sample = f"{n} random targets x {w['s7'].shape[1]} sources per step, forward only"
         if i >= args.warmup:
             rates.append(rate)
     value = float(np.mean(rates)) / 1e9
@@ -181,7 +189,8 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": w["pairs"] / (value * 1e9) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": w["name"], "desc": w["desc"], "pairs_per_step": w["pairs"],
-                                            "device": "cpu", "threads": threads},
+                                            "device": "cpu", "threads": threads,
+                                            "step": "forward propagation (the reference has no adjoint)"},
             "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": threads, "kind": kind,
                              "sample": sample},
             "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -205,23 +214,36 @@ def run_ours(args):
     mode, k = w["mode"], w["k"]
     m_zero = not np.any(w["cur"][6:])
     ns, nt = w["s7"].shape[1], w["t7"].shape[1]
+    nout = engine.n_out(mode)
+    far = mode == "FF"
+    rng = np.random.default_rng(7)
+    cot_np = rng.standard_normal((nout, nt))
     s7 = torch.tensor(w["s7"], device=dev)
     cur = torch.tensor(w["cur"], device=dev)
     t7 = torch.tensor(w["t7"], device=dev)
-    out = torch.empty((engine.n_out(mode), nt), dtype=torch.float64, device=dev)
+    cot = torch.tensor(cot_np, device=dev)
+    out = torch.empty((nout, nt), dtype=torch.float64, device=dev)
+    g_cur = torch.empty((12, ns), dtype=torch.float64, device=dev)
+    g_ds = torch.empty(ns, dtype=torch.float64, device=dev)
+    g_dt = None if far else torch.empty(nt, dtype=torch.float64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
     stream = torch.cuda.current_stream(dev)
+    grid = (w["gmode"], w["ncx"], w["ncy"])
 
     def step():
         flush.zero_()
-        engine.propagate_dev(mode, s7, cur, w["gmode"], w["ncx"], w["ncy"], t7, k, 1.0, -1.0, "mixed",
-                             m_zero=m_zero, out=out, stream=stream)
+        engine.propagate_dev(mode, s7, cur, *grid, t7, k, 1.0, -1.0, "mixed", m_zero=m_zero, out=out,
+                             stream=stream)
+        n1 = engine.last_launches()
+        engine.adjoint_dev(mode, s7, cur, *grid, t7, k, cot, 1.0, -1.0, "mixed", m_zero=m_zero, grad_cur=g_cur,
+                           grad_ds=g_ds, grad_dt=g_dt, stream=stream)
+        return n1 + engine.last_launches()
 
     for _ in range(args.warmup):
-        step()
+        launches_per_step = step()
     torch.cuda.synchronize()
-    launches_per_step = engine.last_launches()
-    engine.timing_enable(args.steps)
+    kernels_per_step = 2 if far else 3
+    engine.timing_enable(args.steps * kernels_per_step)
     sampler = ClockSampler(gpu_index(local))
     sampler.start()
     time.sleep(0.3)
@@ -238,7 +260,7 @@ def run_ours(args):
         torch.distributed.barrier()
     clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
-    main_ms = engine.timing_collect()
+    launch_ms = np.array(engine.timing_collect()).reshape(args.steps, kernels_per_step)
     engine.timing_enable(0)
     assert engine.device_error(stream) == 0, "a kernel reported a wait timeout"
     if world > 1:
@@ -248,15 +270,22 @@ def run_ours(args):
     value = w["pairs"] * args.steps * world / (ms * 1e-3) / 1e9
 
     # ---- end to end through the host-buffer C-ABI (pinned host memory)
-    s7_h = torch.from_numpy(np.ascontiguousarray(w["s7"])).pin_memory()
-    cur_h = torch.from_numpy(np.ascontiguousarray(w["cur"])).pin_memory()
-    t7_h = torch.from_numpy(np.ascontiguousarray(w["t7"])).pin_memory()
-    out_h = torch.empty((engine.n_out(mode), nt), dtype=torch.float64).pin_memory()
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    s7_h, cur_h, t7_h, cot_h = pin(w["s7"]), pin(w["cur"]), pin(w["t7"]), pin(cot_np)
+    out_h = torch.empty((nout, nt), dtype=torch.float64).pin_memory()
+    gc_h = torch.empty((12, ns), dtype=torch.float64).pin_memory()
+    gs_h = torch.empty(ns, dtype=torch.float64).pin_memory()
+    gt_h = torch.empty(nt, dtype=torch.float64).pin_memory()
+    lib = load()
 
     def step_e2e():
         flush.zero_()
-        engine.propagate(mode, s7_h.numpy(), cur_h.numpy(), w["gmode"], w["ncx"], w["ncy"], t7_h.numpy(), k,
-                         1.0, -1.0, "mixed", out=out_h.numpy())
+        engine.propagate(mode, s7_h.numpy(), cur_h.numpy(), *grid, t7_h.numpy(), k, 1.0, -1.0, "mixed",
+                         out=out_h.numpy())
+        rc = lib.po_adjoint_d(engine.MODE_ID[mode], ns, s7_h.data_ptr(), *grid, cur_h.data_ptr(), nt,
+                              t7_h.data_ptr(), float(k), 1.0, -1.0, 0, cot_h.data_ptr(), gc_h.data_ptr(),
+                              gs_h.data_ptr(), None if far else gt_h.data_ptr())
+        assert rc == 0, lib.po_last_error()
 
     for _ in range(max(1, args.warmup // 2)):
         step_e2e()
@@ -267,64 +296,85 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e = w["pairs"] * args.steps / e2e_s / 1e9 * world
-    h2d = (7 + 12) * ns * 8 + 7 * nt * 8
-    d2h = engine.n_out(mode) * nt * 8
+    h2d = 2 * (7 + 12) * ns * 8 + 2 * 7 * nt * 8 + nout * nt * 8
+    d2h = nout * nt * 8 + 13 * ns * 8 + (0 if far else nt * 8)
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
 
-    # ---- accuracy of the step's output against the plain FP64 GPU sum
-    rng = np.random.default_rng(0)
+    # ---- forward accuracy against the plain FP64 GPU sum (sampled targets, all sources)
     idx = np.sort(rng.choice(nt, size=min(1024, nt), replace=False))
     t7s = torch.tensor(np.ascontiguousarray(w["t7"][:, idx]), device=dev)
-    ref = engine.propagate_dev(mode, s7, cur, w["gmode"], w["ncx"], w["ncy"], t7s, k, 1.0, -1.0, "fp64")
-    got = out[:, idx]
+    ref = engine.propagate_dev(mode, s7, cur, *grid, t7s, k, 1.0, -1.0, "fp64")
     torch.cuda.synchronize()
-    ref_n, got_n = ref.cpu().numpy(), got.cpu().numpy()
+    ref_n, got_n = ref.cpu().numpy(), out[:, idx].cpu().numpy()
     rel_l2 = float(np.linalg.norm(got_n - ref_n) / np.linalg.norm(ref_n))
     rc = ref_n[0:3] + 1j * ref_n[3:6]
-    gc = got_n[0:3] + 1j * got_n[3:6]
+    gcx = got_n[0:3] + 1j * got_n[3:6]
     sel = np.abs(rc) >= np.abs(rc).max() * 0.1
-    max_phase = float(np.abs(np.angle(gc[sel] / rc[sel])).max())
+    max_phase = float(np.abs(np.angle(gcx[sel] / rc[sel])).max())
 
-    # ---- the FP64 GPU sum's own pair rate (all targets, every 16th source)
+    # ---- adjoint accuracy and FP64 step rate on a sub-problem (every 16th source, all targets)
     sub = slice(0, ns, 16)
-    s7f = s7[:, sub].contiguous()
-    curf = cur[:, sub].contiguous()
+    s7f, curf = s7[:, sub].contiguous(), cur[:, sub].contiguous()
     nsf = s7f.shape[1]
-    outf = torch.empty_like(out)
-    engine.propagate_dev(mode, s7f, curf, -1, 0, 0, t7, k, 1.0, -1.0, "fp64", out=outf)
+
+    def adj(prec):
+        gc = torch.empty((12, nsf), dtype=torch.float64, device=dev)
+        gs = torch.empty(nsf, dtype=torch.float64, device=dev)
+        gt = None if far else torch.empty(nt, dtype=torch.float64, device=dev)
+        engine.adjoint_dev(mode, s7f, curf, -1, 0, 0, t7, k, cot, 1.0, -1.0, prec, m_zero=m_zero, grad_cur=gc,
+                           grad_ds=gs, grad_dt=gt)
+        return gc, gs, gt
+
+    def rel(a, b):
+        return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+    am, ad = adj("mixed"), adj("fp64")
     torch.cuda.synchronize()
+    adj_acc = {"grad_cur_rel_l2": rel(am[0], ad[0]), "grad_ds_rel_l2": rel(am[1], ad[1])}
+    if not far:
+        adj_acc["grad_dt_rel_l2"] = rel(am[2], ad[2])
+    outf = torch.empty_like(out)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     engine.propagate_dev(mode, s7f, curf, -1, 0, 0, t7, k, 1.0, -1.0, "fp64", out=outf)
+    adj("fp64")
     e1.record(stream)
     torch.cuda.synchronize()
     fp64_rate = nsf * nt / (e0.elapsed_time(e1) * 1e-3) / 1e9
 
-    # ---- FP32 roofline of the main kernel
-    lib = load()
+    # ---- FP32 roofline of each kernel of the step
     probe = torch.empty(152 * 8 * 256, dtype=torch.float32, device=dev)
     blocks, iters = probe.numel() // 256, 100000
-    best = 0.0
+    peak = 0.0
     for _ in range(3):
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         p0.record(stream)
-        rc_ = lib.po_fp32_probe(blocks, iters, probe.data_ptr(), stream.cuda_stream)
+        assert lib.po_fp32_probe(blocks, iters, probe.data_ptr(), stream.cuda_stream) == 0
         p1.record(stream)
         torch.cuda.synchronize()
-        assert rc_ == 0
-        best = max(best, blocks * 256 * iters * 16 / (p0.elapsed_time(p1) * 1e-3) / 1e12)
-    fpp = FLOPS_PER_PAIR[(mode, not m_zero)]
-    launch_ms = float(np.mean(main_ms)) if main_ms else float("nan")
-    achieved = fpp * w["pairs"] / (launch_ms * 1e-3) / 1e12
+        peak = max(peak, blocks * 256 * iters * 16 / (p0.elapsed_time(p1) * 1e-3) / 1e12)
+    mk = ("EH" if not far else "FF", not m_zero)
+    names = ["forward po_main_kernel", "adjoint po_adj_src_kernel", "adjoint po_adj_tgt_kernel"]
+    flops = [FWD_FLOPS[mk], ADJ_SRC_FLOPS.get((mk[0], False)), ADJ_TGT_FLOPS.get((mk[0], False))]
+    kernels = []
+    for j in range(kernels_per_step):
+        lm = float(launch_ms[:, j].mean())
+        ach = flops[j] * w["pairs"] / (lm * 1e-3) / 1e12 if flops[j] else None
+        kernels.append({"kernel": names[j], "launch_ms": lm, "gpairs_per_s": w["pairs"] / (lm * 1e-3) / 1e9,
+                        "flops_per_pair": flops[j], "achieved_tflops": ach,
+                        "frac": ach / peak if ach else None})
+    dom = max(kernels, key=lambda x: x["launch_ms"])
     traffic = None
     prof = ROOT / "profiles" / f"traffic_{w['name']}.json"
-    if prof.exists():
-        traffic = json.loads(prof.read_text()).get("bytes_per_launch")
+    if prof.exists():   # DRAM bytes per launch from an ncu capture, per kernel
+        traffic = json.loads(prof.read_text()).get("kernels", {}).get(dom["kernel"].split()[-1])
+    step_flops = sum(f for f in flops[:kernels_per_step] if f)
+    step_ms_kernels = float(launch_ms.sum(axis=1).mean())
 
-    # ---- FP64 CPU oracle on a bounded sample
+    # ---- FP64 CPU oracle (forward) on a bounded sample
     threads = os.cpu_count() or 1
     cpu_rate, cpu_n, cpu_dt = cpu_oracle_rate(w, 10.0, threads)
 
@@ -332,23 +382,28 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded currents with the configuration's taper and phase noise)",
+        "data": "synthetic (seeded currents with the configuration's taper and phase noise; random cotangent)",
         "config": {"workload": w["name"], "desc": w["desc"], "ns": ns, "nt": nt, "pairs_per_step": w["pairs"],
-                   "step": "forward propagation (adjoint not in this step)",
+                   "step": "forward + adjoint (grad wrt currents, source and target normal displacement)",
                    "precision": "FP32 bulk; separation, R and phase in split hi/lo form",
-                   "l2": "flushed between steps (256 MB write inside the timed loop)",
+                   "l2": "flushed before every step (256 MB write inside the timed loop)",
                    "parallelism": f"replica per GPU x{world}"},
-        "accuracy": {"rel_l2": rel_l2, "max_phase_rad": max_phase,
-                     "against": f"plain FP64 GPU sum on {idx.size} random targets (all sources)",
-                     "phase_on": "E components within 20 dB of the sampled peak"},
-        "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s", "speedup": value / world / fp64_rate,
+        "forward_gpairs_per_s": kernels[0]["gpairs_per_s"],
+        "adjoint_gpairs_per_s": w["pairs"] / (sum(kk["launch_ms"] for kk in kernels[1:]) * 1e-3) / 1e9,
+        "accuracy": {"forward_rel_l2": rel_l2, "forward_max_phase_rad": max_phase,
+                     "forward_against": f"plain FP64 GPU sum on {idx.size} random targets (all sources)",
+                     "phase_on": "E components within 20 dB of the sampled peak",
+                     "adjoint": adj_acc,
+                     "adjoint_against": f"plain FP64 GPU adjoint, all targets x every 16th source ({nsf})"},
+        "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (fwd+adjoint step)", "speedup": value / world / fp64_rate,
                      "sample": f"all {nt} targets x every 16th source ({nsf})"},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": best, "unit": "TFLOP/s",
-                     "frac": achieved / best, "traffic": traffic,
-                     "flops_per_pair": fpp, "kernel": "po_main_kernel (near field, M=0)" if mode == "EH" else
-                     "po_main_kernel", "launch_ms": launch_ms,
+        "roofline": {"bound": "fp32", "kernel": dom["kernel"], "achieved": dom["achieved_tflops"], "peak": peak,
+                     "unit": "TFLOP/s", "frac": dom["frac"], "traffic": traffic,
+                     "flops_per_pair": dom["flops_per_pair"],
+                     "step_frac": step_flops * w["pairs"] / (step_ms_kernels * 1e-3) / 1e12 / peak,
+                     "kernels": kernels,
                      "peak_source": "measured: po_fp32_probe FFMA chains on this GPU, best of 3"},
-        "cpu_baseline": {"value": cpu_rate / 1e9, "unit": "Gpairs/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": cpu_rate / 1e9, "unit": "Gpairs/s (forward)", "cores": threads, "kind": "port",
                          "sample": f"{cpu_n} random targets x {ns} sources ({cpu_dt:.1f} s), FP64 oracle"},
         "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches_per_step * args.steps,

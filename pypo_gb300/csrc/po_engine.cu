@@ -412,8 +412,10 @@ int run_adjoint(const AdjArgs &a)
         if (!rc) rc = launch(adj_src_epilogue_kernel(), dim3(nblk_s), dim3(256), eargs, 0, s);
         if (!rc && grad_dt) {
             void *targs[] = {&srcd, &ns, &tgt7, &gam, &nt, &k, &partt};
+            timing_mark(s, true);
             rc = launch(adj_tgt_fp64_kernel(ts), dim3((unsigned)((nt + kThreadsD - 1) / kThreadsD)), dim3(kThreadsD),
                         targs, 0, s);
+            timing_mark(s, false);
             double one_d = 1.0;
             void *teargs[] = {&one, &nt, &partt, &one_d, &grad_dt};
             if (!rc) rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
@@ -493,7 +495,9 @@ int run_adjoint(const AdjArgs &a)
         if (!rc && (rc = salloc(&partt, (size_t)splitB * nt, s, owned))) { sfree(owned, s); return rc; }
         const float4 *tgc = tgtpk;
         void *targs[] = {&srcc, &ns, &chunkB, &tgc, &gam, &tgt7, &nt, &partt, &err};
+        timing_mark(s, true);
         if (!rc) rc = launch(ftgt, dim3((unsigned)ntb, (unsigned)splitB), dim3(kThreadsA), targs, smem, s);
+        timing_mark(s, false);
         int nsplB = (int)splitB;
         double dsct = kappa;
         void *teargs[] = {&nsplB, &nt, &partt, &dsct, &grad_dt};
