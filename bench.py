@@ -210,7 +210,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    w = configs.WORKLOADS[args.workload]()
+    w = configs.WORKLOADS[args.workload](scale=args.scale)
     mode, k = w["mode"], w["k"]
     m_zero = not np.any(w["cur"][6:])
     ns, nt = w["s7"].shape[1], w["t7"].shape[1]
@@ -383,7 +383,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded currents with the configuration's taper and phase noise; random cotangent)",
-        "config": {"workload": w["name"], "desc": w["desc"], "ns": ns, "nt": nt, "pairs_per_step": w["pairs"],
+        "config": {"workload": w["name"] + ("" if args.scale == 1.0 else f" (scale {args.scale})"), "desc": w["desc"],
+                   "ns": ns, "nt": nt, "pairs_per_step": w["pairs"],
                    "step": "forward + adjoint (grad wrt currents, source and target normal displacement)",
                    "precision": "FP32 bulk; separation, R and phase in split hi/lo form",
                    "l2": "flushed before every step (256 MB write inside the timed loop)",
@@ -421,6 +422,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dish_eh", choices=["dish_eh", "dish_ff"])
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="shrink both grids (profiling runs only; the bench line is the full size)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

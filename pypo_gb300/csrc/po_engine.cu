@@ -450,7 +450,7 @@ int run_adjoint(const AdjArgs &a)
 
     // source side: sources in registers, targets streamed
     void *fsrc = adj_src_kernel(kind, ts, has_m, want_d);
-    const int smem = kStages * kTile * kRec * 16;
+    const int smem = kStages * kTile * kRec * 16 + kAccAdj * kThreadsA * 4;
     int occ = 1;
     if (!rc) {
         PO_CK(cudaFuncSetAttribute(fsrc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));

@@ -59,92 +59,93 @@ __device__ __forceinline__ void nf_pair(float *acc, const float4 &tA, const floa
     const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
     const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
     const float R2 = __fadd_rn(S0, S1);
-    const float rinv = rsqrtf(R2);
-    const float Rh = __fmul_rn(R2, rinv);
+    const float rinv0 = rsqrtf(R2);
+    const float Rh = __fmul_rn(R2, rinv0);
     const float p = __fmul_rn(Rh, Rh);
     const float pe = fmaf(Rh, Rh, -p);
+    // R = Rh + res / (2 Rh): res is the exact residual of Rh^2 against S0 + S1.
     const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
-    const float Rl = __fmul_rn(res, __fmul_rn(0.5f, rinv));
-    // Phase in turns, reduced to [-1/2, 1/2].
-    const float f = __fadd_rn(__fsub_rn(Rh, rint_magic(Rh)), Rl);
+    // Twice the reduced phase in turns, 2 (Rh - rint(Rh)) + res / Rh, in [-1, 1].
+    const float x = __fsub_rn(Rh, rint_magic(Rh));
+    const float f2 = fmaf(res, rinv0, __fadd_rn(x, x));
     float sn, cs;
-    __sincosf(f * 6.28318530717958647f, &sn, &cs);
-    // Unnormalised separation and the illumination test n . d >= 0.
+    __sincosf(f2 * 3.14159265358979324f, &sn, &cs);
+    // Unnormalised separation and the illumination test n . d >= -tol R:
+    // pairs within rounding of exact tangency count as lit (the reference
+    // keeps n . R_hat == 0). An unlit pair gets 1/R = 0, which zeroes every
+    // coefficient below.
     const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
-    // Pairs within rounding of exact tangency count as lit (the reference
-    // keeps n . R_hat == 0), so regular grids with tangent pairs agree.
     const float ndd = fmaf(r[5].x, dz, fmaf(r1.w, dy, r0.w * dx));
-    const bool lit = ndd >= -kTangentTol32 * Rh;
-    const float gc = lit ? cs : 0.0f;
-    const float gs = lit ? (T > 0 ? sn : -sn) : 0.0f;   // G = e^{t j theta}
-    // s1 = t u^2 + j (u^3 - u); s2 = -3 s1 - 2 j u; s3 = -u^2 + j t u; u = 1/(kR).
+    const float rinv = fmaf(kTangentTol32, Rh, ndd) >= 0.0f ? rinv0 : 0.0f;
+    const float ex = dx * rinv, ey = dy * rinv, ez = dz * rinv;   // R_hat
+    // u = 1/(kR), Gu = e^{t j kR} u; then with R_hat instead of d:
+    //   c1  = Gu (t u + j(u^2 - 1))          (s1 = t u^2 + j(u^3 - u))
+    //   c2  = -3 c1 - 2 j Gu                 (s2 R-scaled)
+    //   c3  = Gu (-u + j t)                  (s3 R-scaled)
+    // E = c1 J + c2 (J.R_hat) R_hat + c3 (M x R_hat);  H = c1 M + c2 (M.R_hat) R_hat - c3 (J x R_hat)
     const float u = rinv * 0.159154943091895336f;
-    const float u2 = u * u;
-    const float s1r = T > 0 ? u2 : -u2;
-    const float s1i = fmaf(u2, u, -u);
-    const float c1r = gc * s1r - gs * s1i;
-    const float c1i = gc * s1i + gs * s1r;
-    const float rinv2 = rinv * rinv;
-    const float tu = 2.0f * u;
-    const float c2r = fmaf(-3.0f, c1r, tu * gs) * rinv2;    // G s2 / R^2
-    const float c2i = fmaf(-3.0f, c1i, -tu * gc) * rinv2;
-    const float s3r = -u2 * rinv;
-    const float s3i = (T > 0 ? u : -u) * rinv;
-    const float c3r = gc * s3r - gs * s3i;                    // G s3 / R
-    const float c3i = gc * s3i + gs * s3r;
+    const float gur = cs * u;
+    const float gui = (T > 0 ? sn : -sn) * u;
+    const float tu = T > 0 ? u : -u;
+    const float b = fmaf(u, u, -1.0f);
+    const float c1r = fmaf(gur, tu, -gui * b);
+    const float c1i = fmaf(gur, b, gui * tu);
+    const float c2r = fmaf(-3.0f, c1r, gui + gui);
+    const float c2i = fmaf(-3.0f, c1i, -(gur + gur));
+    const float c3r = T > 0 ? fmaf(-gur, u, -gui) : fmaf(-gur, u, gui);
+    const float c3i = T > 0 ? fmaf(-gui, u, gur) : fmaf(-gui, u, -gur);
 
     const float jxr = r2.x, jxi = r2.y, jyr = r2.z, jyi = r2.w, jzr = r3.x, jzi = r3.y;
-    // J . d and P = c2 (J . d)
-    const float jdr = fmaf(jzr, dz, fmaf(jyr, dy, jxr * dx));
-    const float jdi = fmaf(jzi, dz, fmaf(jyi, dy, jxi * dx));
-    const float Pr = c2r * jdr - c2i * jdi;
-    const float Pi = c2r * jdi + c2i * jdr;
-    // J x d
-    const float axr = jyr * dz - jzr * dy, axi = jyi * dz - jzi * dy;
-    const float ayr = jzr * dx - jxr * dz, ayi = jzi * dx - jxi * dz;
-    const float azr = jxr * dy - jyr * dx, azi = jxi * dy - jyi * dx;
-    // E += c1 J + P d
-    acc[0] += c1r * jxr - c1i * jxi + Pr * dx;
-    acc[1] += c1r * jyr - c1i * jyi + Pr * dy;
-    acc[2] += c1r * jzr - c1i * jzi + Pr * dz;
-    acc[3] += c1r * jxi + c1i * jxr + Pi * dx;
-    acc[4] += c1r * jyi + c1i * jyr + Pi * dy;
-    acc[5] += c1r * jzi + c1i * jzr + Pi * dz;
-    // H -= c3 (J x d)
-    acc[6] -= c3r * axr - c3i * axi;
-    acc[7] -= c3r * ayr - c3i * ayi;
-    acc[8] -= c3r * azr - c3i * azi;
-    acc[9] -= c3r * axi + c3i * axr;
-    acc[10] -= c3r * ayi + c3i * ayr;
-    acc[11] -= c3r * azi + c3i * azr;
+    // P = c2 (J . R_hat)
+    const float jer = fmaf(jzr, ez, fmaf(jyr, ey, jxr * ex));
+    const float jei = fmaf(jzi, ez, fmaf(jyi, ey, jxi * ex));
+    const float Pr = fmaf(c2r, jer, -c2i * jei);
+    const float Pi = fmaf(c2r, jei, c2i * jer);
+    // E += c1 J + P R_hat  (three FMAs into each accumulator)
+    acc[0] = fmaf(Pr, ex, fmaf(-c1i, jxi, fmaf(c1r, jxr, acc[0])));
+    acc[1] = fmaf(Pr, ey, fmaf(-c1i, jyi, fmaf(c1r, jyr, acc[1])));
+    acc[2] = fmaf(Pr, ez, fmaf(-c1i, jzi, fmaf(c1r, jzr, acc[2])));
+    acc[3] = fmaf(Pi, ex, fmaf(c1i, jxr, fmaf(c1r, jxi, acc[3])));
+    acc[4] = fmaf(Pi, ey, fmaf(c1i, jyr, fmaf(c1r, jyi, acc[4])));
+    acc[5] = fmaf(Pi, ez, fmaf(c1i, jzr, fmaf(c1r, jzi, acc[5])));
+    // H -= K x R_hat with K = c3 J
+    const float kxr = fmaf(c3r, jxr, -c3i * jxi), kxi = fmaf(c3r, jxi, c3i * jxr);
+    const float kyr = fmaf(c3r, jyr, -c3i * jyi), kyi = fmaf(c3r, jyi, c3i * jyr);
+    const float kzr = fmaf(c3r, jzr, -c3i * jzi), kzi = fmaf(c3r, jzi, c3i * jzr);
+    acc[6] = fmaf(kzr, ey, fmaf(-kyr, ez, acc[6]));
+    acc[7] = fmaf(kxr, ez, fmaf(-kzr, ex, acc[7]));
+    acc[8] = fmaf(kyr, ex, fmaf(-kxr, ey, acc[8]));
+    acc[9] = fmaf(kzi, ey, fmaf(-kyi, ez, acc[9]));
+    acc[10] = fmaf(kxi, ez, fmaf(-kzi, ex, acc[10]));
+    acc[11] = fmaf(kyi, ex, fmaf(-kxi, ey, acc[11]));
     if (HAS_M) {
         const float4 r4 = r[4];
         const float mxr = r3.z, mxi = r3.w, myr = r4.x, myi = r4.y, mzr = r4.z, mzi = r4.w;
-        const float mdr = fmaf(mzr, dz, fmaf(myr, dy, mxr * dx));
-        const float mdi = fmaf(mzi, dz, fmaf(myi, dy, mxi * dx));
-        const float Qr = c2r * mdr - c2i * mdi;
-        const float Qi = c2r * mdi + c2i * mdr;
-        const float bxr = myr * dz - mzr * dy, bxi = myi * dz - mzi * dy;
-        const float byr = mzr * dx - mxr * dz, byi = mzi * dx - mxi * dz;
-        const float bzr = mxr * dy - myr * dx, bzi = mxi * dy - myi * dx;
-        // E += c3 (M x d)
-        acc[0] += c3r * bxr - c3i * bxi;
-        acc[1] += c3r * byr - c3i * byi;
-        acc[2] += c3r * bzr - c3i * bzi;
-        acc[3] += c3r * bxi + c3i * bxr;
-        acc[4] += c3r * byi + c3i * byr;
-        acc[5] += c3r * bzi + c3i * bzr;
-        // H += c1 M + Q d
-        acc[6] += c1r * mxr - c1i * mxi + Qr * dx;
-        acc[7] += c1r * myr - c1i * myi + Qr * dy;
-        acc[8] += c1r * mzr - c1i * mzi + Qr * dz;
-        acc[9] += c1r * mxi + c1i * mxr + Qi * dx;
-        acc[10] += c1r * myi + c1i * myr + Qi * dy;
-        acc[11] += c1r * mzi + c1i * mzr + Qi * dz;
+        const float mer = fmaf(mzr, ez, fmaf(myr, ey, mxr * ex));
+        const float mei = fmaf(mzi, ez, fmaf(myi, ey, mxi * ex));
+        const float Qr = fmaf(c2r, mer, -c2i * mei);
+        const float Qi = fmaf(c2r, mei, c2i * mer);
+        // H += c1 M + Q R_hat
+        acc[6] = fmaf(Qr, ex, fmaf(-c1i, mxi, fmaf(c1r, mxr, acc[6])));
+        acc[7] = fmaf(Qr, ey, fmaf(-c1i, myi, fmaf(c1r, myr, acc[7])));
+        acc[8] = fmaf(Qr, ez, fmaf(-c1i, mzi, fmaf(c1r, mzr, acc[8])));
+        acc[9] = fmaf(Qi, ex, fmaf(c1i, mxr, fmaf(c1r, mxi, acc[9])));
+        acc[10] = fmaf(Qi, ey, fmaf(c1i, myr, fmaf(c1r, myi, acc[10])));
+        acc[11] = fmaf(Qi, ez, fmaf(c1i, mzr, fmaf(c1r, mzi, acc[11])));
+        // E += L x R_hat with L = c3 M
+        const float lxr = fmaf(c3r, mxr, -c3i * mxi), lxi = fmaf(c3r, mxi, c3i * mxr);
+        const float lyr = fmaf(c3r, myr, -c3i * myi), lyi = fmaf(c3r, myi, c3i * myr);
+        const float lzr = fmaf(c3r, mzr, -c3i * mzi), lzi = fmaf(c3r, mzi, c3i * mzr);
+        acc[0] = fmaf(lyr, ez, fmaf(-lzr, ey, acc[0]));
+        acc[1] = fmaf(lzr, ex, fmaf(-lxr, ez, acc[1]));
+        acc[2] = fmaf(lxr, ey, fmaf(-lyr, ex, acc[2]));
+        acc[3] = fmaf(lyi, ez, fmaf(-lzi, ey, acc[3]));
+        acc[4] = fmaf(lzi, ex, fmaf(-lxi, ez, acc[4]));
+        acc[5] = fmaf(lxi, ey, fmaf(-lyi, ex, acc[5]));
     }
 }
 
-// Far field: target record tA = (rh.x, rh.y, rh.z, rl.x), tB = (rl.y, rl.z, r.x?, -);
+// Far field: target record tA = (rh.x, rh.y, rh.z, rl.x), tB = (rl.y, rl.z, -, -);
 // the full direction r = rh + rl is passed separately (per-target constant).
 template <int T, bool HAS_M>
 __device__ __forceinline__ void ff_pair(float *acc, const float4 &tA, const float4 &tB, const float3 &rr,
@@ -162,20 +163,20 @@ __device__ __forceinline__ void ff_pair(float *acc, const float4 &tA, const floa
     const bool lit = ndr >= -kTangentTol32;
     const float gc = lit ? cs : 0.0f;
     const float gs = lit ? (T > 0 ? -sn : sn) : 0.0f;   // G = e^{-t j theta}
-    acc[0] += gc * r2.x - gs * r2.y;
-    acc[3] += gc * r2.y + gs * r2.x;
-    acc[1] += gc * r2.z - gs * r2.w;
-    acc[4] += gc * r2.w + gs * r2.z;
-    acc[2] += gc * r3.x - gs * r3.y;
-    acc[5] += gc * r3.y + gs * r3.x;
+    acc[0] = fmaf(-gs, r2.y, fmaf(gc, r2.x, acc[0]));
+    acc[3] = fmaf(gs, r2.x, fmaf(gc, r2.y, acc[3]));
+    acc[1] = fmaf(-gs, r2.w, fmaf(gc, r2.z, acc[1]));
+    acc[4] = fmaf(gs, r2.z, fmaf(gc, r2.w, acc[4]));
+    acc[2] = fmaf(-gs, r3.y, fmaf(gc, r3.x, acc[2]));
+    acc[5] = fmaf(gs, r3.x, fmaf(gc, r3.y, acc[5]));
     if (HAS_M) {
         const float4 r4 = r[4];
-        acc[6] += gc * r3.z - gs * r3.w;
-        acc[9] += gc * r3.w + gs * r3.z;
-        acc[7] += gc * r4.x - gs * r4.y;
-        acc[10] += gc * r4.y + gs * r4.x;
-        acc[8] += gc * r4.z - gs * r4.w;
-        acc[11] += gc * r4.w + gs * r4.z;
+        acc[6] = fmaf(-gs, r3.w, fmaf(gc, r3.z, acc[6]));
+        acc[9] = fmaf(gs, r3.z, fmaf(gc, r3.w, acc[9]));
+        acc[7] = fmaf(-gs, r4.y, fmaf(gc, r4.x, acc[7]));
+        acc[10] = fmaf(gs, r4.x, fmaf(gc, r4.y, acc[10]));
+        acc[8] = fmaf(-gs, r4.w, fmaf(gc, r4.z, acc[8]));
+        acc[11] = fmaf(gs, r4.z, fmaf(gc, r4.w, acc[11]));
     }
 }
 
@@ -194,14 +195,14 @@ __device__ __forceinline__ void sc_pair(float *acc, const float4 &tA, const floa
     const float p = __fmul_rn(Rh, Rh);
     const float pe = fmaf(Rh, Rh, -p);
     const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
-    const float Rl = __fmul_rn(res, __fmul_rn(0.5f, rinv));
-    const float f = __fadd_rn(__fsub_rn(Rh, rint_magic(Rh)), Rl);
+    const float x = __fsub_rn(Rh, rint_magic(Rh));
+    const float f2 = fmaf(res, rinv, __fadd_rn(x, x));
     float sn, cs;
-    __sincosf(f * 6.28318530717958647f, &sn, &cs);
+    __sincosf(f2 * 3.14159265358979324f, &sn, &cs);
     const float gr = cs * rinv;
     const float gi = (T > 0 ? -sn : sn) * rinv;
-    acc[0] += gr * r0.w - gi * r1.w;
-    acc[1] += gr * r1.w + gi * r0.w;
+    acc[0] = fmaf(-gi, r1.w, fmaf(gr, r0.w, acc[0]));
+    acc[1] = fmaf(gi, r0.w, fmaf(gr, r1.w, acc[1]));
 }
 
 // --------------------------------------------------------------- main kernel
@@ -234,11 +235,17 @@ po_main_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4
         rr[j] = make_float3(tA[j].x + tA[j].w, tA[j].y + tB[j].x, tA[j].z + tB[j].y);
     }
 
-    float hi[TPT][NACC], lo[TPT][NACC];
+    // Float-float totals: hi in registers, the compensation words (touched
+    // once per tile) in shared memory, [accumulator][target][thread].
+    float hi[TPT][NACC];
+    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * kTile * REC);
 #pragma unroll
     for (int j = 0; j < TPT; ++j)
 #pragma unroll
-        for (int a = 0; a < NACC; ++a) { hi[j][a] = 0.f; lo[j][a] = 0.f; }
+        for (int a = 0; a < NACC; ++a) {
+            hi[j][a] = 0.f;
+            lo[(a * TPT + j) * kThreads + threadIdx.x] = 0.f;
+        }
 
     const long s0 = (long)blockIdx.y * chunk;
     const long s1 = min(ns, s0 + chunk);
@@ -298,7 +305,8 @@ po_main_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4
                 float s, e;
                 two_sum(hi[j][a], acc[j][a], s, e);
                 hi[j][a] = s;
-                lo[j][a] = __fadd_rn(lo[j][a], e);
+                float &l = lo[(a * TPT + j) * kThreads + threadIdx.x];
+                l = __fadd_rn(l, e);
             }
         __syncthreads();   // everyone is done reading this stage
         if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
@@ -317,7 +325,8 @@ po_main_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4
         if (ti >= nt) continue;
 #pragma unroll
         for (int a = 0; a < NACC; ++a)
-            part[((long)blockIdx.y * NACC + a) * nt + ti] = (double)hi[j][a] + (double)lo[j][a];
+            part[((long)blockIdx.y * NACC + a) * nt + ti] =
+                (double)hi[j][a] + (double)lo[(a * TPT + j) * kThreads + threadIdx.x];
     }
 }
 

@@ -54,9 +54,11 @@ struct Frame {
     double inv_q;
 };
 
+// Tile stages plus the per-thread compensation words of the totals.
 inline int main_smem_bytes(int kind)
 {
-    return kStages * kTile * (kind == kKindScalar ? kRecScalar : kRec) * 16;
+    const int nacc = kind == kKindScalar ? 2 : kAcc;
+    return kStages * kTile * (kind == kKindScalar ? kRecScalar : kRec) * 16 + nacc * kTPT * kThreads * 4;
 }
 
 void *main_kernel(int kind, int t_sign, bool has_m);
