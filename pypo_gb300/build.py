@@ -25,16 +25,31 @@ def nvcc():
     return path
 
 
-def _compile(src, verbose=False):
-    obj = BUILD / (src + ".o")
+def _compile(src, verbose=False, defines=(), build_dir=None):
+    obj = (build_dir or BUILD) / (src + ".o")
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
-           "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
+           *[f"-D{d}" for d in defines], "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
     if verbose and src.endswith(".cu"):
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
     return obj, r.stderr
+
+
+def build_variant(out_path, defines, verbose=False):
+    """Build a copy of the library with PO_* tuning macros into out_path (tuning sweeps)."""
+    out_path = pathlib.Path(out_path)
+    bdir = out_path.parent / (out_path.stem + "_obj")
+    bdir.mkdir(parents=True, exist_ok=True)
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        results = list(ex.map(lambda s: _compile(s, verbose, defines, bdir), SOURCES))
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", str(out_path), *[str(o) for o, _ in results],
+           "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return out_path, [log for _, log in results]
 
 
 def build(verbose=False, force=False):

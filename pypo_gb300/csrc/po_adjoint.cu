@@ -597,7 +597,7 @@ __device__ __forceinline__ void nf_adj_tgt_pair(float *acc, const float4 *rec, c
 //   far field:  (rh, rl.x), (rl.y, rl.z, 0, 0), (gSJ ...), ..., (r, 0)
 // Writes 13 accumulators per source per target chunk.
 template <int KIND, int T, bool HAS_M, bool WANT_D>
-__global__ void __launch_bounds__(kThreadsA)
+__global__ void __launch_bounds__(kThreadsA, kMinBlocksA)
 po_adj_src_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
                   double *__restrict__ part, int *__restrict__ err)
 {
@@ -704,7 +704,7 @@ po_adj_src_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__res
 // thread a = conj(gE), b = conj(gH) from the cotangent rows; streams the
 // forward-packed source records. One accumulator: n_t . sum_s grad_d phi.
 template <int T, bool HAS_M>
-__global__ void __launch_bounds__(kThreadsA)
+__global__ void __launch_bounds__(kThreadsA, kMinBlocksA)
 po_adj_tgt_kernel(const float4 *__restrict__ srcpk, long ns, long chunk, const float4 *__restrict__ tgtpk,
                   const double *__restrict__ gam, const double *__restrict__ tgt7, long nt,
                   double *__restrict__ part, int *__restrict__ err)

@@ -208,7 +208,7 @@ __device__ __forceinline__ void sc_pair(float *acc, const float4 &tA, const floa
 // --------------------------------------------------------------- main kernel
 
 template <int KIND, int T, bool HAS_M, int TPT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
 po_main_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt,
                long nt, double *__restrict__ part, int *__restrict__ err)
 {

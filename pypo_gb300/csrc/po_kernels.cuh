@@ -13,11 +13,31 @@ constexpr int kKindNF = 0;      // near field (JM, EH, JMEH, EHP)
 constexpr int kKindFF = 1;      // far field
 constexpr int kKindScalar = 2;  // scalar Green's function
 
-// Mixed-precision N-body kernel geometry.
-constexpr int kThreads = 128;   // threads per CTA
-constexpr int kTPT = 2;         // targets per thread (registers)
-constexpr int kTile = 128;      // sources per shared-memory stage
-constexpr int kStages = 3;      // TMA pipeline depth
+// Mixed-precision N-body kernel geometry (the PO_* macros exist for tuning
+// sweeps; the defaults are the shipped configuration).
+#ifndef PO_THREADS
+#define PO_THREADS 128
+#endif
+#ifndef PO_TPT
+#define PO_TPT 2
+#endif
+#ifndef PO_TILE
+#define PO_TILE 128
+#endif
+#ifndef PO_MINB
+#define PO_MINB 1
+#endif
+#ifndef PO_THREADS_A
+#define PO_THREADS_A 128
+#endif
+#ifndef PO_MINB_A
+#define PO_MINB_A 1
+#endif
+constexpr int kThreads = PO_THREADS;   // threads per CTA
+constexpr int kTPT = PO_TPT;           // targets per thread (registers)
+constexpr int kTile = PO_TILE;         // sources per shared-memory stage
+constexpr int kMinBlocks = PO_MINB;    // resident CTAs per SM asked of ptxas
+constexpr int kStages = 3;             // TMA pipeline depth
 constexpr int kRec = 6;         // float4 per packed source record (96 B)
 constexpr int kRecScalar = 2;   // float4 per packed scalar record (32 B)
 constexpr int kAcc = 12;        // accumulators per target (E, H re/im x y z)
@@ -25,7 +45,8 @@ constexpr uint32_t kWaitLimit = 1u << 24;   // bounded mbarrier polls
 
 // Adjoint kernels: one source (or target) per thread; 12 current
 // accumulators + 1 displacement accumulator.
-constexpr int kThreadsA = 128;
+constexpr int kThreadsA = PO_THREADS_A;
+constexpr int kMinBlocksA = PO_MINB_A;
 constexpr int kAccAdj = 13;
 
 // FP64 comparison kernel.
