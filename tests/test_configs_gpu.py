@@ -1,0 +1,151 @@
+"""The benchmark configurations as parity cases (GPU).
+
+C1 feed -> dish JM (full size) against the oracle; C2 dish EH and C3 dish far
+field (full size, 2.3e10 and 1.6e11 pairs) against the plain FP64 GPU sum on
+sampled targets and the oracle on a few; C4 feed -> perturbed dish -> far
+field with gradients of sum |E_ff - E_ideal|^2 against central finite
+differences (h = 1e-6 lambda) on 64 random dish nodes; C5 Cassegrain chain
+(reduced grids) against the FP64 chain, forward and gradients.
+"""
+import numpy as np
+import pytest
+
+from tests.common import PHASE_TOL, REL_L2_TOL, errors
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_c1_feed_to_dish_full_size(cuda, lib, oracle_mod):
+    from pypo_gb300 import configs, engine
+    w = configs.feed_dish_jm()
+    args = (w["mode"], w["s7"], w["cur"], w["gmode"], w["ncx"], w["ncy"], w["t7"], w["k"])
+    got = engine.propagate(*args)
+    ref = oracle_mod.run(*args)
+    e, p = errors(got, ref, "JM")
+    assert e <= REL_L2_TOL and p <= PHASE_TOL, (e, p)
+
+
+@pytest.mark.parametrize("name", ["dish_eh", "dish_ff"])
+def test_c2_c3_full_size_sampled(cuda, lib, oracle_mod, name):
+    """Full-size run; per-point error on a 2 % random target sample against the
+    FP64 GPU sum, and on 16 targets against the oracle."""
+    import torch
+    from pypo_gb300 import configs, engine
+    w = getattr(configs, name)()
+    dev = cuda
+    s7, cur, t7 = (torch.tensor(w[k], device=dev) for k in ("s7", "cur", "t7"))
+    grid = (w["gmode"], w["ncx"], w["ncy"])
+    got = engine.propagate_dev(w["mode"], s7, cur, *grid, t7, w["k"], m_zero=True).cpu().numpy()
+    rng = np.random.default_rng(0)
+    nt = t7.shape[1]
+    idx = np.sort(rng.choice(nt, size=max(16, nt // 50), replace=False))
+    t7s = torch.tensor(np.ascontiguousarray(w["t7"][:, idx]), device=dev)
+    ref = engine.propagate_dev(w["mode"], s7, cur, *grid, t7s, w["k"], precision="fp64").cpu().numpy()
+    e, p = errors(got[:, idx], ref, w["mode"])
+    assert e <= REL_L2_TOL and p <= PHASE_TOL, (name, e, p)
+    sub = idx[:: max(1, idx.size // 16)][:16]
+    oref = oracle_mod.run(w["mode"], w["s7"], w["cur"], *grid, w["t7"], w["k"], tidx=sub)
+    e2, _ = errors(got[:, sub], oref, w["mode"])
+    assert e2 <= REL_L2_TOL, (name, e2)
+
+
+def _trap_weight(i, gmode, ncx, ncy):
+    xu, yv = i // ncy, i % ncy
+    w = 0.5 if xu in (0, ncx - 1) else 1.0
+    if gmode != 1 and yv in (0, ncy - 1):
+        w *= 0.5
+    return w
+
+
+def test_c4_chain_gradients_against_finite_differences(cuda, lib):
+    """feed -> dish (JM) -> far field (FF), dish displaced by a correlated surface
+    error; L = sum |E_ff - E_ideal|^2 (E rows). Autograd (mixed) gradients against
+    central FD of the FP64 GPU chain on 64 random nodes, and against the FP64
+    autograd gradients on every node."""
+    import torch
+    from pypo_gb300 import autograd as A, configs, engine
+    c = configs.dish_chain()
+    dev = cuda
+    T = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
+    k, lam = c["k"], c["lam"]
+    f7, fcur, d7, ff7 = c["feed7"], c["feed_cur"], c["dish7"], c["ff7"]
+    fg, dg = c["feed_grid"], c["dish_grid"]
+    nd = d7.shape[1]
+    # ideal far field: unperturbed dish, FP64
+    j0 = engine.propagate("JM", f7, fcur, *fg, d7, k, precision="fp64")
+    ideal = engine.propagate("FF", d7, j0, *dg, ff7, k, precision="fp64")
+
+    def grads(precision):
+        dd = T(c["delta"]).requires_grad_(True)
+        fc = T(fcur).requires_grad_(True)
+        jm = A.propagate("JM", T(f7), fc, *fg, T(d7), k, dt=dd, precision=precision)
+        ff = A.propagate("FF", T(d7), jm, *dg, T(ff7), k, ds=dd, precision=precision)
+        loss = ((ff[0:6] - T(ideal)[0:6]) ** 2).sum()
+        loss.backward()
+        return dd.grad.cpu().numpy(), fc.grad.cpu().numpy(), float(loss)
+
+    g_mixed, gf_mixed, loss_mixed = grads("mixed")
+    g_fp64, gf_fp64, loss_fp64 = grads("fp64")
+    assert abs(loss_mixed - loss_fp64) <= 1e-5 * loss_fp64
+    assert _rel(g_mixed, g_fp64) <= 1e-4
+    assert _rel(gf_mixed, gf_fp64) <= 1e-4
+
+    # central FD of the FP64 chain, one node at a time (exact by linearity:
+    # moving node i changes its induced current and its far-field term only)
+    disp = d7.copy()
+    disp[:3] += c["delta"][None, :] * d7[3:6]
+    jd = engine.propagate("JM", f7, fcur, *fg, disp, k, precision="fp64")
+    base = engine.propagate("FF", disp, jd, *dg, ff7, k, precision="fp64")
+
+    def one(i, pos):
+        p7 = disp[:, i:i + 1].copy()
+        p7[:3, 0] = pos
+        ji = engine.propagate("JM", f7, fcur, *fg, p7, k, precision="fp64")
+        s1 = p7.copy()
+        s1[6, 0] = d7[6, i] * _trap_weight(i, *dg)
+        return engine.propagate("FF", s1, ji, -1, 0, 0, ff7, k, precision="fp64")
+
+    def loss_at(i, pos):
+        e = base - one(i, disp[:3, i]) + one(i, pos)
+        return float(((e[0:6] - ideal[0:6]) ** 2).sum())
+
+    h = 1e-6 * lam
+    nodes = np.random.default_rng(2).choice(nd, 64, replace=False)
+    fd = np.array([(loss_at(i, disp[:3, i] + h * d7[3:6, i]) - loss_at(i, disp[:3, i] - h * d7[3:6, i])) / (2 * h)
+                   for i in nodes])
+    assert _rel(g_mixed[nodes], fd) <= 1e-4, np.c_[g_mixed[nodes], fd][:8]
+    assert _rel(g_fp64[nodes], fd) <= 1e-6
+
+
+def test_c5_cassegrain_chain_against_fp64(cuda, lib):
+    """feed -> hyperboloid (JM) -> paraboloid (JM) -> far field on reduced grids:
+    the mixed chain and its displacement gradients against the FP64 chain."""
+    import torch
+    from pypo_gb300 import autograd as A, configs
+    c = configs.cassegrain(scale=0.2)
+    dev = cuda
+    T = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
+    k = c["k"]
+    ref_ff = None
+    out = {}
+    for precision in ("fp64", "mixed"):
+        ds = torch.zeros(c["sec7"].shape[1], dtype=torch.float64, device=dev, requires_grad=True)
+        dp = torch.zeros(c["prim7"].shape[1], dtype=torch.float64, device=dev, requires_grad=True)
+        j1 = A.propagate("JM", T(c["feed7"]), T(c["feed_cur"]), *c["feed_grid"], T(c["sec7"]), k, dt=ds,
+                         precision=precision)
+        j2 = A.propagate("JM", T(c["sec7"]), j1, *c["sec_grid"], T(c["prim7"]), k, ds=ds, dt=dp,
+                         precision=precision)
+        ff = A.propagate("FF", T(c["prim7"]), j2, *c["prim_grid"], T(c["ff7"]), k, ds=dp, precision=precision)
+        if ref_ff is None:
+            ref_ff = ff.detach().clone()
+        loss = (ff[0:6] * ref_ff[0:6]).sum()
+        loss.backward()
+        out[precision] = (ff.detach().cpu().numpy(), ds.grad.cpu().numpy(), dp.grad.cpu().numpy())
+    e, p = errors(out["mixed"][0], out["fp64"][0], "FF")
+    assert e <= REL_L2_TOL and p <= PHASE_TOL, (e, p)
+    assert _rel(out["mixed"][1], out["fp64"][1]) <= 1e-4
+    assert _rel(out["mixed"][2], out["fp64"][2]) <= 1e-4
