@@ -368,7 +368,7 @@ __device__ __forceinline__ PairGeom pair_geom(float thx, float thy, float thz, f
     const float x = __fsub_rn(Rh, rint_magic(Rh));
     const float f2 = fmaf(res, rinv0, __fadd_rn(x, x));
     PairGeom g;
-    __sincosf(f2 * 3.14159265358979324f, &g.sn, &g.cs);
+    sincos_pi(f2, &g.sn, &g.cs);
     const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
     const float ndd = fmaf(nz, dz, fmaf(ny, dy, nx * dx));
     g.rinv = fmaf(kTangentTol32, Rh, ndd) >= 0.0f ? rinv0 : 0.0f;
@@ -668,7 +668,7 @@ po_adj_src_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__res
                              fmaf(q[0].z, r1.y, fmaf(q[0].y, r1.x, q[0].x * r0.w)))));
             const float f = __fadd_rn(__fsub_rn(Ph, rint_magic(Ph)), Pl);
             float sn, cs;
-            __sincosf(f * 6.28318530717958647f, &sn, &cs);
+            sincos_pi(f + f, &sn, &cs);
             const float ndr = fmaf(sc.n[2], r5.z, fmaf(sc.n[1], r5.y, sc.n[0] * r5.x));
             const bool lit = ndr >= -kTangentTol32;
             const cx<float> G = {lit ? cs : 0.f, lit ? (T > 0 ? -sn : sn) : 0.f};   // e^{-t j theta}

@@ -69,7 +69,7 @@ __device__ __forceinline__ void nf_pair(float *acc, const float4 &tA, const floa
     const float x = __fsub_rn(Rh, rint_magic(Rh));
     const float f2 = fmaf(res, rinv0, __fadd_rn(x, x));
     float sn, cs;
-    __sincosf(f2 * 3.14159265358979324f, &sn, &cs);
+    sincos_pi(f2, &sn, &cs);
     // Unnormalised separation and the illumination test n . d >= -tol R:
     // pairs within rounding of exact tangency count as lit (the reference
     // keeps n . R_hat == 0). An unlit pair gets 1/R = 0, which zeroes every
@@ -158,7 +158,7 @@ __device__ __forceinline__ void ff_pair(float *acc, const float4 &tA, const floa
                      fmaf(r0.z, tB.y, fmaf(r0.y, tB.x, r0.x * tA.w)))));
     const float f = __fadd_rn(__fsub_rn(Ph, rint_magic(Ph)), Pl);
     float sn, cs;
-    __sincosf(f * 6.28318530717958647f, &sn, &cs);
+    sincos_pi(f + f, &sn, &cs);
     const float ndr = fmaf(r[5].x, rr.z, fmaf(r1.w, rr.y, r0.w * rr.x));
     const bool lit = ndr >= -kTangentTol32;
     const float gc = lit ? cs : 0.0f;
@@ -198,7 +198,7 @@ __device__ __forceinline__ void sc_pair(float *acc, const float4 &tA, const floa
     const float x = __fsub_rn(Rh, rint_magic(Rh));
     const float f2 = fmaf(res, rinv, __fadd_rn(x, x));
     float sn, cs;
-    __sincosf(f2 * 3.14159265358979324f, &sn, &cs);
+    sincos_pi(f2, &sn, &cs);
     const float gr = cs * rinv;
     const float gi = (T > 0 ? -sn : sn) * rinv;
     acc[0] = fmaf(-gi, r1.w, fmaf(gr, r0.w, acc[0]));
