@@ -109,4 +109,92 @@ __device__ __forceinline__ void sincos_pi(float f2, float *s, float *c)
     *c = __uint_as_float(__float_as_uint(b) ^ (((qi + 1u) & 2u) << 30));
 }
 
+// ------------------------------------------------- packed FP32x2 arithmetic
+//
+// Blackwell's FFMA2/FADD2/FMUL2 do two FP32 operations per issued
+// instruction (the FP32 pipe rate is unchanged, the issue slots are halved).
+// Each lane rounds exactly like the scalar __f*_rn form, so error-free
+// transformations written with these stay exact.
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// 1/sqrt(x), flush-to-zero form (x = R^2 in turns^2 is never subnormal for
+// distinct points).
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// sin(pi y) = y P(y^2) and cos(pi y) = 1 + y^2 Q(y^2) on both lanes for
+// |y| <= 1/2: degree-4 P and Q (near-minimax fits, |error| < 4e-9 before
+// rounding) whose leading coefficients are carried as two floats, so that no
+// rounded pi scales the argument.
+//
+// sincos_half2: sin(pi f) and cos(pi f) up to a common sign (|f| < 2^22):
+// f = q + y with q = rint(f) and |y| <= 1/2, both exact. The true values are
+// (-1)^q times these; q's parity is the low bit of t = 1.5*2^23 + q, returned
+// for flip_parity(). With the half-turn reduction, any error of the reduced
+// sin/cos flips sign with q, so over phases spread across many turns it
+// averages out instead of adding up.
+__device__ __forceinline__ void sincos_poly2(float2 y, float2 &sn, float2 &cs)
+{
+    const float2 y2 = mul2(y, y);
+    float2 p = fma2(y2, dup2(0.07722020894289017f), dup2(-0.5980452299118042f));
+    p = fma2(y2, p, dup2(2.5500314235687256f));
+    p = fma2(y2, p, dup2(-5.1677069664001465f));
+    p = fma2(y2, p, dup2(3.141592502593994f));
+    sn = fma2(y, p, mul2(y, dup2(7.752134223437679e-08f)));
+    float2 r = fma2(y2, dup2(-0.02442070282995701f), dup2(0.23495392501354218f));
+    r = fma2(y2, r, dup2(-1.3352161645889282f));
+    r = fma2(y2, r, dup2(4.058709621429443f));
+    r = fma2(y2, r, dup2(-4.934802055358887f));
+    cs = fma2(y2, dup2(-1.0072982092879101e-07f), fma2(y2, r, dup2(1.0f)));
+}
+
+__device__ __forceinline__ void sincos_half2(float2 f, float2 &sn, float2 &cs, float2 &t)
+{
+    t = add2(f, dup2(12582912.0f));
+    const float2 q = sub2(t, dup2(12582912.0f));
+    sincos_poly2(sub2(f, q), sn, cs);
+}
+
+// a * (-1)^q per lane, with t from sincos_half2 (integer pipe, two ops a lane).
+__device__ __forceinline__ float2 flip_parity(float2 a, float2 t)
+{
+    return make_float2(__uint_as_float(__float_as_uint(a.x) ^ (__float_as_uint(t.x) << 31)),
+                       __uint_as_float(__float_as_uint(a.y) ^ (__float_as_uint(t.y) << 31)));
+}
+
+// Phase of a pair from the split separation, and its sin/cos up to (-1)^q.
+// R^2 = S0 + S1 (S0 exact, S1 small), Rh = R^2 rinv0 ~ R (turns). The
+// residual res = (S0 - Rh^2) + S1 gives R = Rh + res / (2 Rh); the fma
+// rounds S0 - Rh^2 once, an error of ~2^-47 R turns. In half turns,
+// 2R = 2 Rh + res rinv0: q = rint(2R) is taken from a rounded 2R (good to
+// +-1 near the half-way points, which only moves y to the other end of its
+// range), y = (2 Rh - q) + res rinv0 with 2 Rh - q exact (Sterbenz), so
+// |y| <= 1/2 plus a rounding for any R below 2^21 turns.
+__device__ __forceinline__ void phase_sincos2(float2 S0, float2 S1, float2 Rh, float2 rinv0, float2 &sn, float2 &cs,
+                                              float2 &t)
+{
+    const float2 res = add2(fma2(neg2(Rh), Rh, S0), S1);
+    const float2 two_r = fma2(res, rinv0, add2(Rh, Rh));
+    t = add2(two_r, dup2(12582912.0f));
+    const float2 q = sub2(t, dup2(12582912.0f));
+    const float2 y = fma2(res, rinv0, fma2(Rh, dup2(2.0f), neg2(q)));
+#if PO_MUFU_SINCOS
+    // hardware sin/cos of the exactly reduced angle pi y (|pi y| <= pi/2)
+    const float2 a = mul2(y, dup2(3.14159265358979324f));
+    __sincosf(a.x, &sn.x, &cs.x);
+    __sincosf(a.y, &sn.y, &cs.y);
+#else
+    sincos_poly2(y, sn, cs);
+#endif
+}
+
 }  // namespace po

@@ -330,6 +330,214 @@ po_main_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4
     }
 }
 
+// ------------------------------------------------ pair-packed near field
+//
+// Pair-packed source record (kRec2 float4 per pair of sources a = 2p and
+// b = 2p + 1; every float2 slot holds (value for a, value for b)):
+//   slots 0-2 hi position, 3-5 lo position, 6-8 unit normal,
+//   9-14 J' (re, im) for x, y, z, 15-20 M' likewise, 21 unused.
+// Lane x of every packed operation works on source a and lane y on source b;
+// the thread's target is duplicated into both lanes once. The algebra is the
+// one of nf_pair; the sign (-1)^q of the half-turn sin/cos reduction is folded
+// into u, and the illumination test is a per-lane select of 1/R.
+
+template <int T, bool HAS_M>
+__device__ __forceinline__ void nf_pair2(float2 *acc, const float2 *th, const float2 *tl, const float2 *r)
+{
+    const float2 dhx = sub2(th[0], r[0]), dhy = sub2(th[1], r[1]), dhz = sub2(th[2], r[2]);
+    const float2 dlx = sub2(tl[0], r[3]), dly = sub2(tl[1], r[4]), dlz = sub2(tl[2], r[5]);
+    const float2 two = dup2(2.0f);
+    const float2 S0 = fma2(dhz, dhz, fma2(dhy, dhy, mul2(dhx, dhx)));
+    const float2 S1 = fma2(dlz, fma2(two, dhz, dlz), fma2(dly, fma2(two, dhy, dly), mul2(dlx, fma2(two, dhx, dlx))));
+    const float2 R2 = add2(S0, S1);
+    const float2 rinv0 = make_float2(rsqrt_ftz(R2.x), rsqrt_ftz(R2.y));
+    const float2 Rh = mul2(R2, rinv0);
+    float2 sn, cs, tq;
+    phase_sincos2(S0, S1, Rh, rinv0, sn, cs, tq);
+    const float2 dx = add2(dhx, dlx), dy = add2(dhy, dly), dz = add2(dhz, dlz);
+    const float2 w = fma2(dup2(kTangentTol32), Rh, fma2(r[8], dz, fma2(r[7], dy, mul2(r[6], dx))));
+    const float2 rinv = make_float2(w.x >= 0.0f ? rinv0.x : 0.0f, w.y >= 0.0f ? rinv0.y : 0.0f);
+    const float2 ex = mul2(dx, rinv), ey = mul2(dy, rinv), ez = mul2(dz, rinv);
+    const float2 u = mul2(rinv, dup2(0.159154943091895336f));
+    const float2 us = flip_parity(u, tq);
+    const float2 gur = mul2(cs, us);
+    const float2 gui = mul2(T > 0 ? sn : neg2(sn), us);
+    const float2 tu = T > 0 ? u : neg2(u);
+    const float2 b = fma2(u, u, dup2(-1.0f));
+    const float2 c1r = fma2(gur, tu, mul2(neg2(gui), b));
+    const float2 c1i = fma2(gur, b, mul2(gui, tu));
+    const float2 c2r = fma2(dup2(-3.0f), c1r, add2(gui, gui));
+    const float2 c2i = fma2(dup2(-3.0f), c1i, mul2(dup2(-2.0f), gur));
+    const float2 c3r = T > 0 ? fma2(neg2(gur), u, neg2(gui)) : fma2(neg2(gur), u, gui);
+    const float2 c3i = T > 0 ? fma2(neg2(gui), u, gur) : fma2(neg2(gui), u, neg2(gur));
+
+    const float2 jxr = r[9], jxi = r[10], jyr = r[11], jyi = r[12], jzr = r[13], jzi = r[14];
+    const float2 jer = fma2(jzr, ez, fma2(jyr, ey, mul2(jxr, ex)));
+    const float2 jei = fma2(jzi, ez, fma2(jyi, ey, mul2(jxi, ex)));
+    const float2 Pr = fma2(c2r, jer, mul2(neg2(c2i), jei));
+    const float2 Pi = fma2(c2r, jei, mul2(c2i, jer));
+    acc[0] = fma2(Pr, ex, fma2(neg2(c1i), jxi, fma2(c1r, jxr, acc[0])));
+    acc[1] = fma2(Pr, ey, fma2(neg2(c1i), jyi, fma2(c1r, jyr, acc[1])));
+    acc[2] = fma2(Pr, ez, fma2(neg2(c1i), jzi, fma2(c1r, jzr, acc[2])));
+    acc[3] = fma2(Pi, ex, fma2(c1i, jxr, fma2(c1r, jxi, acc[3])));
+    acc[4] = fma2(Pi, ey, fma2(c1i, jyr, fma2(c1r, jyi, acc[4])));
+    acc[5] = fma2(Pi, ez, fma2(c1i, jzr, fma2(c1r, jzi, acc[5])));
+    const float2 kxr = fma2(c3r, jxr, mul2(neg2(c3i), jxi)), kxi = fma2(c3r, jxi, mul2(c3i, jxr));
+    const float2 kyr = fma2(c3r, jyr, mul2(neg2(c3i), jyi)), kyi = fma2(c3r, jyi, mul2(c3i, jyr));
+    const float2 kzr = fma2(c3r, jzr, mul2(neg2(c3i), jzi)), kzi = fma2(c3r, jzi, mul2(c3i, jzr));
+    acc[6] = fma2(kzr, ey, fma2(neg2(kyr), ez, acc[6]));
+    acc[7] = fma2(kxr, ez, fma2(neg2(kzr), ex, acc[7]));
+    acc[8] = fma2(kyr, ex, fma2(neg2(kxr), ey, acc[8]));
+    acc[9] = fma2(kzi, ey, fma2(neg2(kyi), ez, acc[9]));
+    acc[10] = fma2(kxi, ez, fma2(neg2(kzi), ex, acc[10]));
+    acc[11] = fma2(kyi, ex, fma2(neg2(kxi), ey, acc[11]));
+    if (HAS_M) {
+        const float2 mxr = r[15], mxi = r[16], myr = r[17], myi = r[18], mzr = r[19], mzi = r[20];
+        const float2 mer = fma2(mzr, ez, fma2(myr, ey, mul2(mxr, ex)));
+        const float2 mei = fma2(mzi, ez, fma2(myi, ey, mul2(mxi, ex)));
+        const float2 Qr = fma2(c2r, mer, mul2(neg2(c2i), mei));
+        const float2 Qi = fma2(c2r, mei, mul2(c2i, mer));
+        acc[6] = fma2(Qr, ex, fma2(neg2(c1i), mxi, fma2(c1r, mxr, acc[6])));
+        acc[7] = fma2(Qr, ey, fma2(neg2(c1i), myi, fma2(c1r, myr, acc[7])));
+        acc[8] = fma2(Qr, ez, fma2(neg2(c1i), mzi, fma2(c1r, mzr, acc[8])));
+        acc[9] = fma2(Qi, ex, fma2(c1i, mxr, fma2(c1r, mxi, acc[9])));
+        acc[10] = fma2(Qi, ey, fma2(c1i, myr, fma2(c1r, myi, acc[10])));
+        acc[11] = fma2(Qi, ez, fma2(c1i, mzr, fma2(c1r, mzi, acc[11])));
+        const float2 lxr = fma2(c3r, mxr, mul2(neg2(c3i), mxi)), lxi = fma2(c3r, mxi, mul2(c3i, mxr));
+        const float2 lyr = fma2(c3r, myr, mul2(neg2(c3i), myi)), lyi = fma2(c3r, myi, mul2(c3i, myr));
+        const float2 lzr = fma2(c3r, mzr, mul2(neg2(c3i), mzi)), lzi = fma2(c3r, mzi, mul2(c3i, mzr));
+        acc[0] = fma2(lyr, ez, fma2(neg2(lzr), ey, acc[0]));
+        acc[1] = fma2(lzr, ex, fma2(neg2(lxr), ez, acc[1]));
+        acc[2] = fma2(lxr, ey, fma2(neg2(lyr), ex, acc[2]));
+        acc[3] = fma2(lyi, ez, fma2(neg2(lzi), ey, acc[3]));
+        acc[4] = fma2(lzi, ex, fma2(neg2(lxi), ez, acc[4]));
+        acc[5] = fma2(lxi, ey, fma2(neg2(lyi), ex, acc[5]));
+    }
+}
+
+// Same grid and pipeline as po_main_kernel: blockIdx.y picks a source chunk
+// (a multiple of kTile sources, so chunks start on a pair boundary), tiles of
+// kTile/2 pair records stream through kStages TMA stages.
+template <int T, bool HAS_M, int TP>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+po_nf2_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt, long nt,
+              double *__restrict__ part, int *__restrict__ err)
+{
+    constexpr int PT = kTile / 2;                // pairs per tile
+    constexpr int NLD = HAS_M ? kRec2 : 8;       // float4 read per pair (slots 0-15 without M)
+    extern __shared__ __align__(128) float4 stage[];   // kStages * PT * kRec2
+    __shared__ __align__(8) uint64_t full[kStages];
+
+    const long tbase = (long)blockIdx.x * kThreads * TP + threadIdx.x;
+    float2 th[TP][3], tl[TP][3];
+#pragma unroll
+    for (int j = 0; j < TP; ++j) {
+        const long ti = tbase + (long)j * kThreads;
+        float4 a = make_float4(0.f, 0.f, 1.0f, 0.f), c = make_float4(0.f, 0.f, 0.f, 0.f);   // idle: R > 0
+        if (ti < nt) {
+            a = tgt[2 * ti];
+            c = tgt[2 * ti + 1];
+        }
+        th[j][0] = dup2(a.x);
+        th[j][1] = dup2(a.y);
+        th[j][2] = dup2(a.z);
+        tl[j][0] = dup2(a.w);
+        tl[j][1] = dup2(c.x);
+        tl[j][2] = dup2(c.y);
+    }
+
+    float hi[TP][kAcc];
+    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * PT * kRec2);
+#pragma unroll
+    for (int j = 0; j < TP; ++j)
+#pragma unroll
+        for (int a = 0; a < kAcc; ++a) {
+            hi[j][a] = 0.f;
+            lo[(a * TP + j) * kThreads + threadIdx.x] = 0.f;
+        }
+
+    const long s0 = (long)blockIdx.y * chunk;
+    const long s1 = min(ns, s0 + chunk);
+    const long p0 = s0 / 2, p1 = (s1 + 1) / 2;
+    const int ntiles = p1 > p0 ? (int)((p1 - p0 + PT - 1) / PT) : 0;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int it) {
+        const long first = p0 + (long)it * PT;
+        const long cnt = min((long)PT, p1 - first);
+        const uint32_t bytes = (uint32_t)(cnt * kRec2 * sizeof(float4));
+        uint64_t *bar = &full[it % kStages];
+        fence_proxy_async();
+        mbar_expect_tx(bar, bytes);
+        tma_load_1d(stage + (size_t)(it % kStages) * PT * kRec2, src + first * kRec2, bytes, bar);
+    };
+    if (threadIdx.x == 0)
+        for (int it = 0; it < ntiles && it < kStages; ++it) issue(it);
+
+    bool aborted = false;
+    for (int it = 0; it < ntiles; ++it) {
+        const bool ok = mbar_wait_bounded(&full[it % kStages], (uint32_t)((it / kStages) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicExch(err, kErrWaitTimeout);
+            aborted = true;
+            break;
+        }
+        const float4 *tile = stage + (size_t)(it % kStages) * PT * kRec2;
+        const int cnt = (int)min((long)PT, p1 - (p0 + (long)it * PT));
+        float2 acc[TP][kAcc];
+#pragma unroll
+        for (int j = 0; j < TP; ++j)
+#pragma unroll
+            for (int a = 0; a < kAcc; ++a) acc[j][a] = make_float2(0.f, 0.f);
+
+#pragma unroll 1
+        for (int s = 0; s < cnt; ++s) {
+            float2 rec[2 * NLD];
+#pragma unroll
+            for (int q = 0; q < NLD; ++q) {
+                const float4 v = tile[s * kRec2 + q];
+                rec[2 * q] = make_float2(v.x, v.y);
+                rec[2 * q + 1] = make_float2(v.z, v.w);
+            }
+#pragma unroll
+            for (int j = 0; j < TP; ++j) nf_pair2<T, HAS_M>(acc[j], th[j], tl[j], rec);
+        }
+#pragma unroll
+        for (int j = 0; j < TP; ++j)
+#pragma unroll
+            for (int a = 0; a < kAcc; ++a) {
+                float s, e;
+                two_sum(hi[j][a], __fadd_rn(acc[j][a].x, acc[j][a].y), s, e);
+                hi[j][a] = s;
+                float &l = lo[(a * TP + j) * kThreads + threadIdx.x];
+                l = __fadd_rn(l, e);
+            }
+        __syncthreads();
+        if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
+    }
+
+    if (aborted) {
+        if (threadIdx.x == 0)
+            for (int s = 0; s < kStages; ++s) (void)mbar_wait_bounded(&full[s], 0);
+        return;
+    }
+
+#pragma unroll
+    for (int j = 0; j < TP; ++j) {
+        const long ti = tbase + (long)j * kThreads;
+        if (ti >= nt) continue;
+#pragma unroll
+        for (int a = 0; a < kAcc; ++a)
+            part[((long)blockIdx.y * kAcc + a) * nt + ti] =
+                (double)hi[j][a] + (double)lo[(a * TP + j) * kThreads + threadIdx.x];
+    }
+}
+
 // ----------------------------------------------------------- frame & packing
 
 __global__ void po_bbox_kernel(const double *__restrict__ a, long na, const double *__restrict__ b, long nb,
@@ -439,6 +647,35 @@ __global__ void po_pack_src_kernel(long ns, const double *__restrict__ src7, con
     o[3] = make_float4(c[4], c[5], c[6], c[7]);
     o[4] = make_float4(c[8], c[9], c[10], c[11]);
     o[5] = make_float4((float)src7[5 * ns + i], 0.f, 0.f, 0.f);
+}
+
+// Pair-packed near-field records (layout above po_nf2_kernel). One thread per
+// lane; an odd source count pads the last pair with a copy of the last
+// source carrying zero currents.
+__global__ void po_pack_src2_kernel(long ns, const double *__restrict__ src7, const double *__restrict__ cur,
+                                    int gmode, int ncx, int ncy, const Frame *__restrict__ frp, double fac_re,
+                                    double fac_im, float *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long np = (ns + 1) / 2;
+    if (i >= 2 * np) return;
+    const long k = i < ns ? i : ns - 1;
+    const Frame fr = *frp;
+    float v[2 * kRec2];
+    for (int c = 0; c < 3; ++c) split_hi_lo((src7[c * ns + k] - fr.o[c]) * fr.kappa, fr, v[c], v[3 + c]);
+    for (int c = 0; c < 3; ++c) v[6 + c] = (float)src7[(3 + c) * ns + k];
+    const double w = i < ns ? trap_weight(k, gmode, ncx, ncy) * src7[6 * ns + k] : 0.0;
+    const double fr_ = fac_re * w, fi_ = fac_im * w;
+    for (int q = 0; q < 6; ++q) {
+        const int grp = q / 3, ax = q % 3;
+        const double re = cur[(grp * 6 + ax) * ns + k];
+        const double im = cur[(grp * 6 + 3 + ax) * ns + k];
+        v[9 + 2 * q] = (float)(fr_ * re - fi_ * im);
+        v[10 + 2 * q] = (float)(fr_ * im + fi_ * re);
+    }
+    v[21] = 0.f;
+    float *o = out + (i >> 1) * (kRec2 * 4) + (i & 1);
+    for (int q = 0; q < 2 * kRec2; ++q) o[2 * q] = v[q];
 }
 
 // Near-field / scalar targets: hi/lo split positions in the same frame.
@@ -770,6 +1007,19 @@ void *fp64_kernel(int kind)
     return reinterpret_cast<void *>(&po_fp64_kernel<kKindScalar>);
 }
 
+template <int T, bool HAS_M>
+static void *nf2_ptr()
+{
+    return reinterpret_cast<void *>(&po_nf2_kernel<T, HAS_M, kTPT2>);
+}
+
+void *nf2_kernel(int t_sign, bool has_m)
+{
+    if (t_sign < 0) return has_m ? nf2_ptr<-1, true>() : nf2_ptr<-1, false>();
+    return has_m ? nf2_ptr<1, true>() : nf2_ptr<1, false>();
+}
+
+void *pack_src2_kernel() { return reinterpret_cast<void *>(&po_pack_src2_kernel); }
 void *bbox_kernel() { return reinterpret_cast<void *>(&po_bbox_kernel); }
 void *frame_kernel() { return reinterpret_cast<void *>(&po_frame_kernel); }
 void *pack_src_kernel() { return reinterpret_cast<void *>(&po_pack_src_kernel); }
