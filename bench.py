@@ -45,8 +45,11 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Gpairs/s fwd+adjoint, mixed-prec vs FP64 sum, 1 GB300 at ≤1e-5 rel err vs FP64"
 #: algorithmic FP32 flops per pair (FMA = 2; split-precision overhead not counted)
 FWD_FLOPS = {("EH", True): 234, ("EH", False): 140, ("FF", True): 61, ("FF", False): 37}
-ADJ_SRC_FLOPS = {("EH", False): 416, ("FF", False): 99}   # currents + source displacement, M = 0 sources
-ADJ_TGT_FLOPS = {("EH", False): 245}                       # target displacement, M = 0 sources
+# Adjoint, M = 0 sources. Near field: the fused kernel (currents 12 rows, source
+# displacement 416 flops/pair, plus 62 for the target displacement sharing the
+# pair's geometry, phase, coefficients and S). Far field: currents + source
+# displacement.
+ADJ_FLOPS = {("EH", False): 478, ("FF", False): 99}
 
 
 def dist_env():
@@ -242,7 +245,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         launches_per_step = step()
     torch.cuda.synchronize()
-    kernels_per_step = 2 if far else 3
+    kernels_per_step = 2   # forward + adjoint
     engine.timing_enable(args.steps * kernels_per_step)
     sampler = ClockSampler(gpu_index(local))
     sampler.start()
@@ -357,10 +360,10 @@ def run_ours(args):
         torch.cuda.synchronize()
         peak = max(peak, blocks * 256 * iters * 16 / (p0.elapsed_time(p1) * 1e-3) / 1e12)
     mk = ("EH" if not far else "FF", not m_zero)
-    # near-field modes run the pair-packed forward kernel, the far field the one-source-per-step kernel
-    names = ["forward " + ("po_main_kernel" if far else "po_nf2_kernel"), "adjoint po_adj_src_kernel",
-             "adjoint po_adj_tgt_kernel"]
-    flops = [FWD_FLOPS[mk], ADJ_SRC_FLOPS.get((mk[0], False)), ADJ_TGT_FLOPS.get((mk[0], False))]
+    # near field: pair-packed forward and fused adjoint; far field: one-source-per-step kernels
+    names = (["forward po_main_kernel", "adjoint po_adj_src_kernel"] if far else
+             ["forward po_nf2_kernel", "adjoint po_adj_nf2_kernel"])
+    flops = [FWD_FLOPS[mk], ADJ_FLOPS.get((mk[0], False))]
     kernels = []
     for j in range(kernels_per_step):
         lm = float(launch_ms[:, j].mean())

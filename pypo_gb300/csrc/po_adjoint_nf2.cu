@@ -1,0 +1,438 @@
+// po_adjoint_nf2.cu -- fused, pair-packed near-field adjoint (mixed precision).
+//
+// One kernel computes, for every (source, target) pair, both halves of the
+// near-field adjoint of po_adjoint.cu:
+//   source side  Jbar', Mbar' (12 accumulators) and n_s . grad_d phi (1);
+//   target side  n_t . grad_d phi, summed over the sources.
+// Both displacement terms share the pair's geometry, phase, coefficients and
+// S = G (D1 alpha + D2 beta + D3 W.R_hat); only the normal differs
+// (n . grad_d phi = (1/R) Re[(R_hat.n) S + C2 (grad(beta).n) + C3 (W.n)]).
+//
+// Layout: a thread owns one source (forward-packed record, registers) and
+// streams PAIRS of targets through shared memory with TMA bulk copies; every
+// packed FP32x2 operation works on the two targets of a pair (lane x: target
+// 2p, lane y: target 2p + 1). Source-side sums stay per thread (float-float
+// totals per tile). Target-side values are transposed through shared memory
+// every kFlush target pairs, summed over the CTA's sources, and added into
+// an FP64 accumulator per target with atomicAdd (the order of those adds
+// varies from run to run: grad_dt is reproducible to ~1e-16, not bitwise).
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "po_device.cuh"
+#include "po_kernels.cuh"
+
+namespace po {
+
+// Pair-packed cotangent record, float2 slots (target 2p, target 2p + 1):
+//   0-2 hi position, 3-5 lo position (turns), 6-11 gE (re, im) x y z, 12-17 gH;
+//   with the target displacement: 18-20 n_t, 21-22 a.n_t, 23-28 n_t x b
+//   (re, im) x y z; with M as well: 29-30 b.n_t, 31-36 n_t x a
+//   (a = conj(gE), b = conj(gH)). A padding target has zero cotangent.
+__host__ __device__ constexpr int adj2_rec(bool has_m, bool want_t) { return want_t ? (has_m ? 19 : 15) : 9; }
+
+constexpr int kPairsA2 = 32;   // target pairs per shared-memory stage
+constexpr int kFlush = 16;     // target pairs per transpose of the target-side values
+static_assert(kThreadsA == 128 && kFlush == 16, "the transpose maps 128 threads onto 16 pairs x 8 segments");
+
+__global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7, const double *__restrict__ gam,
+                                        const Frame *__restrict__ frp, int rec4, float *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long np = (nt + 1) / 2;
+    if (i >= 2 * np) return;
+    const long k = i < nt ? i : nt - 1;
+    const bool real = i < nt;
+    const Frame fr = *frp;
+    float v[38];
+    for (int c = 0; c < 3; ++c) {
+        const double x = (tgt7[c * nt + k] - fr.o[c]) * fr.kappa;
+        const double hd = rint(x * fr.inv_q) * fr.q;
+        v[c] = (float)hd;
+        v[3 + c] = (float)(x - hd);
+    }
+    double ge[6], gh[6], n[3];   // (re, im) x y z
+    for (int c = 0; c < 3; ++c) {
+        ge[2 * c] = real ? gam[c * nt + k] : 0.0;
+        ge[2 * c + 1] = real ? gam[(3 + c) * nt + k] : 0.0;
+        gh[2 * c] = real ? gam[(6 + c) * nt + k] : 0.0;
+        gh[2 * c + 1] = real ? gam[(9 + c) * nt + k] : 0.0;
+        n[c] = real ? tgt7[(3 + c) * nt + k] : 0.0;
+    }
+    for (int q = 0; q < 6; ++q) {
+        v[6 + q] = (float)ge[q];
+        v[12 + q] = (float)gh[q];
+    }
+    // a = conj(gE), b = conj(gH): a.n, n x b, b.n, n x a
+    for (int w = 0; w < 2; ++w) {
+        const double *g = w == 0 ? ge : gh;
+        const double ar[3] = {g[0], g[2], g[4]}, ai[3] = {-g[1], -g[3], -g[5]};
+        const double dr = ar[0] * n[0] + ar[1] * n[1] + ar[2] * n[2];
+        const double di = ai[0] * n[0] + ai[1] * n[1] + ai[2] * n[2];
+        const double cr[3] = {n[1] * ar[2] - n[2] * ar[1], n[2] * ar[0] - n[0] * ar[2], n[0] * ar[1] - n[1] * ar[0]};
+        const double ci[3] = {n[1] * ai[2] - n[2] * ai[1], n[2] * ai[0] - n[0] * ai[2], n[0] * ai[1] - n[1] * ai[0]};
+        const int dot_at = w == 0 ? 21 : 29, cross_at = w == 0 ? 31 : 23;   // a.n, n x a | b.n, n x b
+        v[dot_at] = (float)dr;
+        v[dot_at + 1] = (float)di;
+        for (int c = 0; c < 3; ++c) {
+            v[cross_at + 2 * c] = (float)cr[c];
+            v[cross_at + 2 * c + 1] = (float)ci[c];
+        }
+    }
+    for (int c = 0; c < 3; ++c) v[18 + c] = (float)n[c];
+    v[37] = 0.f;
+    float *o = out + (i >> 1) * (long)(rec4 * 4) + (i & 1);
+    for (int q = 0; q < 2 * rec4; ++q) o[2 * q] = v[q];
+}
+
+// Per-thread constants of the thread's source (forward-packed record).
+struct SrcC {
+    float sh[3], sl[3], n[3];
+    float J[6], M[6];            // (re, im) x y z
+    float Jn[2], Mn[2];          // J.n_s, M.n_s
+    float Jxn[6], Mxn[6];        // J x n_s, M x n_s
+};
+
+// One pair of targets against the thread's source. acc: 12 current
+// accumulators + the source displacement term; vt: the two targets' terms.
+template <int T, bool HAS_M, bool WANT_D, bool WANT_T>
+__device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const float2 *r, const SrcC &s)
+{
+    const float2 dhx = sub2(r[0], dup2(s.sh[0])), dhy = sub2(r[1], dup2(s.sh[1])), dhz = sub2(r[2], dup2(s.sh[2]));
+    const float2 dlx = sub2(r[3], dup2(s.sl[0])), dly = sub2(r[4], dup2(s.sl[1])), dlz = sub2(r[5], dup2(s.sl[2]));
+    const float2 two = dup2(2.0f);
+    const float2 S0 = fma2(dhz, dhz, fma2(dhy, dhy, mul2(dhx, dhx)));
+    const float2 S1 = fma2(dlz, fma2(two, dhz, dlz), fma2(dly, fma2(two, dhy, dly), mul2(dlx, fma2(two, dhx, dlx))));
+    const float2 R2 = add2(S0, S1);
+    const float2 rinv0 = make_float2(rsqrt_ftz(R2.x), rsqrt_ftz(R2.y));
+    const float2 Rh = mul2(R2, rinv0);
+    float2 sn, cs, tq;
+    phase_sincos2(S0, S1, Rh, rinv0, sn, cs, tq);
+    cs = flip_parity(cs, tq);   // cos, sin of k R
+    sn = flip_parity(sn, tq);
+    const float2 dx = add2(dhx, dlx), dy = add2(dhy, dly), dz = add2(dhz, dlz);
+    const float2 ndd = fma2(dup2(s.n[2]), dz, fma2(dup2(s.n[1]), dy, mul2(dup2(s.n[0]), dx)));
+    const float2 w = fma2(dup2(kTangentTol32), Rh, ndd);
+    const float2 rinv = make_float2(w.x >= 0.0f ? rinv0.x : 0.0f, w.y >= 0.0f ? rinv0.y : 0.0f);
+    const float2 ex = mul2(dx, rinv), ey = mul2(dy, rinv), ez = mul2(dz, rinv);
+    const float2 u = mul2(rinv, dup2(0.159154943091895336f));
+    // c1 = Gu (t u + j(u^2 - 1)), C2 = -3 c1 - 2 j Gu, C3 = Gu (-u + j t)
+    const float2 gur = mul2(cs, u);
+    const float2 gui = mul2(T > 0 ? sn : neg2(sn), u);
+    const float2 tu = T > 0 ? u : neg2(u);
+    const float2 b = fma2(u, u, dup2(-1.0f));
+    const float2 c1r = fma2(gur, tu, mul2(neg2(gui), b));
+    const float2 c1i = fma2(gur, b, mul2(gui, tu));
+    const float2 C2r = fma2(dup2(-3.0f), c1r, add2(gui, gui));
+    const float2 C2i = fma2(dup2(-3.0f), c1i, mul2(dup2(-2.0f), gur));
+    const float2 C3r = T > 0 ? fma2(neg2(gur), u, neg2(gui)) : fma2(neg2(gur), u, gui);
+    const float2 C3i = T > 0 ? fma2(neg2(gui), u, gur) : fma2(neg2(gui), u, neg2(gur));
+
+    const float2 Exr = r[6], Exi = r[7], Eyr = r[8], Eyi = r[9], Ezr = r[10], Ezi = r[11];
+    const float2 Hxr = r[12], Hxi = r[13], Hyr = r[14], Hyi = r[15], Hzr = r[16], Hzi = r[17];
+    // gE.R_hat, gH.R_hat
+    const float2 ger = fma2(Ezr, ez, fma2(Eyr, ey, mul2(Exr, ex))), gei = fma2(Ezi, ez, fma2(Eyi, ey, mul2(Exi, ex)));
+    const float2 ghr = fma2(Hzr, ez, fma2(Hyr, ey, mul2(Hxr, ex))), ghi = fma2(Hzi, ez, fma2(Hyi, ey, mul2(Hxi, ex)));
+    // P = conj(C2) (gE.R_hat), Q = conj(C2) (gH.R_hat)
+    const float2 Pr = fma2(C2r, ger, mul2(C2i, gei)), Pi = fma2(C2r, gei, mul2(neg2(C2i), ger));
+    const float2 Qr = fma2(C2r, ghr, mul2(C2i, ghi)), Qi = fma2(C2r, ghi, mul2(neg2(C2i), ghr));
+    // K = conj(C3) gH, L = conj(C3) gE
+    const float2 Kxr = fma2(C3r, Hxr, mul2(C3i, Hxi)), Kxi = fma2(C3r, Hxi, mul2(neg2(C3i), Hxr));
+    const float2 Kyr = fma2(C3r, Hyr, mul2(C3i, Hyi)), Kyi = fma2(C3r, Hyi, mul2(neg2(C3i), Hyr));
+    const float2 Kzr = fma2(C3r, Hzr, mul2(C3i, Hzi)), Kzi = fma2(C3r, Hzi, mul2(neg2(C3i), Hzr));
+    const float2 Lxr = fma2(C3r, Exr, mul2(C3i, Exi)), Lxi = fma2(C3r, Exi, mul2(neg2(C3i), Exr));
+    const float2 Lyr = fma2(C3r, Eyr, mul2(C3i, Eyi)), Lyi = fma2(C3r, Eyi, mul2(neg2(C3i), Eyr));
+    const float2 Lzr = fma2(C3r, Ezr, mul2(C3i, Ezi)), Lzi = fma2(C3r, Ezi, mul2(neg2(C3i), Ezr));
+    // Jbar' += conj(c1) gE + P R_hat + K x R_hat
+    acc[0] = fma2(c1r, Exr, fma2(c1i, Exi, fma2(Pr, ex, fma2(Kyr, ez, fma2(neg2(Kzr), ey, acc[0])))));
+    acc[1] = fma2(c1r, Eyr, fma2(c1i, Eyi, fma2(Pr, ey, fma2(Kzr, ex, fma2(neg2(Kxr), ez, acc[1])))));
+    acc[2] = fma2(c1r, Ezr, fma2(c1i, Ezi, fma2(Pr, ez, fma2(Kxr, ey, fma2(neg2(Kyr), ex, acc[2])))));
+    acc[3] = fma2(c1r, Exi, fma2(neg2(c1i), Exr, fma2(Pi, ex, fma2(Kyi, ez, fma2(neg2(Kzi), ey, acc[3])))));
+    acc[4] = fma2(c1r, Eyi, fma2(neg2(c1i), Eyr, fma2(Pi, ey, fma2(Kzi, ex, fma2(neg2(Kxi), ez, acc[4])))));
+    acc[5] = fma2(c1r, Ezi, fma2(neg2(c1i), Ezr, fma2(Pi, ez, fma2(Kxi, ey, fma2(neg2(Kyi), ex, acc[5])))));
+    // Mbar' += conj(c1) gH + Q R_hat - L x R_hat
+    acc[6] = fma2(c1r, Hxr, fma2(c1i, Hxi, fma2(Qr, ex, fma2(neg2(Lyr), ez, fma2(Lzr, ey, acc[6])))));
+    acc[7] = fma2(c1r, Hyr, fma2(c1i, Hyi, fma2(Qr, ey, fma2(neg2(Lzr), ex, fma2(Lxr, ez, acc[7])))));
+    acc[8] = fma2(c1r, Hzr, fma2(c1i, Hzi, fma2(Qr, ez, fma2(neg2(Lxr), ey, fma2(Lyr, ex, acc[8])))));
+    acc[9] = fma2(c1r, Hxi, fma2(neg2(c1i), Hxr, fma2(Qi, ex, fma2(neg2(Lyi), ez, fma2(Lzi, ey, acc[9])))));
+    acc[10] = fma2(c1r, Hyi, fma2(neg2(c1i), Hyr, fma2(Qi, ey, fma2(neg2(Lzi), ex, fma2(Lxi, ez, acc[10])))));
+    acc[11] = fma2(c1r, Hzi, fma2(neg2(c1i), Hzr, fma2(Qi, ez, fma2(neg2(Lxi), ey, fma2(Lyi, ex, acc[11])))));
+    if (!WANT_D && !WANT_T) return;
+
+    // a = conj(gE), b = conj(gH): alpha = a.J (+ b.M), beta = (J.R_hat)(a.R_hat) (+ (M.R_hat)(b.R_hat)),
+    // w = W.R_hat = -b.(J x R_hat) (+ a.(M x R_hat))
+    const float2 Jxr = dup2(s.J[0]), Jxi = dup2(s.J[1]), Jyr = dup2(s.J[2]), Jyi = dup2(s.J[3]);
+    const float2 Jzr = dup2(s.J[4]), Jzi = dup2(s.J[5]);
+    float2 alr = fma2(Ezr, Jzr, fma2(Ezi, Jzi, fma2(Eyr, Jyr, fma2(Eyi, Jyi, fma2(Exr, Jxr, mul2(Exi, Jxi))))));
+    float2 ali = fma2(Ezr, Jzi, fma2(neg2(Ezi), Jzr, fma2(Eyr, Jyi, fma2(neg2(Eyi), Jyr, fma2(Exr, Jxi,
+                      mul2(neg2(Exi), Jxr))))));
+    const float2 jer = fma2(Jzr, ez, fma2(Jyr, ey, mul2(Jxr, ex))), jei = fma2(Jzi, ez, fma2(Jyi, ey, mul2(Jxi, ex)));
+    float2 ber = fma2(jer, ger, mul2(jei, gei)), bei = fma2(jei, ger, mul2(neg2(jer), gei));
+    const float2 xxr = fma2(Jyr, ez, mul2(neg2(Jzr), ey)), xxi = fma2(Jyi, ez, mul2(neg2(Jzi), ey));
+    const float2 xyr = fma2(Jzr, ex, mul2(neg2(Jxr), ez)), xyi = fma2(Jzi, ex, mul2(neg2(Jxi), ez));
+    const float2 xzr = fma2(Jxr, ey, mul2(neg2(Jyr), ex)), xzi = fma2(Jxi, ey, mul2(neg2(Jyi), ex));
+    float2 wr = neg2(fma2(Hzr, xzr, fma2(Hzi, xzi, fma2(Hyr, xyr, fma2(Hyi, xyi, fma2(Hxr, xxr, mul2(Hxi, xxi)))))));
+    float2 wi = neg2(fma2(Hzr, xzi, fma2(neg2(Hzi), xzr, fma2(Hyr, xyi, fma2(neg2(Hyi), xyr, fma2(Hxr, xxi,
+                     mul2(neg2(Hxi), xxr)))))));
+    float2 mer = dup2(0.f), mei = dup2(0.f);
+    if (HAS_M) {
+        const float2 Mxr = dup2(s.M[0]), Mxi = dup2(s.M[1]), Myr = dup2(s.M[2]), Myi = dup2(s.M[3]);
+        const float2 Mzr = dup2(s.M[4]), Mzi = dup2(s.M[5]);
+        alr = fma2(Hzr, Mzr, fma2(Hzi, Mzi, fma2(Hyr, Myr, fma2(Hyi, Myi, fma2(Hxr, Mxr, fma2(Hxi, Mxi, alr))))));
+        ali = fma2(Hzr, Mzi, fma2(neg2(Hzi), Mzr, fma2(Hyr, Myi, fma2(neg2(Hyi), Myr, fma2(Hxr, Mxi,
+                   fma2(neg2(Hxi), Mxr, ali))))));
+        mer = fma2(Mzr, ez, fma2(Myr, ey, mul2(Mxr, ex)));
+        mei = fma2(Mzi, ez, fma2(Myi, ey, mul2(Mxi, ex)));
+        ber = fma2(mer, ghr, fma2(mei, ghi, ber));
+        bei = fma2(mei, ghr, fma2(neg2(mer), ghi, bei));
+        const float2 yxr = fma2(Myr, ez, mul2(neg2(Mzr), ey)), yxi = fma2(Myi, ez, mul2(neg2(Mzi), ey));
+        const float2 yyr = fma2(Mzr, ex, mul2(neg2(Mxr), ez)), yyi = fma2(Mzi, ex, mul2(neg2(Mxi), ez));
+        const float2 yzr = fma2(Mxr, ey, mul2(neg2(Myr), ex)), yzi = fma2(Mxi, ey, mul2(neg2(Myi), ex));
+        wr = fma2(Ezr, yzr, fma2(Ezi, yzi, fma2(Eyr, yyr, fma2(Eyi, yyi, fma2(Exr, yxr, fma2(Exi, yxi, wr))))));
+        wi = fma2(Ezr, yzi, fma2(neg2(Ezi), yzr, fma2(Eyr, yyi, fma2(neg2(Eyi), yyr, fma2(Exr, yxi,
+                  fma2(neg2(Exi), yxr, wi))))));
+    }
+    // Re S, S = G (D1 alpha + D2 beta + D3 w), G = (cs, t sn)
+    const float2 u2 = mul2(u, u);
+    const float2 p1 = fma2(dup2(-3.0f), u2, dup2(1.0f));
+    const float2 d1r = T > 0 ? p1 : neg2(p1), d1i = mul2(u, fma2(dup2(-3.0f), u2, dup2(2.0f)));
+    const float2 p2 = fma2(dup2(-15.0f), u2, dup2(1.0f));
+    const float2 d2r = T > 0 ? neg2(p2) : p2, d2i = mul2(u, fma2(dup2(15.0f), u2, dup2(-6.0f)));
+    const float2 d3r = neg2(p1), d3i = mul2(u, dup2(T > 0 ? -3.0f : 3.0f));
+    const float2 xr = fma2(d3r, wr, fma2(neg2(d3i), wi, fma2(d2r, ber, fma2(neg2(d2i), bei, fma2(d1r, alr,
+                           mul2(neg2(d1i), ali))))));
+    const float2 xi = fma2(d3r, wi, fma2(d3i, wr, fma2(d2r, bei, fma2(d2i, ber, fma2(d1r, ali, mul2(d1i, alr))))));
+    const float2 gi = T > 0 ? sn : neg2(sn);
+    const float2 Sr = fma2(cs, xr, mul2(neg2(gi), xi));
+
+    if (WANT_D) {
+        // W.n_s = -b.(J x n_s) (+ a.(M x n_s)); grad(beta).n_s = (a.R_hat)(J.n_s) + (J.R_hat)(a.n_s) (+ M terms)
+        const float *Jxn = s.Jxn;
+        float2 wnr = neg2(fma2(Hzr, dup2(Jxn[4]), fma2(Hzi, dup2(Jxn[5]), fma2(Hyr, dup2(Jxn[2]),
+                          fma2(Hyi, dup2(Jxn[3]), fma2(Hxr, dup2(Jxn[0]), mul2(Hxi, dup2(Jxn[1]))))))));
+        float2 wni = neg2(fma2(Hzr, dup2(Jxn[5]), fma2(neg2(Hzi), dup2(Jxn[4]), fma2(Hyr, dup2(Jxn[3]),
+                          fma2(neg2(Hyi), dup2(Jxn[2]), fma2(Hxr, dup2(Jxn[1]), mul2(neg2(Hxi), dup2(Jxn[0]))))))));
+        const float2 anr = fma2(Ezr, dup2(s.n[2]), fma2(Eyr, dup2(s.n[1]), mul2(Exr, dup2(s.n[0]))));
+        const float2 ani = neg2(fma2(Ezi, dup2(s.n[2]), fma2(Eyi, dup2(s.n[1]), mul2(Exi, dup2(s.n[0])))));
+        float2 gbr = fma2(ger, dup2(s.Jn[0]), fma2(gei, dup2(s.Jn[1]), fma2(jer, anr, mul2(neg2(jei), ani))));
+        float2 gbi = fma2(ger, dup2(s.Jn[1]), fma2(neg2(gei), dup2(s.Jn[0]), fma2(jer, ani, mul2(jei, anr))));
+        if (HAS_M) {
+            const float *Mxn = s.Mxn;
+            wnr = fma2(Ezr, dup2(Mxn[4]), fma2(Ezi, dup2(Mxn[5]), fma2(Eyr, dup2(Mxn[2]), fma2(Eyi, dup2(Mxn[3]),
+                       fma2(Exr, dup2(Mxn[0]), fma2(Exi, dup2(Mxn[1]), wnr))))));
+            wni = fma2(Ezr, dup2(Mxn[5]), fma2(neg2(Ezi), dup2(Mxn[4]), fma2(Eyr, dup2(Mxn[3]),
+                       fma2(neg2(Eyi), dup2(Mxn[2]), fma2(Exr, dup2(Mxn[1]), fma2(neg2(Exi), dup2(Mxn[0]), wni))))));
+            const float2 bnr = fma2(Hzr, dup2(s.n[2]), fma2(Hyr, dup2(s.n[1]), mul2(Hxr, dup2(s.n[0]))));
+            const float2 bni = neg2(fma2(Hzi, dup2(s.n[2]), fma2(Hyi, dup2(s.n[1]), mul2(Hxi, dup2(s.n[0])))));
+            gbr = fma2(ghr, dup2(s.Mn[0]), fma2(ghi, dup2(s.Mn[1]), fma2(mer, bnr, fma2(neg2(mei), bni, gbr))));
+            gbi = fma2(ghr, dup2(s.Mn[1]), fma2(neg2(ghi), dup2(s.Mn[0]), fma2(mer, bni, fma2(mei, bnr, gbi))));
+        }
+        const float2 en = mul2(ndd, rinv);   // R_hat . n_s
+        const float2 inner = fma2(en, Sr, fma2(C2r, gbr, fma2(neg2(C2i), gbi, fma2(C3r, wnr,
+                                  mul2(neg2(C3i), wni)))));
+        acc[12] = fma2(rinv, inner, acc[12]);
+    }
+    if (WANT_T) {
+        // W.n_t = -J.(n_t x b) (+ M.(n_t x a)); grad(beta).n_t = (a.R_hat)(J.n_t) + (J.R_hat)(a.n_t) (+ M terms)
+        const float2 ntx = r[18], nty = r[19], ntz = r[20];
+        const float2 ent = fma2(ez, ntz, fma2(ey, nty, mul2(ex, ntx)));
+        const float2 jnr = fma2(Jzr, ntz, fma2(Jyr, nty, mul2(Jxr, ntx)));
+        const float2 jni = fma2(Jzi, ntz, fma2(Jyi, nty, mul2(Jxi, ntx)));
+        float2 gbr = fma2(ger, jnr, fma2(gei, jni, fma2(jer, r[21], mul2(neg2(jei), r[22]))));
+        float2 gbi = fma2(ger, jni, fma2(neg2(gei), jnr, fma2(jer, r[22], mul2(jei, r[21]))));
+        float2 wnr = neg2(fma2(Jzr, r[27], fma2(neg2(Jzi), r[28], fma2(Jyr, r[25], fma2(neg2(Jyi), r[26],
+                          fma2(Jxr, r[23], mul2(neg2(Jxi), r[24])))))));
+        float2 wni = neg2(fma2(Jzr, r[28], fma2(Jzi, r[27], fma2(Jyr, r[26], fma2(Jyi, r[25],
+                          fma2(Jxr, r[24], mul2(Jxi, r[23])))))));
+        if (HAS_M) {
+            const float2 Mxr = dup2(s.M[0]), Mxi = dup2(s.M[1]), Myr = dup2(s.M[2]), Myi = dup2(s.M[3]);
+            const float2 Mzr = dup2(s.M[4]), Mzi = dup2(s.M[5]);
+            const float2 mnr = fma2(Mzr, ntz, fma2(Myr, nty, mul2(Mxr, ntx)));
+            const float2 mni = fma2(Mzi, ntz, fma2(Myi, nty, mul2(Mxi, ntx)));
+            gbr = fma2(ghr, mnr, fma2(ghi, mni, fma2(mer, r[29], fma2(neg2(mei), r[30], gbr))));
+            gbi = fma2(ghr, mni, fma2(neg2(ghi), mnr, fma2(mer, r[30], fma2(mei, r[29], gbi))));
+            wnr = fma2(Mzr, r[35], fma2(neg2(Mzi), r[36], fma2(Myr, r[33], fma2(neg2(Myi), r[34],
+                       fma2(Mxr, r[31], fma2(neg2(Mxi), r[32], wnr))))));
+            wni = fma2(Mzr, r[36], fma2(Mzi, r[35], fma2(Myr, r[34], fma2(Myi, r[33], fma2(Mxr, r[32],
+                       fma2(Mxi, r[31], wni))))));
+        }
+        const float2 inner = fma2(ent, Sr, fma2(C2r, gbr, fma2(neg2(C2i), gbi, fma2(C3r, wnr,
+                                  mul2(neg2(C3i), wni)))));
+        vt = mul2(rinv, inner);
+    }
+}
+
+template <int T, bool HAS_M, bool WANT_D, bool WANT_T>
+__global__ void __launch_bounds__(kThreadsA, kMinBlocksA2)
+po_adj_nf2_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
+                  double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err)
+{
+    constexpr int RT = adj2_rec(HAS_M, WANT_T);
+    constexpr int NL = 2 * RT;                    // float2 slots read per pair
+    extern __shared__ __align__(128) float4 stage[];   // kStages * kPairsA2 * RT, lo, transpose buffer
+    __shared__ __align__(8) uint64_t full[kStages];
+    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * kPairsA2 * RT);
+    float2 *vbuf = reinterpret_cast<float2 *>(lo + kAccAdj * kThreadsA);   // [kFlush][kThreadsA]
+
+    const long si = (long)blockIdx.x * kThreadsA + threadIdx.x;
+    float4 q[kRec];
+#pragma unroll
+    for (int c = 0; c < kRec; ++c) q[c] = si < ns ? srcpk[(size_t)kRec * si + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (si >= ns) q[0].z = 1e3f;   // idle lanes: keep R > 0 (zero currents)
+    SrcC s;
+    s.sh[0] = q[0].x; s.sh[1] = q[0].y; s.sh[2] = q[0].z;
+    s.sl[0] = q[1].x; s.sl[1] = q[1].y; s.sl[2] = q[1].z;
+    s.n[0] = q[0].w; s.n[1] = q[1].w; s.n[2] = q[5].x;
+    const float jm[12] = {q[2].x, q[2].y, q[2].z, q[2].w, q[3].x, q[3].y, q[3].z, q[3].w, q[4].x, q[4].y, q[4].z, q[4].w};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        s.J[c] = jm[c];
+        s.M[c] = jm[6 + c];
+    }
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+        const float *v = w == 0 ? s.J : s.M;
+        float *dn = w == 0 ? s.Jn : s.Mn;
+        float *o = w == 0 ? s.Jxn : s.Mxn;
+#pragma unroll
+        for (int ri = 0; ri < 2; ++ri) {
+            dn[ri] = fmaf(v[4 + ri], s.n[2], fmaf(v[2 + ri], s.n[1], v[ri] * s.n[0]));
+            o[0 + ri] = fmaf(v[2 + ri], s.n[2], -v[4 + ri] * s.n[1]);
+            o[2 + ri] = fmaf(v[4 + ri], s.n[0], -v[0 + ri] * s.n[2]);
+            o[4 + ri] = fmaf(v[0 + ri], s.n[1], -v[2 + ri] * s.n[0]);
+        }
+    }
+
+    float hi[kAccAdj];
+#pragma unroll
+    for (int a = 0; a < kAccAdj; ++a) {
+        hi[a] = 0.f;
+        lo[a * kThreadsA + threadIdx.x] = 0.f;
+    }
+
+    const long t0 = (long)blockIdx.y * chunk;     // chunk: a multiple of 2 * kPairsA2 targets
+    const long t1 = min(nt, t0 + chunk);
+    const long p0 = t0 / 2, p1 = (t1 + 1) / 2;
+    const int ntiles = p1 > p0 ? (int)((p1 - p0 + kPairsA2 - 1) / kPairsA2) : 0;
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < kStages; ++st) mbar_init(&full[st], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int it) {
+        const long first = p0 + (long)it * kPairsA2;
+        const long cnt = min((long)kPairsA2, p1 - first);
+        const uint32_t bytes = (uint32_t)(cnt * RT * sizeof(float4));
+        uint64_t *bar = &full[it % kStages];
+        fence_proxy_async();
+        mbar_expect_tx(bar, bytes);
+        tma_load_1d(stage + (size_t)(it % kStages) * kPairsA2 * RT, trec + first * RT, bytes, bar);
+    };
+    if (threadIdx.x == 0)
+        for (int it = 0; it < ntiles && it < kStages; ++it) issue(it);
+
+    for (int it = 0; it < ntiles; ++it) {
+        const bool ok = mbar_wait_bounded(&full[it % kStages], (uint32_t)((it / kStages) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicExch(err, kErrWaitTimeout);
+                for (int st = 0; st < kStages; ++st) (void)mbar_wait_bounded(&full[st], 0);
+            }
+            return;
+        }
+        const float4 *tile = stage + (size_t)(it % kStages) * kPairsA2 * RT;
+        const long pfirst = p0 + (long)it * kPairsA2;
+        const int cnt = (int)min((long)kPairsA2, p1 - pfirst);
+        float2 acc[kAccAdj];
+#pragma unroll
+        for (int a = 0; a < kAccAdj; ++a) acc[a] = make_float2(0.f, 0.f);
+        for (int fb = 0; fb < cnt; fb += kFlush) {
+            const int fend = min(cnt, fb + kFlush);
+#pragma unroll 1
+            for (int p = fb; p < fend; ++p) {
+                float2 rec[NL];
+#pragma unroll
+                for (int c = 0; c < RT; ++c) {
+                    const float4 v = tile[p * RT + c];
+                    rec[2 * c] = make_float2(v.x, v.y);
+                    rec[2 * c + 1] = make_float2(v.z, v.w);
+                }
+                float2 vt = make_float2(0.f, 0.f);
+                adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s);
+                if (WANT_T) vbuf[(p - fb) * kThreadsA + threadIdx.x] = vt;
+            }
+            if (WANT_T) {
+                // Sum the CTA's sources for each target pair of this flush: thread
+                // (pl, k) adds 16 sources of pair pl (rotated reads: no bank
+                // conflicts), then the 8 segments combine by shuffles.
+                __syncthreads();
+                const int pl = threadIdx.x >> 3, k = threadIdx.x & 7;
+                float2 sum = make_float2(0.f, 0.f);
+                if (pl < fend - fb) {
+                    const float4 *row = reinterpret_cast<const float4 *>(vbuf + pl * kThreadsA);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const float4 v = row[8 * k + ((j + k) & 7)];
+                        sum = add2(sum, add2(make_float2(v.x, v.y), make_float2(v.z, v.w)));
+                    }
+                }
+#pragma unroll
+                for (int m = 1; m < 8; m <<= 1) {
+                    sum.x += __shfl_xor_sync(0xffffffffu, sum.x, m);
+                    sum.y += __shfl_xor_sync(0xffffffffu, sum.y, m);
+                }
+                if (k == 0 && pl < fend - fb) {
+                    const long tg = 2 * (pfirst + fb + pl);
+                    if (tg < nt) atomicAdd(&gt[tg], (double)sum.x);
+                    if (tg + 1 < nt) atomicAdd(&gt[tg + 1], (double)sum.y);
+                }
+                __syncthreads();
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < kAccAdj; ++a) {
+            float sm, e;
+            two_sum(hi[a], __fadd_rn(acc[a].x, acc[a].y), sm, e);
+            hi[a] = sm;
+            float &l = lo[a * kThreadsA + threadIdx.x];
+            l = __fadd_rn(l, e);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
+    }
+    if (si >= ns) return;
+#pragma unroll
+    for (int a = 0; a < kAccAdj; ++a)
+        part[((long)blockIdx.y * kAccAdj + a) * ns + si] = (double)hi[a] + (double)lo[a * kThreadsA + threadIdx.x];
+}
+
+int adj_nf2_smem_bytes(bool has_m, bool want_t)
+{
+    return kStages * kPairsA2 * adj2_rec(has_m, want_t) * 16 + kAccAdj * kThreadsA * 4 +
+           (want_t ? kFlush * kThreadsA * 8 : 0);
+}
+
+int adj_nf2_pairs_per_tile() { return kPairsA2; }
+
+template <int T, bool HAS_M, bool WANT_D, bool WANT_T>
+static void *adj_nf2_ptr()
+{
+    return reinterpret_cast<void *>(&po_adj_nf2_kernel<T, HAS_M, WANT_D, WANT_T>);
+}
+
+template <int T, bool HAS_M>
+static void *adj_nf2_sel(bool want_d, bool want_t)
+{
+    if (want_d) return want_t ? adj_nf2_ptr<T, HAS_M, true, true>() : adj_nf2_ptr<T, HAS_M, true, false>();
+    return want_t ? adj_nf2_ptr<T, HAS_M, false, true>() : adj_nf2_ptr<T, HAS_M, false, false>();
+}
+
+void *adj_nf2_kernel(int t_sign, bool has_m, bool want_d, bool want_t)
+{
+    if (t_sign < 0) return has_m ? adj_nf2_sel<-1, true>(want_d, want_t) : adj_nf2_sel<-1, false>(want_d, want_t);
+    return has_m ? adj_nf2_sel<1, true>(want_d, want_t) : adj_nf2_sel<1, false>(want_d, want_t);
+}
+
+void *adj_pack_tgt2_kernel() { return reinterpret_cast<void *>(&po_adj_pack_tgt2_kernel); }
+
+}  // namespace po

@@ -115,9 +115,9 @@ static int device_info(DeviceInfo *&out)
 // Number of source chunks: minimise waves * chunk length, given `slots`
 // resident CTAs, with a small cost per extra chunk (partials, prologue) and
 // the partial buffer capped near 1 GiB.
-static long choose_split(long ntb, long ns, long slots, long nt, int nacc)
+static long choose_split(long ntb, long ns, long slots, long nt, int nacc, long tile = kTile)
 {
-    const long tiles = std::max(1L, (ns + kTile - 1) / kTile);
+    const long tiles = std::max(1L, (ns + tile - 1) / tile);
     const long cap = std::max(1L, (1L << 30) / std::max(1L, nt * nacc * 8));
     long best = 1;
     double best_cost = 1e300;
@@ -457,7 +457,7 @@ int run_adjoint(const AdjArgs &a)
     float4 *srcpk = nullptr, *trec = nullptr;
     if (!rc && ((rc = salloc(&bbox, (size_t)kBboxBlocks * 6, s, owned)) || (rc = salloc(&frame, 1, s, owned)) ||
                 (rc = salloc(&srcpk, (size_t)ns * kRec, s, owned)) ||
-                (rc = salloc(&trec, (size_t)nt * kRec, s, owned)))) {
+                (far && (rc = salloc(&trec, (size_t)nt * kRec, s, owned))))) {
         sfree(owned, s);
         return rc;
     }
@@ -471,11 +471,62 @@ int run_adjoint(const AdjArgs &a)
     if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
     void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&zero_scalar, &srcpk};
     if (!rc) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
-    int farflag = far ? 1 : 0;
+    if (!far) {
+        // Fused near-field adjoint: one pass over the pairs for the currents
+        // and both displacement terms (targets streamed in pairs).
+        const bool want_t = grad_dt != nullptr;
+        const int rec4 = want_t ? (has_m ? 19 : 15) : 9;
+        const long npair = (nt + 1) / 2;
+        float *trec2 = nullptr;
+        double *gt = nullptr;
+        if (!rc && ((rc = salloc(&trec2, (size_t)npair * rec4 * 4, s, owned)) ||
+                    (want_t && (rc = salloc(&gt, (size_t)nt, s, owned))))) {
+            sfree(owned, s);
+            return rc;
+        }
+        void *p2args[] = {&nt, &tgt7, &gam, &frame, (void *)&rec4, &trec2};
+        const unsigned nblk_p = (unsigned)((2 * npair + 255) / 256);
+        if (!rc) rc = launch(adj_pack_tgt2_kernel(), dim3(nblk_p), dim3(256), p2args, 0, s);
+        if (!rc && want_t) PO_CK(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
+        void *fk = adj_nf2_kernel(ts, has_m, want_d, want_t);
+        const int smem2 = adj_nf2_smem_bytes(has_m, want_t);
+        int occ2 = 1;
+        if (!rc) {
+            PO_CK(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+            PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, fk, kThreadsA, smem2));
+            occ2 = std::max(occ2, 1);
+        }
+        const long tile_t = 2L * adj_nf2_pairs_per_tile();
+        const long nsb = (ns + kThreadsA - 1) / kThreadsA;
+        const long split = choose_split(nsb, nt, (long)di->sms * occ2, ns, kAccAdj, tile_t);
+        const long tiles = std::max(1L, (nt + tile_t - 1) / tile_t);
+        long chunk = ((tiles + split - 1) / split) * tile_t;
+        double *part = nullptr;
+        if (!rc && (rc = salloc(&part, (size_t)split * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
+        const float4 *srcc = srcpk, *trc2 = reinterpret_cast<const float4 *>(trec2);
+        void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err};
+        timing_mark(s, true);
+        if (!rc) rc = launch(fk, dim3((unsigned)nsb, (unsigned)split), dim3(kThreadsA), fargs, smem2, s);
+        timing_mark(s, false);
+        int nspl = (int)split;
+        double dsc = -kappa;
+        void *eargs[] = {(void *)&kind, &nspl, &ns, &part, &src7, &gmode, &ncx, &ncy, &fac_re, &fac_im, &dsc,
+                         &grad_cur, &grad_ds};
+        if (!rc) rc = launch(adj_src_epilogue_kernel(), dim3(nblk_s), dim3(256), eargs, 0, s);
+        if (!rc && want_t) {
+            int one = 1;
+            double dsct = kappa;
+            void *teargs[] = {&one, &nt, &gt, &dsct, &grad_dt};
+            rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
+        }
+        sfree(owned, s);
+        return rc;
+    }
+
+    // far field, source side: sources in registers, targets streamed
+    int farflag = 1;
     void *paargs[] = {&nt, &tgt7, &gam, &frame, &farflag, &trec};
     if (!rc) rc = launch(adj_pack_tgt_kernel(), dim3(nblk_t), dim3(256), paargs, 0, s);
-
-    // source side: sources in registers, targets streamed
     void *fsrc = adj_src_kernel(kind, ts, has_m, want_d);
     const int smem = kStages * kTile * kRec * 16 + kAccAdj * kThreadsA * 4;
     int occ = 1;

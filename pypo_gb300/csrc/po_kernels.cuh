@@ -55,6 +55,10 @@ constexpr uint32_t kWaitLimit = 1u << 24;   // bounded mbarrier polls
 // accumulators + 1 displacement accumulator.
 constexpr int kThreadsA = PO_THREADS_A;
 constexpr int kMinBlocksA = PO_MINB_A;
+#ifndef PO_MINB_A2
+#define PO_MINB_A2 2
+#endif
+constexpr int kMinBlocksA2 = PO_MINB_A2;   // fused near-field adjoint: resident CTAs asked of ptxas
 constexpr int kAccAdj = 13;
 
 // FP64 comparison kernel.
@@ -111,6 +115,11 @@ void *adj_tgt_fp64_kernel(int t_sign);
 void *adj_cot_kernel();
 void *adj_pack_tgt_kernel();
 void *adj_src_epilogue_kernel();
+// Fused pair-packed near-field adjoint (currents, source and target displacement).
+void *adj_nf2_kernel(int t_sign, bool has_m, bool want_d, bool want_t);
+void *adj_pack_tgt2_kernel();
+int adj_nf2_smem_bytes(bool has_m, bool want_t);
+int adj_nf2_pairs_per_tile();
 void *adj_tgt_epilogue_kernel();
 
 }  // namespace po
