@@ -171,6 +171,31 @@ __device__ __forceinline__ float2 flip_parity(float2 a, float2 t)
                        __uint_as_float(__float_as_uint(a.y) ^ (__float_as_uint(t.y) << 31)));
 }
 
+// sin(pi y), cos(pi y) for the exactly reduced |y| <= 1/2 (plus a rounding).
+__device__ __forceinline__ void sincos_reduced2(float2 y, float2 &sn, float2 &cs)
+{
+#if PO_MUFU_SINCOS
+    // hardware sin/cos of the exactly reduced angle pi y (|pi y| <= pi/2)
+    const float2 a = mul2(y, dup2(3.14159265358979324f));
+    __sincosf(a.x, &sn.x, &cs.x);
+    __sincosf(a.y, &sn.y, &cs.y);
+#else
+    sincos_poly2(y, sn, cs);
+#endif
+}
+
+// Far-field phase 2 pi (x + p) in turns, x = frac(hi projection) exact with
+// |x| <= 1/2, p the small lo projection: in half turns 2x + 2p, q = rint of
+// its rounded value, y = (2x - q) + 2p with 2x - q exact. sin/cos up to
+// (-1)^q, q's parity in t as for phase_sincos2.
+__device__ __forceinline__ void ff_phase_sincos2(float2 x, float2 p, float2 &sn, float2 &cs, float2 &t)
+{
+    const float2 two = dup2(2.0f);
+    t = add2(fma2(p, two, add2(x, x)), dup2(12582912.0f));
+    const float2 q = sub2(t, dup2(12582912.0f));
+    sincos_reduced2(fma2(p, two, fma2(x, two, neg2(q))), sn, cs);
+}
+
 // Phase of a pair from the split separation, and its sin/cos up to (-1)^q.
 // R^2 = S0 + S1 (S0 exact, S1 small), Rh = R^2 rinv0 ~ R (turns). The
 // residual res = (S0 - Rh^2) + S1 gives R = Rh + res / (2 Rh); the fma
@@ -186,15 +211,7 @@ __device__ __forceinline__ void phase_sincos2(float2 S0, float2 S1, float2 Rh, f
     const float2 two_r = fma2(res, rinv0, add2(Rh, Rh));
     t = add2(two_r, dup2(12582912.0f));
     const float2 q = sub2(t, dup2(12582912.0f));
-    const float2 y = fma2(res, rinv0, fma2(Rh, dup2(2.0f), neg2(q)));
-#if PO_MUFU_SINCOS
-    // hardware sin/cos of the exactly reduced angle pi y (|pi y| <= pi/2)
-    const float2 a = mul2(y, dup2(3.14159265358979324f));
-    __sincosf(a.x, &sn.x, &cs.x);
-    __sincosf(a.y, &sn.y, &cs.y);
-#else
-    sincos_poly2(y, sn, cs);
-#endif
+    sincos_reduced2(fma2(res, rinv0, fma2(Rh, dup2(2.0f), neg2(q))), sn, cs);
 }
 
 }  // namespace po

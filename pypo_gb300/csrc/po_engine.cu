@@ -30,7 +30,7 @@ struct DeviceInfo {
     bool ready = false;
     int sms = 0;
     int occ[3][2][2] = {};   // [kind][t>0][has_m] resident CTAs per SM
-    int occ2[2][2] = {};     // pair-packed near-field kernel, [t>0][has_m]
+    int occ2[3][2][2] = {};  // pair-packed kernels, [kind][t>0][has_m]
 };
 
 std::mutex g_mu;
@@ -97,15 +97,17 @@ static int device_info(DeviceInfo *&out)
                     PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
                     di.occ[kind][ts][hm] = std::max(nb, 1);
                 }
-        for (int ts = 0; ts < 2; ++ts)
-            for (int hm = 0; hm < 2; ++hm) {
-                void *fn = nf2_kernel(ts ? 1 : -1, hm != 0);
-                const int smem = nf2_smem_bytes();
-                PO_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-                int nb = 0;
-                PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
-                di.occ2[ts][hm] = std::max(nb, 1);
-            }
+        for (int kind = 0; kind < 3; ++kind)
+            for (int ts = 0; ts < 2; ++ts)
+                for (int hm = 0; hm < 2; ++hm) {
+                    if (kind == kKindScalar && hm) continue;
+                    void *fn = pk_kernel(kind, ts ? 1 : -1, hm != 0);
+                    const int smem = pk_smem_bytes(kind);
+                    PO_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+                    int nb = 0;
+                    PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
+                    di.occ2[kind][ts][hm] = std::max(nb, 1);
+                }
         di.ready = true;
     }
     out = &di;
@@ -305,20 +307,15 @@ int run_device(const RunArgs &a)
         return rc;
     }
 
-    // ---- mixed precision
-    // Near-field modes run the pair-packed kernel (two sources per FP32x2
-    // lane pair); far field and scalar the one-source-per-step kernel.
-    const bool packed = kind == kKindNF;
+    // ---- mixed precision: pair-packed kernels (two sources per FP32x2 lane pair)
     const bool has_m = kind != kKindScalar && !a.m_zero;
     double *bbox = nullptr;
     Frame *frame = nullptr;
     float4 *srcpk = nullptr, *tgtpk = nullptr;
     double *part = nullptr;
-    const long tpt = packed ? kTPT2 : kTPT;
-    const size_t src_f4 = packed ? (size_t)((std::max(ns, 1L) + 1) / 2) * kRec2
-                                 : (size_t)std::max(ns, 1L) * (scalar ? kRecScalar : kRec);
-    const long ntb = (nt + (long)kThreads * tpt - 1) / ((long)kThreads * tpt);
-    const int occ = packed ? di->occ2[ts > 0][has_m ? 1 : 0] : di->occ[kind][ts > 0][has_m ? 1 : 0];
+    const size_t src_f4 = (size_t)((std::max(ns, 1L) + 1) / 2) * (scalar ? kRec2Scalar : kRec2);
+    const long ntb = (nt + (long)kThreads * kTPT2 - 1) / ((long)kThreads * kTPT2);
+    const int occ = di->occ2[kind][ts > 0][has_m ? 1 : 0];
     const long nsplit = choose_split(ntb, ns, (long)di->sms * occ, nt, nacc);
     const long tiles = std::max(1L, (ns + kTile - 1) / kTile);
     long chunk = ((tiles + nsplit - 1) / nsplit) * kTile;
@@ -338,29 +335,19 @@ int run_device(const RunArgs &a)
     int centred = far ? 0 : 1;
     void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
     if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
-    if (packed) {
-        float *srcf = reinterpret_cast<float *>(srcpk);
-        void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, &srcf};
-        const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
-        if (!rc && ns > 0) rc = launch(pack_src2_kernel(), dim3(nblk_p), dim3(256), psargs, 0, s);
-    } else {
-        void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcpk};
-        if (!rc && ns > 0) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
-    }
+    float *srcf = reinterpret_cast<float *>(srcpk);
+    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcf};
+    const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
+    if (!rc && ns > 0) rc = launch(pack_src2_kernel(), dim3(nblk_p), dim3(256), psargs, 0, s);
     int farflag = far ? 1 : 0;
     void *ptargs[] = {&nt, &tgt7, &frame, &farflag, &tgtpk};
     if (!rc) rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
     const float4 *srcc = srcpk, *tgtc = tgtpk;
     void *margs[] = {&srcc, &ns, &chunk, &tgtc, &nt, &part, &err};
     timing_mark(s, true);
-    if (!rc) {
-        if (packed)
-            rc = launch(nf2_kernel(ts, has_m), dim3((unsigned)ntb, (unsigned)nsplit), dim3(kThreads), margs,
-                        nf2_smem_bytes(), s);
-        else
-            rc = launch(main_kernel(kind, ts, has_m), dim3((unsigned)ntb, (unsigned)nsplit), dim3(kThreads), margs,
-                        main_smem_bytes(kind), s);
-    }
+    if (!rc)
+        rc = launch(pk_kernel(kind, ts, has_m), dim3((unsigned)ntb, (unsigned)nsplit), dim3(kThreads), margs,
+                    pk_smem_bytes(kind), s);
     timing_mark(s, false);
     int nspl = (int)nsplit;
     double zi = zeta_inv;

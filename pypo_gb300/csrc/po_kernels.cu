@@ -415,43 +415,109 @@ __device__ __forceinline__ void nf_pair2(float2 *acc, const float2 *th, const fl
     }
 }
 
-// Same grid and pipeline as po_main_kernel: blockIdx.y picks a source chunk
-// (a multiple of kTile sources, so chunks start on a pair boundary), tiles of
-// kTile/2 pair records stream through kStages TMA stages.
-template <int T, bool HAS_M, int TP>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
-po_nf2_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt, long nt,
-              double *__restrict__ part, int *__restrict__ err)
+// Far field, pair-packed: tc = (rh xyz, rl xyz, r xyz) of the thread's
+// direction (r = rh + rl), r = the pair-packed record (slots 0-2 hi position,
+// 3-5 lo position, 6-8 normal, 9-14 J', 15-20 M').
+template <int T, bool HAS_M>
+__device__ __forceinline__ void ff_pair2(float2 *acc, const float2 *tc, const float2 *r)
 {
-    constexpr int PT = kTile / 2;                // pairs per tile
-    constexpr int NLD = HAS_M ? kRec2 : 8;       // float4 read per pair (slots 0-15 without M)
-    extern __shared__ __align__(128) float4 stage[];   // kStages * PT * kRec2
+    // r' . r_hat in turns: hi products are exact (hi parts have few bits)
+    const float2 Ph = fma2(r[2], tc[2], fma2(r[1], tc[1], mul2(r[0], tc[0])));
+    const float2 Pl = fma2(r[5], tc[8], fma2(r[4], tc[7], fma2(r[3], tc[6], fma2(r[2], tc[5],
+                      fma2(r[1], tc[4], mul2(r[0], tc[3]))))));
+    const float2 x = sub2(Ph, sub2(add2(Ph, dup2(12582912.0f)), dup2(12582912.0f)));   // frac(Ph), exact
+    float2 sn, cs, tq;
+    ff_phase_sincos2(x, Pl, sn, cs, tq);
+    const float2 ndr = fma2(r[8], tc[8], fma2(r[7], tc[7], mul2(r[6], tc[6])));
+    // G = e^{-t j theta}; (-1)^q and the illumination mask in one per-lane factor
+    const float2 one = flip_parity(dup2(1.0f), tq);
+    const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
+    const float2 gc = mul2(cs, m);
+    const float2 gs = mul2(T > 0 ? neg2(sn) : sn, m);
+    acc[0] = fma2(neg2(gs), r[10], fma2(gc, r[9], acc[0]));
+    acc[3] = fma2(gs, r[9], fma2(gc, r[10], acc[3]));
+    acc[1] = fma2(neg2(gs), r[12], fma2(gc, r[11], acc[1]));
+    acc[4] = fma2(gs, r[11], fma2(gc, r[12], acc[4]));
+    acc[2] = fma2(neg2(gs), r[14], fma2(gc, r[13], acc[2]));
+    acc[5] = fma2(gs, r[13], fma2(gc, r[14], acc[5]));
+    if (HAS_M) {
+        acc[6] = fma2(neg2(gs), r[16], fma2(gc, r[15], acc[6]));
+        acc[9] = fma2(gs, r[15], fma2(gc, r[16], acc[9]));
+        acc[7] = fma2(neg2(gs), r[18], fma2(gc, r[17], acc[7]));
+        acc[10] = fma2(gs, r[17], fma2(gc, r[18], acc[10]));
+        acc[8] = fma2(neg2(gs), r[20], fma2(gc, r[19], acc[8]));
+        acc[11] = fma2(gs, r[19], fma2(gc, r[20], acc[11]));
+    }
+}
+
+// Scalar, pair-packed: acc += S' e^{-t j k r} / r. Record slots: 0-2 hi,
+// 3-5 lo, 6-7 S' (re, im) with prefactor, weights and k/2pi folded in.
+template <int T>
+__device__ __forceinline__ void sc_pair2(float2 *acc, const float2 *tc, const float2 *r)
+{
+    const float2 dhx = sub2(tc[0], r[0]), dhy = sub2(tc[1], r[1]), dhz = sub2(tc[2], r[2]);
+    const float2 dlx = sub2(tc[3], r[3]), dly = sub2(tc[4], r[4]), dlz = sub2(tc[5], r[5]);
+    const float2 two = dup2(2.0f);
+    const float2 S0 = fma2(dhz, dhz, fma2(dhy, dhy, mul2(dhx, dhx)));
+    const float2 S1 = fma2(dlz, fma2(two, dhz, dlz), fma2(dly, fma2(two, dhy, dly), mul2(dlx, fma2(two, dhx, dlx))));
+    const float2 R2 = add2(S0, S1);
+    const float2 rinv0 = make_float2(rsqrt_ftz(R2.x), rsqrt_ftz(R2.y));
+    const float2 Rh = mul2(R2, rinv0);
+    float2 sn, cs, tq;
+    phase_sincos2(S0, S1, Rh, rinv0, sn, cs, tq);
+    const float2 rs = flip_parity(rinv0, tq);
+    const float2 gr = mul2(cs, rs);
+    const float2 gi = mul2(T > 0 ? neg2(sn) : sn, rs);
+    acc[0] = fma2(neg2(gi), r[7], fma2(gr, r[6], acc[0]));
+    acc[1] = fma2(gi, r[6], fma2(gr, r[7], acc[1]));
+}
+
+// Pair-packed main kernel of all three kinds. Same grid and pipeline as
+// po_main_kernel: blockIdx.y picks a source chunk (a multiple of kTile
+// sources, so chunks start on a pair boundary), tiles of kTile/2 pair records
+// stream through kStages TMA stages. The thread's target is duplicated into
+// both lanes once: near field and scalar (hi xyz, lo xyz), far field
+// (r_hat hi xyz, lo xyz, full xyz).
+template <int KIND, int T, bool HAS_M, int TP>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt, long nt,
+             double *__restrict__ part, int *__restrict__ err)
+{
+    constexpr int PT = kTile / 2;                                       // pairs per tile
+    constexpr int REC = KIND == kKindScalar ? kRec2Scalar : kRec2;      // float4 per pair record
+    constexpr int NLD = KIND == kKindScalar ? kRec2Scalar : (HAS_M ? kRec2 : 8);   // float4 read per pair
+    constexpr int NACC = KIND == kKindScalar ? 2 : kAcc;
+    extern __shared__ __align__(128) float4 stage[];   // kStages * PT * REC, then the compensation words
     __shared__ __align__(8) uint64_t full[kStages];
 
     const long tbase = (long)blockIdx.x * kThreads * TP + threadIdx.x;
-    float2 th[TP][3], tl[TP][3];
+    float2 tc[TP][9];
 #pragma unroll
     for (int j = 0; j < TP; ++j) {
         const long ti = tbase + (long)j * kThreads;
-        float4 a = make_float4(0.f, 0.f, 1.0f, 0.f), c = make_float4(0.f, 0.f, 0.f, 0.f);   // idle: R > 0
+        float4 a = make_float4(0.f, 0.f, KIND == kKindFF ? 0.f : 1.0f, 0.f);   // idle lanes: R > 0
+        float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
         if (ti < nt) {
             a = tgt[2 * ti];
             c = tgt[2 * ti + 1];
         }
-        th[j][0] = dup2(a.x);
-        th[j][1] = dup2(a.y);
-        th[j][2] = dup2(a.z);
-        tl[j][0] = dup2(a.w);
-        tl[j][1] = dup2(c.x);
-        tl[j][2] = dup2(c.y);
+        tc[j][0] = dup2(a.x);
+        tc[j][1] = dup2(a.y);
+        tc[j][2] = dup2(a.z);
+        tc[j][3] = dup2(a.w);
+        tc[j][4] = dup2(c.x);
+        tc[j][5] = dup2(c.y);
+        tc[j][6] = dup2(a.x + a.w);
+        tc[j][7] = dup2(a.y + c.x);
+        tc[j][8] = dup2(a.z + c.y);
     }
 
-    float hi[TP][kAcc];
-    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * PT * kRec2);
+    float hi[TP][NACC];
+    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * PT * REC);
 #pragma unroll
     for (int j = 0; j < TP; ++j)
 #pragma unroll
-        for (int a = 0; a < kAcc; ++a) {
+        for (int a = 0; a < NACC; ++a) {
             hi[j][a] = 0.f;
             lo[(a * TP + j) * kThreads + threadIdx.x] = 0.f;
         }
@@ -470,11 +536,11 @@ po_nf2_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 
     auto issue = [&](int it) {
         const long first = p0 + (long)it * PT;
         const long cnt = min((long)PT, p1 - first);
-        const uint32_t bytes = (uint32_t)(cnt * kRec2 * sizeof(float4));
+        const uint32_t bytes = (uint32_t)(cnt * REC * sizeof(float4));
         uint64_t *bar = &full[it % kStages];
         fence_proxy_async();
         mbar_expect_tx(bar, bytes);
-        tma_load_1d(stage + (size_t)(it % kStages) * PT * kRec2, src + first * kRec2, bytes, bar);
+        tma_load_1d(stage + (size_t)(it % kStages) * PT * REC, src + first * REC, bytes, bar);
     };
     if (threadIdx.x == 0)
         for (int it = 0; it < ntiles && it < kStages; ++it) issue(it);
@@ -487,30 +553,34 @@ po_nf2_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 
             aborted = true;
             break;
         }
-        const float4 *tile = stage + (size_t)(it % kStages) * PT * kRec2;
+        const float4 *tile = stage + (size_t)(it % kStages) * PT * REC;
         const int cnt = (int)min((long)PT, p1 - (p0 + (long)it * PT));
-        float2 acc[TP][kAcc];
+        float2 acc[TP][NACC];
 #pragma unroll
         for (int j = 0; j < TP; ++j)
 #pragma unroll
-            for (int a = 0; a < kAcc; ++a) acc[j][a] = make_float2(0.f, 0.f);
+            for (int a = 0; a < NACC; ++a) acc[j][a] = make_float2(0.f, 0.f);
 
 #pragma unroll 1
         for (int s = 0; s < cnt; ++s) {
             float2 rec[2 * NLD];
 #pragma unroll
             for (int q = 0; q < NLD; ++q) {
-                const float4 v = tile[s * kRec2 + q];
+                const float4 v = tile[s * REC + q];
                 rec[2 * q] = make_float2(v.x, v.y);
                 rec[2 * q + 1] = make_float2(v.z, v.w);
             }
 #pragma unroll
-            for (int j = 0; j < TP; ++j) nf_pair2<T, HAS_M>(acc[j], th[j], tl[j], rec);
+            for (int j = 0; j < TP; ++j) {
+                if (KIND == kKindNF) nf_pair2<T, HAS_M>(acc[j], tc[j], tc[j] + 3, rec);
+                else if (KIND == kKindFF) ff_pair2<T, HAS_M>(acc[j], tc[j], rec);
+                else sc_pair2<T>(acc[j], tc[j], rec);
+            }
         }
 #pragma unroll
         for (int j = 0; j < TP; ++j)
 #pragma unroll
-            for (int a = 0; a < kAcc; ++a) {
+            for (int a = 0; a < NACC; ++a) {
                 float s, e;
                 two_sum(hi[j][a], __fadd_rn(acc[j][a].x, acc[j][a].y), s, e);
                 hi[j][a] = s;
@@ -532,8 +602,8 @@ po_nf2_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 
         const long ti = tbase + (long)j * kThreads;
         if (ti >= nt) continue;
 #pragma unroll
-        for (int a = 0; a < kAcc; ++a)
-            part[((long)blockIdx.y * kAcc + a) * nt + ti] =
+        for (int a = 0; a < NACC; ++a)
+            part[((long)blockIdx.y * NACC + a) * nt + ti] =
                 (double)hi[j][a] + (double)lo[(a * TP + j) * kThreads + threadIdx.x];
     }
 }
@@ -649,12 +719,13 @@ __global__ void po_pack_src_kernel(long ns, const double *__restrict__ src7, con
     o[5] = make_float4((float)src7[5 * ns + i], 0.f, 0.f, 0.f);
 }
 
-// Pair-packed near-field records (layout above po_nf2_kernel). One thread per
-// lane; an odd source count pads the last pair with a copy of the last
-// source carrying zero currents.
+// Pair-packed source records (layouts above ff_pair2 / sc_pair2; rec4 float4
+// per pair: kRec2, or kRec2Scalar for the scalar kind). One thread per lane;
+// an odd source count pads the last pair with a copy of the last source
+// carrying zero currents.
 __global__ void po_pack_src2_kernel(long ns, const double *__restrict__ src7, const double *__restrict__ cur,
                                     int gmode, int ncx, int ncy, const Frame *__restrict__ frp, double fac_re,
-                                    double fac_im, float *__restrict__ out)
+                                    double fac_im, int scalar, float *__restrict__ out)
 {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long np = (ns + 1) / 2;
@@ -663,19 +734,26 @@ __global__ void po_pack_src2_kernel(long ns, const double *__restrict__ src7, co
     const Frame fr = *frp;
     float v[2 * kRec2];
     for (int c = 0; c < 3; ++c) split_hi_lo((src7[c * ns + k] - fr.o[c]) * fr.kappa, fr, v[c], v[3 + c]);
-    for (int c = 0; c < 3; ++c) v[6 + c] = (float)src7[(3 + c) * ns + k];
     const double w = i < ns ? trap_weight(k, gmode, ncx, ncy) * src7[6 * ns + k] : 0.0;
     const double fr_ = fac_re * w, fi_ = fac_im * w;
-    for (int q = 0; q < 6; ++q) {
-        const int grp = q / 3, ax = q % 3;
-        const double re = cur[(grp * 6 + ax) * ns + k];
-        const double im = cur[(grp * 6 + 3 + ax) * ns + k];
-        v[9 + 2 * q] = (float)(fr_ * re - fi_ * im);
-        v[10 + 2 * q] = (float)(fr_ * im + fi_ * re);
+    const int rec4 = scalar ? kRec2Scalar : kRec2;
+    if (scalar) {
+        const double re = cur[k], im = cur[ns + k];
+        v[6] = (float)(fr_ * re - fi_ * im);
+        v[7] = (float)(fr_ * im + fi_ * re);
+    } else {
+        for (int c = 0; c < 3; ++c) v[6 + c] = (float)src7[(3 + c) * ns + k];
+        for (int q = 0; q < 6; ++q) {
+            const int grp = q / 3, ax = q % 3;
+            const double re = cur[(grp * 6 + ax) * ns + k];
+            const double im = cur[(grp * 6 + 3 + ax) * ns + k];
+            v[9 + 2 * q] = (float)(fr_ * re - fi_ * im);
+            v[10 + 2 * q] = (float)(fr_ * im + fi_ * re);
+        }
+        v[21] = 0.f;
     }
-    v[21] = 0.f;
-    float *o = out + (i >> 1) * (kRec2 * 4) + (i & 1);
-    for (int q = 0; q < 2 * kRec2; ++q) o[2 * q] = v[q];
+    float *o = out + (i >> 1) * (rec4 * 4) + (i & 1);
+    for (int q = 0; q < 2 * rec4; ++q) o[2 * q] = v[q];
 }
 
 // Near-field / scalar targets: hi/lo split positions in the same frame.
@@ -1007,16 +1085,23 @@ void *fp64_kernel(int kind)
     return reinterpret_cast<void *>(&po_fp64_kernel<kKindScalar>);
 }
 
-template <int T, bool HAS_M>
-static void *nf2_ptr()
+template <int KIND, int T, bool HAS_M>
+static void *pk_ptr()
 {
-    return reinterpret_cast<void *>(&po_nf2_kernel<T, HAS_M, kTPT2>);
+    return reinterpret_cast<void *>(&po_pk_kernel<KIND, T, HAS_M, kTPT2>);
 }
 
-void *nf2_kernel(int t_sign, bool has_m)
+void *pk_kernel(int kind, int t_sign, bool has_m)
 {
-    if (t_sign < 0) return has_m ? nf2_ptr<-1, true>() : nf2_ptr<-1, false>();
-    return has_m ? nf2_ptr<1, true>() : nf2_ptr<1, false>();
+    if (kind == kKindNF) {
+        if (t_sign < 0) return has_m ? pk_ptr<kKindNF, -1, true>() : pk_ptr<kKindNF, -1, false>();
+        return has_m ? pk_ptr<kKindNF, 1, true>() : pk_ptr<kKindNF, 1, false>();
+    }
+    if (kind == kKindFF) {
+        if (t_sign < 0) return has_m ? pk_ptr<kKindFF, -1, true>() : pk_ptr<kKindFF, -1, false>();
+        return has_m ? pk_ptr<kKindFF, 1, true>() : pk_ptr<kKindFF, 1, false>();
+    }
+    return t_sign < 0 ? pk_ptr<kKindScalar, -1, false>() : pk_ptr<kKindScalar, 1, false>();
 }
 
 void *pack_src2_kernel() { return reinterpret_cast<void *>(&po_pack_src2_kernel); }

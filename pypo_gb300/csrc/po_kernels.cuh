@@ -41,7 +41,8 @@ constexpr int kStages = 3;             // TMA pipeline depth
 constexpr int kRec = 6;         // float4 per packed source record (96 B)
 constexpr int kRecScalar = 2;   // float4 per packed scalar record (32 B)
 constexpr int kAcc = 12;        // accumulators per target (E, H re/im x y z)
-constexpr int kRec2 = 11;       // float4 per pair-packed near-field record (two sources)
+constexpr int kRec2 = 11;       // float4 per pair-packed record (two sources), near and far field
+constexpr int kRec2Scalar = 4;  // float4 per pair-packed scalar record
 #ifndef PO_MUFU_SINCOS
 #define PO_MUFU_SINCOS 1         // 0: the polynomial sin/cos (accuracy comparisons)
 #endif
@@ -94,11 +95,15 @@ inline int main_smem_bytes(int kind)
     return kStages * kTile * (kind == kKindScalar ? kRecScalar : kRec) * 16 + nacc * kTPT * kThreads * 4;
 }
 
-// Pair-packed near-field kernel: stages plus the compensation words.
-inline int nf2_smem_bytes() { return kStages * (kTile / 2) * kRec2 * 16 + kAcc * kTPT2 * kThreads * 4; }
+// Pair-packed main kernel: stages plus the compensation words.
+inline int pk_smem_bytes(int kind)
+{
+    const bool sc = kind == kKindScalar;
+    return kStages * (kTile / 2) * (sc ? kRec2Scalar : kRec2) * 16 + (sc ? 2 : kAcc) * kTPT2 * kThreads * 4;
+}
 
 void *main_kernel(int kind, int t_sign, bool has_m);
-void *nf2_kernel(int t_sign, bool has_m);
+void *pk_kernel(int kind, int t_sign, bool has_m);
 void *pack_src2_kernel();
 void *fp64_kernel(int kind);
 void *bbox_kernel();
