@@ -360,9 +360,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         peak = max(peak, blocks * 256 * iters * 16 / (p0.elapsed_time(p1) * 1e-3) / 1e12)
     mk = ("EH" if not far else "FF", not m_zero)
-    # near field: pair-packed forward and fused adjoint; far field: one-source-per-step kernels
-    names = (["forward po_main_kernel", "adjoint po_adj_src_kernel"] if far else
-             ["forward po_nf2_kernel", "adjoint po_adj_nf2_kernel"])
+    # pair-packed forward and adjoint (near field: the fused adjoint)
+    names = ["forward po_pk_kernel", "adjoint po_adj_pk_kernel"]
     flops = [FWD_FLOPS[mk], ADJ_FLOPS.get((mk[0], False))]
     kernels = []
     for j in range(kernels_per_step):
@@ -391,7 +390,7 @@ def run_ours(args):
         "config": {"workload": w["name"] + ("" if args.scale == 1.0 else f" (scale {args.scale})"), "desc": w["desc"],
                    "ns": ns, "nt": nt, "pairs_per_step": w["pairs"],
                    "step": "forward + adjoint (grad wrt currents, source and target normal displacement)",
-                   "precision": "FP32 bulk (packed FP32x2 near-field forward); separation, R and phase in split hi/lo form",
+                   "precision": "FP32 bulk in packed FP32x2; separation, R and phase in split hi/lo form",
                    "l2": "flushed before every step (256 MB write inside the timed loop)",
                    "parallelism": f"replica per GPU x{world}"},
         "forward_gpairs_per_s": kernels[0]["gpairs_per_s"],

@@ -185,7 +185,7 @@ int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int nc
  * to 101 if a kernel gave up a bounded wait (NULL: an internal word).
  * The scratch is a fixed 64 MiB device array inside the library, held by
  * every GPU that loads it until the process exits; problems needing more
- * (about 96*ns + 128*nt bytes, plus 96*nt per extra source chunk) are
+ * (about 88*ns + 128*nt bytes, plus 96*nt per extra source chunk) are
  * rejected with status 5 and a message. The first call on a device looks up
  * that array's address: make it before any stream capture. All calls share
  * the array, so calls that overlap on the GPU race; the caller serialises

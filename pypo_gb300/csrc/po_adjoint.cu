@@ -26,9 +26,9 @@
 //                 dL/d delta_s = n_s . sum_t Re[-t j k G (conj(gS_J).J' + conj(gS_M).M')] r.
 // The illumination mask is piecewise constant: its derivative is dropped.
 //
-// Mixed precision: the same split hi/lo separation and phase as the forward
-// kernels, the same TMA tile pipeline, float-float totals per tile. The FP64
-// kernels are the plain comparison path.
+// This file holds the formulas in generic form, the cotangent mapping, the
+// plain FP64 adjoint kernels (the comparison path) and the epilogues. The
+// mixed-precision kernels, pair-packed, are in po_adjoint_pk.cu.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <cstdint>
@@ -85,7 +85,7 @@ __device__ __forceinline__ void ccross_r(const cx<F> *v, F x, F y, F z, cx<F> *o
 }
 
 // Forward coefficients (and radial derivatives) of one lit pair, in the
-// units of d (turns for the mixed kernels, mm for FP64): rinv = 1/R,
+// units of d (mm for the FP64 kernels): rinv = 1/R,
 // u = 1/(kR) given, G = (gc, gs) = e^{t j k R} (zero when not lit).
 template <typename F, int T>
 struct Coef {
@@ -239,528 +239,6 @@ __device__ __forceinline__ F nf_adj_tgt_algebra(F dx, F dy, F dz, F rinv, F u, F
     return sig.r * ndn + cmul(k.c2, gbn).r + cmul(k.c3, Wn).r;
 }
 
-// ------------------------------------------------------------- tile driver
-
-// Streams records [s0, s1) of `rec` (REC float4 each) through shared memory,
-// calling body(acc, record) for each and folding tile partials into hi/lo.
-// Returns false (after setting *err) if a tile wait timed out.
-// hi stays in registers; the compensation words lo live in shared memory
-// after the tile stages ([accumulator][thread]) and are touched once per tile.
-template <int REC, int NACC, class Body>
-__device__ __forceinline__ bool stream_tiles(const float4 *__restrict__ rec, long s0, long s1, float4 *stage,
-                                             uint64_t *full, float (&hi)[NACC], float *lo, int *err, Body &&body)
-{
-    const int ntiles = s1 > s0 ? (int)((s1 - s0 + kTile - 1) / kTile) : 0;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    auto issue = [&](int it) {
-        const long first = s0 + (long)it * kTile;
-        const long cnt = min((long)kTile, s1 - first);
-        const uint32_t bytes = (uint32_t)(cnt * REC * sizeof(float4));
-        uint64_t *bar = &full[it % kStages];
-        fence_proxy_async();
-        mbar_expect_tx(bar, bytes);
-        tma_load_1d(stage + (size_t)(it % kStages) * kTile * REC, rec + first * REC, bytes, bar);
-    };
-    if (threadIdx.x == 0)
-        for (int it = 0; it < ntiles && it < kStages; ++it) issue(it);
-    for (int it = 0; it < ntiles; ++it) {
-        const bool ok = mbar_wait_bounded(&full[it % kStages], (uint32_t)((it / kStages) & 1));
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) {
-                atomicExch(err, kErrWaitTimeout);
-                for (int s = 0; s < kStages; ++s) (void)mbar_wait_bounded(&full[s], 0);
-            }
-            return false;
-        }
-        const float4 *tile = stage + (size_t)(it % kStages) * kTile * REC;
-        const int cnt = (int)min((long)kTile, s1 - (s0 + (long)it * kTile));
-        float acc[NACC];
-#pragma unroll
-        for (int a = 0; a < NACC; ++a) acc[a] = 0.f;
-#pragma unroll 1
-        for (int s = 0; s < cnt; ++s) body(acc, tile + s * REC);
-#pragma unroll
-        for (int a = 0; a < NACC; ++a) {
-            float sm, e;
-            two_sum(hi[a], acc[a], sm, e);
-            hi[a] = sm;
-            float &l = lo[a * blockDim.x + threadIdx.x];
-            l = __fadd_rn(l, e);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
-    }
-    return true;
-}
-
-// Split-precision separation of the mixed kernels: from hi/lo target and
-// source positions (turns) to d, 1/R, the reduced phase (turns) and R.
-struct Sep {
-    float dx, dy, dz, rinv, Rh, f;
-};
-
-__device__ __forceinline__ Sep separation(float thx, float thy, float thz, float tlx, float tly, float tlz, float shx,
-                                          float shy, float shz, float slx, float sly, float slz)
-{
-    const float dhx = __fsub_rn(thx, shx), dhy = __fsub_rn(thy, shy), dhz = __fsub_rn(thz, shz);
-    const float dlx = __fsub_rn(tlx, slx), dly = __fsub_rn(tly, sly), dlz = __fsub_rn(tlz, slz);
-    const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
-    const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
-    const float R2 = __fadd_rn(S0, S1);
-    Sep s;
-    s.rinv = rsqrtf(R2);
-    s.Rh = __fmul_rn(R2, s.rinv);
-    const float p = __fmul_rn(s.Rh, s.Rh);
-    const float pe = fmaf(s.Rh, s.Rh, -p);
-    const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
-    const float Rl = __fmul_rn(res, __fmul_rn(0.5f, s.rinv));
-    s.f = __fadd_rn(__fsub_rn(s.Rh, rint_magic(s.Rh)), Rl);
-    s.dx = dhx + dlx;
-    s.dy = dhy + dly;
-    s.dz = dhz + dlz;
-    return s;
-}
-
-// ------------------------------------------- mixed-precision pair algebra
-//
-// The same quantities in unit-vector form, written as FMA chains. With
-// R_hat = d / R, u = 1/(kR), G = e^{t j kR}, Gu = G u and
-//   c1 = Gu (t u + j(u^2 - 1)),  C2 = -3 c1 - 2 j Gu,  C3 = Gu (-u + j t)
-// (C2 = c2' R^2, C3 = c3' R), the forward kernel is
-//   E = c1 J + C2 (J.R_hat) R_hat + C3 (M x R_hat), H = c1 M + C2 (M.R_hat) R_hat - C3 (J x R_hat)
-// and the displacement term becomes
-//   n . grad_d phi = (1/R) Re[(R_hat.n) S + C2 (grad(beta).n) + C3 (W.n)],
-//   S = G D1 alpha + G D2 beta + G D3 (W.R_hat),
-//   D1 = t(1-3u^2) + j(2u-3u^3), D2 = -t(1-15u^2) + j(-6u+15u^3), D3 = -(1-3u^2) - 3jtu,
-// with beta = (J.R_hat)(a.R_hat) + (M.R_hat)(b.R_hat) and
-// grad(beta).n = (a.R_hat)(J.n) + (J.R_hat)(a.n) + (b.R_hat)(M.n) + (M.R_hat)(b.n).
-// An unlit pair gets 1/R = 0, which zeroes the currents' coefficients and
-// the overall 1/R of the displacement term.
-
-struct PairGeom {
-    float ex, ey, ez;   // R_hat (zero when unlit)
-    float rinv;         // 1/R in turns (zero when unlit)
-    float en;           // R_hat . n_mask (the masking normal)
-    float cs, sn;       // cos / sin of k R
-    float u;
-};
-
-// d = t - s from hi/lo parts; n_mask = the normal of the illumination test.
-template <int T>
-__device__ __forceinline__ PairGeom pair_geom(float thx, float thy, float thz, float tlx, float tly, float tlz,
-                                              float shx, float shy, float shz, float slx, float sly, float slz,
-                                              float nx, float ny, float nz)
-{
-    const float dhx = __fsub_rn(thx, shx), dhy = __fsub_rn(thy, shy), dhz = __fsub_rn(thz, shz);
-    const float dlx = __fsub_rn(tlx, slx), dly = __fsub_rn(tly, sly), dlz = __fsub_rn(tlz, slz);
-    const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
-    const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
-    const float R2 = __fadd_rn(S0, S1);
-    const float rinv0 = rsqrtf(R2);
-    const float Rh = __fmul_rn(R2, rinv0);
-    const float p = __fmul_rn(Rh, Rh);
-    const float pe = fmaf(Rh, Rh, -p);
-    const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
-    const float x = __fsub_rn(Rh, rint_magic(Rh));
-    const float f2 = fmaf(res, rinv0, __fadd_rn(x, x));
-    PairGeom g;
-    sincos_pi(f2, &g.sn, &g.cs);
-    const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
-    const float ndd = fmaf(nz, dz, fmaf(ny, dy, nx * dx));
-    g.rinv = fmaf(kTangentTol32, Rh, ndd) >= 0.0f ? rinv0 : 0.0f;
-    g.ex = dx * g.rinv;
-    g.ey = dy * g.rinv;
-    g.ez = dz * g.rinv;
-    g.en = ndd * g.rinv;
-    g.u = g.rinv * 0.159154943091895336f;
-    return g;
-}
-
-struct Coefs {
-    float c1r, c1i, C2r, C2i, C3r, C3i;
-};
-
-template <int T>
-__device__ __forceinline__ Coefs pair_coefs(const PairGeom &g)
-{
-    Coefs c;
-    const float u = g.u;
-    const float gur = g.cs * u;
-    const float gui = (T > 0 ? g.sn : -g.sn) * u;
-    const float tu = T > 0 ? u : -u;
-    const float b = fmaf(u, u, -1.0f);
-    c.c1r = fmaf(gur, tu, -gui * b);
-    c.c1i = fmaf(gur, b, gui * tu);
-    c.C2r = fmaf(-3.0f, c.c1r, gui + gui);
-    c.C2i = fmaf(-3.0f, c.c1i, -(gur + gur));
-    c.C3r = T > 0 ? fmaf(-gur, u, -gui) : fmaf(-gur, u, gui);
-    c.C3i = T > 0 ? fmaf(-gui, u, gur) : fmaf(-gui, u, -gur);
-    return c;
-}
-
-// S = G D1 alpha + G D2 beta + G D3 w (all complex), G = (cs, t sn).
-template <int T>
-__device__ __forceinline__ void dterm(const PairGeom &g, float ar, float ai, float br, float bi, float wr, float wi,
-                                      float &Sr, float &Si)
-{
-    const float u = g.u, u2 = u * u;
-    const float gr = g.cs, gi = T > 0 ? g.sn : -g.sn;
-    const float p1 = fmaf(-3.0f, u2, 1.0f);                       // 1 - 3u^2
-    const float d1r = T > 0 ? p1 : -p1, d1i = u * fmaf(-3.0f, u2, 2.0f);
-    const float p2 = fmaf(-15.0f, u2, 1.0f);                      // 1 - 15u^2
-    const float d2r = T > 0 ? -p2 : p2, d2i = u * fmaf(15.0f, u2, -6.0f);
-    const float d3r = -p1, d3i = T > 0 ? -3.0f * u : 3.0f * u;
-    // X = D1 alpha + D2 beta + D3 w, then S = G X
-    const float xr = fmaf(d3r, wr, fmaf(-d3i, wi, fmaf(d2r, br, fmaf(-d2i, bi, fmaf(d1r, ar, -d1i * ai)))));
-    const float xi = fmaf(d3r, wi, fmaf(d3i, wr, fmaf(d2r, bi, fmaf(d2i, br, fmaf(d1r, ai, d1i * ar)))));
-    Sr = fmaf(gr, xr, -gi * xi);
-    Si = fmaf(gr, xi, gi * xr);
-}
-
-// Thread-constant data of one source for the source-side kernel.
-struct SrcF {
-    float shx, shy, shz, slx, sly, slz;
-    float nx, ny, nz;
-    float J[6], M[6];            // re/im interleaved x y z
-    float Jnr, Jni, Mnr, Mni;    // J.n, M.n
-    float Jxn[6], Mxn[6];        // J x n, M x n
-};
-
-// Near-field source-side pair. rec: streamed target record (kRec float4:
-// (th, -), (tl, -), (gE x, gE y), (gE z, gH x), (gH y, gH z), -).
-template <int T, bool HAS_M, bool WANT_D>
-__device__ __forceinline__ void nf_adj_src_pair(float *acc, const float4 *rec, const SrcF &s)
-{
-    const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3], r4 = rec[4];
-    const PairGeom g = pair_geom<T>(r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, s.shx, s.shy, s.shz, s.slx, s.sly, s.slz,
-                                    s.nx, s.ny, s.nz);
-    const Coefs c = pair_coefs<T>(g);
-    const float ex = g.ex, ey = g.ey, ez = g.ez;
-    const float Exr = r2.x, Exi = r2.y, Eyr = r2.z, Eyi = r2.w, Ezr = r3.x, Ezi = r3.y;
-    const float Hxr = r3.z, Hxi = r3.w, Hyr = r4.x, Hyi = r4.y, Hzr = r4.z, Hzi = r4.w;
-    // gE.R_hat, gH.R_hat
-    const float ger = fmaf(Ezr, ez, fmaf(Eyr, ey, Exr * ex)), gei = fmaf(Ezi, ez, fmaf(Eyi, ey, Exi * ex));
-    const float ghr = fmaf(Hzr, ez, fmaf(Hyr, ey, Hxr * ex)), ghi = fmaf(Hzi, ez, fmaf(Hyi, ey, Hxi * ex));
-    // P = conj(C2) (gE.R_hat), Q = conj(C2) (gH.R_hat)
-    const float Pr = fmaf(c.C2r, ger, c.C2i * gei), Pi = fmaf(c.C2r, gei, -c.C2i * ger);
-    const float Qr = fmaf(c.C2r, ghr, c.C2i * ghi), Qi = fmaf(c.C2r, ghi, -c.C2i * ghr);
-    // K = conj(C3) gH, L = conj(C3) gE
-    const float Kxr = fmaf(c.C3r, Hxr, c.C3i * Hxi), Kxi = fmaf(c.C3r, Hxi, -c.C3i * Hxr);
-    const float Kyr = fmaf(c.C3r, Hyr, c.C3i * Hyi), Kyi = fmaf(c.C3r, Hyi, -c.C3i * Hyr);
-    const float Kzr = fmaf(c.C3r, Hzr, c.C3i * Hzi), Kzi = fmaf(c.C3r, Hzi, -c.C3i * Hzr);
-    const float Lxr = fmaf(c.C3r, Exr, c.C3i * Exi), Lxi = fmaf(c.C3r, Exi, -c.C3i * Exr);
-    const float Lyr = fmaf(c.C3r, Eyr, c.C3i * Eyi), Lyi = fmaf(c.C3r, Eyi, -c.C3i * Eyr);
-    const float Lzr = fmaf(c.C3r, Ezr, c.C3i * Ezi), Lzi = fmaf(c.C3r, Ezi, -c.C3i * Ezr);
-    // Jbar' += conj(c1) gE + P R_hat + K x R_hat
-    acc[0] = fmaf(c.c1r, Exr, fmaf(c.c1i, Exi, fmaf(Pr, ex, fmaf(Kyr, ez, fmaf(-Kzr, ey, acc[0])))));
-    acc[1] = fmaf(c.c1r, Eyr, fmaf(c.c1i, Eyi, fmaf(Pr, ey, fmaf(Kzr, ex, fmaf(-Kxr, ez, acc[1])))));
-    acc[2] = fmaf(c.c1r, Ezr, fmaf(c.c1i, Ezi, fmaf(Pr, ez, fmaf(Kxr, ey, fmaf(-Kyr, ex, acc[2])))));
-    acc[3] = fmaf(c.c1r, Exi, fmaf(-c.c1i, Exr, fmaf(Pi, ex, fmaf(Kyi, ez, fmaf(-Kzi, ey, acc[3])))));
-    acc[4] = fmaf(c.c1r, Eyi, fmaf(-c.c1i, Eyr, fmaf(Pi, ey, fmaf(Kzi, ex, fmaf(-Kxi, ez, acc[4])))));
-    acc[5] = fmaf(c.c1r, Ezi, fmaf(-c.c1i, Ezr, fmaf(Pi, ez, fmaf(Kxi, ey, fmaf(-Kyi, ex, acc[5])))));
-    // Mbar' += conj(c1) gH + Q R_hat - L x R_hat
-    acc[6] = fmaf(c.c1r, Hxr, fmaf(c.c1i, Hxi, fmaf(Qr, ex, fmaf(-Lyr, ez, fmaf(Lzr, ey, acc[6])))));
-    acc[7] = fmaf(c.c1r, Hyr, fmaf(c.c1i, Hyi, fmaf(Qr, ey, fmaf(-Lzr, ex, fmaf(Lxr, ez, acc[7])))));
-    acc[8] = fmaf(c.c1r, Hzr, fmaf(c.c1i, Hzi, fmaf(Qr, ez, fmaf(-Lxr, ey, fmaf(Lyr, ex, acc[8])))));
-    acc[9] = fmaf(c.c1r, Hxi, fmaf(-c.c1i, Hxr, fmaf(Qi, ex, fmaf(-Lyi, ez, fmaf(Lzi, ey, acc[9])))));
-    acc[10] = fmaf(c.c1r, Hyi, fmaf(-c.c1i, Hyr, fmaf(Qi, ey, fmaf(-Lzi, ex, fmaf(Lxi, ez, acc[10])))));
-    acc[11] = fmaf(c.c1r, Hzi, fmaf(-c.c1i, Hzr, fmaf(Qi, ez, fmaf(-Lxi, ey, fmaf(Lyi, ex, acc[11])))));
-    if (WANT_D) {
-        // a = conj(gE), b = conj(gH); a.R_hat = conj(gE.R_hat)
-        const float* J = s.J;
-        // alpha = a.J (+ b.M)
-        float alr = fmaf(Ezr, J[4], fmaf(Ezi, J[5], fmaf(Eyr, J[2], fmaf(Eyi, J[3], fmaf(Exr, J[0], Exi * J[1])))));
-        float ali = fmaf(Ezr, J[5], fmaf(-Ezi, J[4], fmaf(Eyr, J[3], fmaf(-Eyi, J[2], fmaf(Exr, J[1], -Exi * J[0])))));
-        // J.R_hat
-        const float jer = fmaf(J[4], ez, fmaf(J[2], ey, J[0] * ex)), jei = fmaf(J[5], ez, fmaf(J[3], ey, J[1] * ex));
-        // beta = (J.R_hat)(a.R_hat), a.R_hat = (ger, -gei)
-        float ber = fmaf(jer, ger, jei * gei), bei = fmaf(jei, ger, -jer * gei);
-        // J x R_hat, then w = W.R_hat = -b.(J x R_hat) (+ a.(M x R_hat))
-        const float xxr = fmaf(J[2], ez, -J[4] * ey), xxi = fmaf(J[3], ez, -J[5] * ey);
-        const float xyr = fmaf(J[4], ex, -J[0] * ez), xyi = fmaf(J[5], ex, -J[1] * ez);
-        const float xzr = fmaf(J[0], ey, -J[2] * ex), xzi = fmaf(J[1], ey, -J[3] * ex);
-        // b.X = sum conj(gH) X:  re = gHr Xr + gHi Xi ; im = gHr Xi - gHi Xr
-        float wr = -fmaf(Hzr, xzr, fmaf(Hzi, xzi, fmaf(Hyr, xyr, fmaf(Hyi, xyi, fmaf(Hxr, xxr, Hxi * xxi)))));
-        float wi = -fmaf(Hzr, xzi, fmaf(-Hzi, xzr, fmaf(Hyr, xyi, fmaf(-Hyi, xyr, fmaf(Hxr, xxi, -Hxi * xxr)))));
-        // W.n = -b.(J x n) (+ a.(M x n))
-        const float* Jxn = s.Jxn;
-        float wnr = -fmaf(Hzr, Jxn[4], fmaf(Hzi, Jxn[5], fmaf(Hyr, Jxn[2], fmaf(Hyi, Jxn[3], fmaf(Hxr, Jxn[0], Hxi * Jxn[1])))));
-        float wni = -fmaf(Hzr, Jxn[5], fmaf(-Hzi, Jxn[4], fmaf(Hyr, Jxn[3], fmaf(-Hyi, Jxn[2], fmaf(Hxr, Jxn[1], -Hxi * Jxn[0])))));
-        // a.n
-        const float anr = fmaf(Ezr, s.nz, fmaf(Eyr, s.ny, Exr * s.nx)), ani = -fmaf(Ezi, s.nz, fmaf(Eyi, s.ny, Exi * s.nx));
-        // grad(beta).n = (a.R_hat)(J.n) + (J.R_hat)(a.n)
-        float gbr = fmaf(ger, s.Jnr, fmaf(gei, s.Jni, fmaf(jer, anr, -jei * ani)));
-        float gbi = fmaf(ger, s.Jni, fmaf(-gei, s.Jnr, fmaf(jer, ani, jei * anr)));
-        if (HAS_M) {
-            const float* M = s.M;
-            alr = fmaf(Hzr, M[4], fmaf(Hzi, M[5], fmaf(Hyr, M[2], fmaf(Hyi, M[3], fmaf(Hxr, M[0], fmaf(Hxi, M[1], alr))))));
-            ali = fmaf(Hzr, M[5], fmaf(-Hzi, M[4], fmaf(Hyr, M[3], fmaf(-Hyi, M[2], fmaf(Hxr, M[1], fmaf(-Hxi, M[0], ali))))));
-            const float mer = fmaf(M[4], ez, fmaf(M[2], ey, M[0] * ex)), mei = fmaf(M[5], ez, fmaf(M[3], ey, M[1] * ex));
-            ber = fmaf(mer, ghr, fmaf(mei, ghi, ber));
-            bei = fmaf(mei, ghr, fmaf(-mer, ghi, bei));
-            const float yxr = fmaf(M[2], ez, -M[4] * ey), yxi = fmaf(M[3], ez, -M[5] * ey);
-            const float yyr = fmaf(M[4], ex, -M[0] * ez), yyi = fmaf(M[5], ex, -M[1] * ez);
-            const float yzr = fmaf(M[0], ey, -M[2] * ex), yzi = fmaf(M[1], ey, -M[3] * ex);
-            wr = fmaf(Ezr, yzr, fmaf(Ezi, yzi, fmaf(Eyr, yyr, fmaf(Eyi, yyi, fmaf(Exr, yxr, fmaf(Exi, yxi, wr))))));
-            wi = fmaf(Ezr, yzi, fmaf(-Ezi, yzr, fmaf(Eyr, yyi, fmaf(-Eyi, yyr, fmaf(Exr, yxi, fmaf(-Exi, yxr, wi))))));
-            const float* Mxn = s.Mxn;
-            wnr = fmaf(Ezr, Mxn[4], fmaf(Ezi, Mxn[5], fmaf(Eyr, Mxn[2], fmaf(Eyi, Mxn[3], fmaf(Exr, Mxn[0], fmaf(Exi, Mxn[1], wnr))))));
-            wni = fmaf(Ezr, Mxn[5], fmaf(-Ezi, Mxn[4], fmaf(Eyr, Mxn[3], fmaf(-Eyi, Mxn[2], fmaf(Exr, Mxn[1], fmaf(-Exi, Mxn[0], wni))))));
-            const float bnr = fmaf(Hzr, s.nz, fmaf(Hyr, s.ny, Hxr * s.nx)), bni = -fmaf(Hzi, s.nz, fmaf(Hyi, s.ny, Hxi * s.nx));
-            gbr = fmaf(ghr, s.Mnr, fmaf(ghi, s.Mni, fmaf(mer, bnr, fmaf(-mei, bni, gbr))));
-            gbi = fmaf(ghr, s.Mni, fmaf(-ghi, s.Mnr, fmaf(mer, bni, fmaf(mei, bnr, gbi))));
-        }
-        float Sr, Si;
-        dterm<T>(g, alr, ali, ber, bei, wr, wi, Sr, Si);
-        const float inner = fmaf(g.en, Sr, fmaf(c.C2r, gbr, fmaf(-c.C2i, gbi, fmaf(c.C3r, wnr, -c.C3i * wni))));
-        acc[12] = fmaf(g.rinv, inner, acc[12]);
-    }
-}
-
-// Near-field target-side pair (thread = target): n_t . grad_d phi for one
-// streamed source (forward-packed record: positions, normal, J', M').
-struct TgtF {
-    float thx, thy, thz, tlx, tly, tlz;
-    float nx, ny, nz;
-    float a[6], b[6];            // conj(gE), conj(gH): re/im interleaved
-    float anr, ani, bnr, bni;    // a.n, b.n
-    float nxa[6], nxb[6];        // n x a, n x b
-};
-
-template <int T, bool HAS_M>
-__device__ __forceinline__ void nf_adj_tgt_pair(float *acc, const float4 *rec, const TgtF &t)
-{
-    const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
-    const PairGeom g = pair_geom<T>(t.thx, t.thy, t.thz, t.tlx, t.tly, t.tlz, r0.x, r0.y, r0.z, r1.x, r1.y, r1.z,
-                                    r0.w, r1.w, rec[5].x);
-    const Coefs c = pair_coefs<T>(g);
-    const float ex = g.ex, ey = g.ey, ez = g.ez;
-    const float Jxr = r2.x, Jxi = r2.y, Jyr = r2.z, Jyi = r2.w, Jzr = r3.x, Jzi = r3.y;
-    const float* a = t.a;
-    const float* b = t.b;
-    // alpha = a.J
-    float alr = fmaf(a[4], Jzr, fmaf(-a[5], Jzi, fmaf(a[2], Jyr, fmaf(-a[3], Jyi, fmaf(a[0], Jxr, -a[1] * Jxi)))));
-    float ali = fmaf(a[4], Jzi, fmaf(a[5], Jzr, fmaf(a[2], Jyi, fmaf(a[3], Jyr, fmaf(a[0], Jxi, a[1] * Jxr)))));
-    const float jer = fmaf(Jzr, ez, fmaf(Jyr, ey, Jxr * ex)), jei = fmaf(Jzi, ez, fmaf(Jyi, ey, Jxi * ex));
-    const float aer = fmaf(a[4], ez, fmaf(a[2], ey, a[0] * ex)), aei = fmaf(a[5], ez, fmaf(a[3], ey, a[1] * ex));
-    float ber = fmaf(jer, aer, -jei * aei), bei = fmaf(jer, aei, jei * aer);
-    // W.R_hat = -J.(R_hat x b) (+ M.(R_hat x a));  W.n = -J.(n x b) (+ M.(n x a))
-    const float zxr = fmaf(ey, b[4], -ez * b[2]), zxi = fmaf(ey, b[5], -ez * b[3]);
-    const float zyr = fmaf(ez, b[0], -ex * b[4]), zyi = fmaf(ez, b[1], -ex * b[5]);
-    const float zzr = fmaf(ex, b[2], -ey * b[0]), zzi = fmaf(ex, b[3], -ey * b[1]);
-    float wr = -fmaf(Jzr, zzr, fmaf(-Jzi, zzi, fmaf(Jyr, zyr, fmaf(-Jyi, zyi, fmaf(Jxr, zxr, -Jxi * zxi)))));
-    float wi = -fmaf(Jzr, zzi, fmaf(Jzi, zzr, fmaf(Jyr, zyi, fmaf(Jyi, zyr, fmaf(Jxr, zxi, Jxi * zxr)))));
-    const float* nxb = t.nxb;
-    float wnr = -fmaf(Jzr, nxb[4], fmaf(-Jzi, nxb[5], fmaf(Jyr, nxb[2], fmaf(-Jyi, nxb[3], fmaf(Jxr, nxb[0], -Jxi * nxb[1])))));
-    float wni = -fmaf(Jzr, nxb[5], fmaf(Jzi, nxb[4], fmaf(Jyr, nxb[3], fmaf(Jyi, nxb[2], fmaf(Jxr, nxb[1], Jxi * nxb[0])))));
-    const float jnr = fmaf(Jzr, t.nz, fmaf(Jyr, t.ny, Jxr * t.nx)), jni = fmaf(Jzi, t.nz, fmaf(Jyi, t.ny, Jxi * t.nx));
-    float gbr = fmaf(aer, jnr, fmaf(-aei, jni, fmaf(jer, t.anr, -jei * t.ani)));
-    float gbi = fmaf(aer, jni, fmaf(aei, jnr, fmaf(jer, t.ani, jei * t.anr)));
-    if (HAS_M) {
-        const float4 r4 = rec[4];
-        const float Mxr = r3.z, Mxi = r3.w, Myr = r4.x, Myi = r4.y, Mzr = r4.z, Mzi = r4.w;
-        alr = fmaf(b[4], Mzr, fmaf(-b[5], Mzi, fmaf(b[2], Myr, fmaf(-b[3], Myi, fmaf(b[0], Mxr, fmaf(-b[1], Mxi, alr))))));
-        ali = fmaf(b[4], Mzi, fmaf(b[5], Mzr, fmaf(b[2], Myi, fmaf(b[3], Myr, fmaf(b[0], Mxi, fmaf(b[1], Mxr, ali))))));
-        const float mer = fmaf(Mzr, ez, fmaf(Myr, ey, Mxr * ex)), mei = fmaf(Mzi, ez, fmaf(Myi, ey, Mxi * ex));
-        const float ber_ = fmaf(b[4], ez, fmaf(b[2], ey, b[0] * ex)), bei_ = fmaf(b[5], ez, fmaf(b[3], ey, b[1] * ex));
-        ber = fmaf(mer, ber_, fmaf(-mei, bei_, ber));
-        bei = fmaf(mer, bei_, fmaf(mei, ber_, bei));
-        const float vxr = fmaf(ey, a[4], -ez * a[2]), vxi = fmaf(ey, a[5], -ez * a[3]);
-        const float vyr = fmaf(ez, a[0], -ex * a[4]), vyi = fmaf(ez, a[1], -ex * a[5]);
-        const float vzr = fmaf(ex, a[2], -ey * a[0]), vzi = fmaf(ex, a[3], -ey * a[1]);
-        wr = fmaf(Mzr, vzr, fmaf(-Mzi, vzi, fmaf(Myr, vyr, fmaf(-Myi, vyi, fmaf(Mxr, vxr, fmaf(-Mxi, vxi, wr))))));
-        wi = fmaf(Mzr, vzi, fmaf(Mzi, vzr, fmaf(Myr, vyi, fmaf(Myi, vyr, fmaf(Mxr, vxi, fmaf(Mxi, vxr, wi))))));
-        const float* nxa = t.nxa;
-        wnr = fmaf(Mzr, nxa[4], fmaf(-Mzi, nxa[5], fmaf(Myr, nxa[2], fmaf(-Myi, nxa[3], fmaf(Mxr, nxa[0], fmaf(-Mxi, nxa[1], wnr))))));
-        wni = fmaf(Mzr, nxa[5], fmaf(Mzi, nxa[4], fmaf(Myr, nxa[3], fmaf(Myi, nxa[2], fmaf(Mxr, nxa[1], fmaf(Mxi, nxa[0], wni))))));
-        const float mnr = fmaf(Mzr, t.nz, fmaf(Myr, t.ny, Mxr * t.nx)), mni = fmaf(Mzi, t.nz, fmaf(Myi, t.ny, Mxi * t.nx));
-        gbr = fmaf(ber_, mnr, fmaf(-bei_, mni, fmaf(mer, t.bnr, fmaf(-mei, t.bni, gbr))));
-        gbi = fmaf(ber_, mni, fmaf(bei_, mnr, fmaf(mer, t.bni, fmaf(mei, t.bnr, gbi))));
-    }
-    float Sr, Si;
-    dterm<T>(g, alr, ali, ber, bei, wr, wi, Sr, Si);
-    // R_hat . n_t (the masking normal of this pair is the source's)
-    const float ent = fmaf(ez, t.nz, fmaf(ey, t.ny, ex * t.nx));
-    const float inner = fmaf(ent, Sr, fmaf(c.C2r, gbr, fmaf(-c.C2i, gbi, fmaf(c.C3r, wnr, -c.C3i * wni))));
-    acc[0] = fmaf(g.rinv, inner, acc[0]);
-}
-
-// ------------------------------------------------------------ mixed kernels
-
-// Source-side adjoint. Thread = one source (forward-packed record). Streams
-// the cotangent target records (kRec float4):
-//   near field: (th, 0), (tl, 0), (gEx, gEy), (gEz, gHx), (gHy, gHz), (0)
-//   far field:  (rh, rl.x), (rl.y, rl.z, 0, 0), (gSJ ...), ..., (r, 0)
-// Writes 13 accumulators per source per target chunk.
-template <int KIND, int T, bool HAS_M, bool WANT_D>
-__global__ void __launch_bounds__(kThreadsA, kMinBlocksA)
-po_adj_src_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
-                  double *__restrict__ part, int *__restrict__ err)
-{
-    constexpr int NACC = kAccAdj;
-    extern __shared__ __align__(128) float4 stage[];
-    __shared__ __align__(8) uint64_t full[kStages];
-    const long si = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    float4 q[kRec];
-#pragma unroll
-    for (int c = 0; c < kRec; ++c) q[c] = si < ns ? srcpk[(size_t)kRec * si + c] : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (si >= ns) q[0].z = 1e3f;   // idle lanes: keep R > 0
-    SrcConst<float> sc;   // far field
-    sc.n[0] = q[0].w;
-    sc.n[1] = q[1].w;
-    sc.n[2] = q[5].x;
-    sc.J[0] = {q[2].x, q[2].y};
-    sc.J[1] = {q[2].z, q[2].w};
-    sc.J[2] = {q[3].x, q[3].y};
-    sc.M[0] = {q[3].z, q[3].w};
-    sc.M[1] = {q[4].x, q[4].y};
-    sc.M[2] = {q[4].z, q[4].w};
-    SrcF sf;              // near field
-    sf.shx = q[0].x; sf.shy = q[0].y; sf.shz = q[0].z;
-    sf.slx = q[1].x; sf.sly = q[1].y; sf.slz = q[1].z;
-    sf.nx = q[0].w; sf.ny = q[1].w; sf.nz = q[5].x;
-    const float jm[12] = {q[2].x, q[2].y, q[2].z, q[2].w, q[3].x, q[3].y, q[3].z, q[3].w, q[4].x, q[4].y, q[4].z, q[4].w};
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        sf.J[c] = jm[c];
-        sf.M[c] = jm[6 + c];
-    }
-    if (WANT_D && KIND == kKindNF) {
-        sf.Jnr = fmaf(sf.J[4], sf.nz, fmaf(sf.J[2], sf.ny, sf.J[0] * sf.nx));
-        sf.Jni = fmaf(sf.J[5], sf.nz, fmaf(sf.J[3], sf.ny, sf.J[1] * sf.nx));
-        sf.Mnr = fmaf(sf.M[4], sf.nz, fmaf(sf.M[2], sf.ny, sf.M[0] * sf.nx));
-        sf.Mni = fmaf(sf.M[5], sf.nz, fmaf(sf.M[3], sf.ny, sf.M[1] * sf.nx));
-        // v x n for v = J, M (re/im interleaved)
-        for (int w = 0; w < 2; ++w) {
-            const float *v = w == 0 ? sf.J : sf.M;
-            float *o = w == 0 ? sf.Jxn : sf.Mxn;
-            for (int ri = 0; ri < 2; ++ri) {
-                o[0 + ri] = fmaf(v[2 + ri], sf.nz, -v[4 + ri] * sf.ny);
-                o[2 + ri] = fmaf(v[4 + ri], sf.nx, -v[0 + ri] * sf.nz);
-                o[4 + ri] = fmaf(v[0 + ri], sf.ny, -v[2 + ri] * sf.nx);
-            }
-        }
-    }
-    if (WANT_D && KIND == kKindFF) src_const_finish<float, HAS_M>(sc);
-    float hi[NACC];
-    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * kTile * kRec);
-#pragma unroll
-    for (int a = 0; a < NACC; ++a) {
-        hi[a] = 0.f;
-        lo[a * blockDim.x + threadIdx.x] = 0.f;
-    }
-    const long t0 = (long)blockIdx.y * chunk;
-    const long t1 = min(nt, t0 + chunk);
-    const bool ok = stream_tiles<kRec, NACC>(trec, t0, t1, stage, full, hi, lo, err, [&](float *acc, const float4 *r) {
-        const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4];
-        const cx<float> gE[3] = {{r2.x, r2.y}, {r2.z, r2.w}, {r3.x, r3.y}};
-        const cx<float> gH[3] = {{r3.z, r3.w}, {r4.x, r4.y}, {r4.z, r4.w}};
-        if (KIND == kKindNF) {
-            nf_adj_src_pair<T, HAS_M, WANT_D>(acc, r, sf);
-        } else {
-            const float4 r5 = r[5];
-            const float Ph = fmaf(q[0].z, r0.z, fmaf(q[0].y, r0.y, __fmul_rn(q[0].x, r0.x)));
-            const float Pl = fmaf(q[1].z, r5.z, fmaf(q[1].y, r5.y, fmaf(q[1].x, r5.x,
-                             fmaf(q[0].z, r1.y, fmaf(q[0].y, r1.x, q[0].x * r0.w)))));
-            const float f = __fadd_rn(__fsub_rn(Ph, rint_magic(Ph)), Pl);
-            float sn, cs;
-            sincos_pi(f + f, &sn, &cs);
-            const float ndr = fmaf(sc.n[2], r5.z, fmaf(sc.n[1], r5.y, sc.n[0] * r5.x));
-            const bool lit = ndr >= -kTangentTol32;
-            const cx<float> G = {lit ? cs : 0.f, lit ? (T > 0 ? -sn : sn) : 0.f};   // e^{-t j theta}
-            const cx<float> Gc = cconj(G);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const cx<float> jb = cmul(Gc, gE[c]), mb = cmul(Gc, gH[c]);
-                acc[c] += jb.r;
-                acc[3 + c] += jb.i;
-                acc[6 + c] += mb.r;
-                acc[9 + c] += mb.i;
-            }
-            if (WANT_D) {
-                // sigma = Re(-t j 2pi G X), X = conj(gSJ).J' + conj(gSM).M'
-                cx<float> gEc[3] = {cconj(gE[0]), cconj(gE[1]), cconj(gE[2])};
-                cx<float> X = cdot_c(gEc, sc.J);
-                if (HAS_M) {
-                    cx<float> gHc[3] = {cconj(gH[0]), cconj(gH[1]), cconj(gH[2])};
-                    X = cadd(X, cdot_c(gHc, sc.M));
-                }
-                const cx<float> Z = cmul(G, X);
-                acc[12] += (T > 0 ? 6.28318530717958647f : -6.28318530717958647f) * Z.i * ndr;
-            }
-        }
-    });
-    if (!ok || si >= ns) return;
-#pragma unroll
-    for (int a = 0; a < NACC; ++a)
-        part[((long)blockIdx.y * NACC + a) * ns + si] = (double)hi[a] + (double)lo[a * blockDim.x + threadIdx.x];
-}
-
-// Target-side displacement adjoint (near field). Thread = one target; per
-// thread a = conj(gE), b = conj(gH) from the cotangent rows; streams the
-// forward-packed source records. One accumulator: n_t . sum_s grad_d phi.
-template <int T, bool HAS_M>
-__global__ void __launch_bounds__(kThreadsA, kMinBlocksA)
-po_adj_tgt_kernel(const float4 *__restrict__ srcpk, long ns, long chunk, const float4 *__restrict__ tgtpk,
-                  const double *__restrict__ gam, const double *__restrict__ tgt7, long nt,
-                  double *__restrict__ part, int *__restrict__ err)
-{
-    extern __shared__ __align__(128) float4 stage[];
-    __shared__ __align__(8) uint64_t full[kStages];
-    const long ti = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    float4 tA = make_float4(0.f, 0.f, 1e3f, 0.f), tB = make_float4(0.f, 0.f, 0.f, 0.f);
-    float n[3] = {0.f, 0.f, 0.f};
-    cx<float> a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, b[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    if (ti < nt) {
-        tA = tgtpk[2 * ti];
-        tB = tgtpk[2 * ti + 1];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            n[c] = (float)tgt7[(3 + c) * nt + ti];
-            a[c] = {(float)gam[c * nt + ti], -(float)gam[(3 + c) * nt + ti]};
-            b[c] = {(float)gam[(6 + c) * nt + ti], -(float)gam[(9 + c) * nt + ti]};
-        }
-    }
-    TgtF tf;
-    tf.thx = tA.x; tf.thy = tA.y; tf.thz = tA.z;
-    tf.tlx = tA.w; tf.tly = tB.x; tf.tlz = tB.y;
-    tf.nx = n[0]; tf.ny = n[1]; tf.nz = n[2];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        tf.a[2 * c] = a[c].r;
-        tf.a[2 * c + 1] = a[c].i;
-        tf.b[2 * c] = b[c].r;
-        tf.b[2 * c + 1] = b[c].i;
-    }
-    tf.anr = fmaf(tf.a[4], n[2], fmaf(tf.a[2], n[1], tf.a[0] * n[0]));
-    tf.ani = fmaf(tf.a[5], n[2], fmaf(tf.a[3], n[1], tf.a[1] * n[0]));
-    tf.bnr = fmaf(tf.b[4], n[2], fmaf(tf.b[2], n[1], tf.b[0] * n[0]));
-    tf.bni = fmaf(tf.b[5], n[2], fmaf(tf.b[3], n[1], tf.b[1] * n[0]));
-    // n x v for v = a, b
-    for (int w = 0; w < 2; ++w) {
-        const float *v = w == 0 ? tf.a : tf.b;
-        float *o = w == 0 ? tf.nxa : tf.nxb;
-        for (int ri = 0; ri < 2; ++ri) {
-            o[0 + ri] = fmaf(n[1], v[4 + ri], -n[2] * v[2 + ri]);
-            o[2 + ri] = fmaf(n[2], v[0 + ri], -n[0] * v[4 + ri]);
-            o[4 + ri] = fmaf(n[0], v[2 + ri], -n[1] * v[0 + ri]);
-        }
-    }
-    float hi[1] = {0.f};
-    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * kTile * kRec);
-    lo[threadIdx.x] = 0.f;
-    const long s0 = (long)blockIdx.y * chunk;
-    const long s1 = min(ns, s0 + chunk);
-    const bool ok = stream_tiles<kRec, 1>(srcpk, s0, s1, stage, full, hi, lo, err,
-                                          [&](float *acc, const float4 *r) { nf_adj_tgt_pair<T, HAS_M>(acc, r, tf); });
-    if (!ok || ti >= nt) return;
-    part[(long)blockIdx.y * nt + ti] = (double)hi[0] + (double)lo[threadIdx.x];
-}
-
 // ------------------------------------------------------- cotangent mapping
 
 // Cotangents of the mode's output rows -> (gE, gH) per target (near field)
@@ -819,52 +297,6 @@ __global__ void po_adj_cot_kernel(int mode, long nt, const double *__restrict__ 
         gam[(long)c * nt + i] = ge[c];
         gam[(long)(6 + c) * nt + i] = gh[c];
     }
-}
-
-// Streamed cotangent records of the mixed source-side kernel (layout above).
-__global__ void po_adj_pack_tgt_kernel(long nt, const double *__restrict__ tgt7, const double *__restrict__ gam,
-                                       const Frame *__restrict__ frp, int far, float4 *__restrict__ out)
-{
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nt) return;
-    float h[3], l[3], rf[3] = {0.f, 0.f, 0.f};
-    if (far) {
-        const double th = tgt7[i], ph = tgt7[nt + i];
-        const double r[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
-        for (int c = 0; c < 3; ++c) {
-            const double hd = rint(r[c] * 2048.0) / 2048.0;
-            h[c] = (float)hd;
-            l[c] = (float)(r[c] - hd);
-            rf[c] = h[c] + l[c];
-        }
-    } else {
-        const Frame fr = *frp;
-        for (int c = 0; c < 3; ++c) {
-            const double x = (tgt7[c * nt + i] - fr.o[c]) * fr.kappa;
-            const double hd = rint(x * fr.inv_q) * fr.q;
-            h[c] = (float)hd;
-            l[c] = (float)(x - hd);
-        }
-    }
-    float g[12];
-    for (int c = 0; c < 3; ++c) {
-        g[2 * c] = (float)gam[c * nt + i];
-        g[2 * c + 1] = (float)gam[(3 + c) * nt + i];
-        g[6 + 2 * c] = (float)gam[(6 + c) * nt + i];
-        g[7 + 2 * c] = (float)gam[(9 + c) * nt + i];
-    }
-    float4 *o = out + (size_t)kRec * i;
-    if (far) {
-        o[0] = make_float4(h[0], h[1], h[2], l[0]);
-        o[1] = make_float4(l[1], l[2], 0.f, 0.f);
-    } else {
-        o[0] = make_float4(h[0], h[1], h[2], 0.f);
-        o[1] = make_float4(l[0], l[1], l[2], 0.f);
-    }
-    o[2] = make_float4(g[0], g[1], g[2], g[3]);
-    o[3] = make_float4(g[4], g[5], g[6], g[7]);
-    o[4] = make_float4(g[8], g[9], g[10], g[11]);
-    o[5] = make_float4(rf[0], rf[1], rf[2], 0.f);
 }
 
 // ------------------------------------------------------------- FP64 kernels
@@ -1055,37 +487,6 @@ __global__ void po_adj_tgt_epilogue_kernel(int nsplit, long nt, const double *__
 
 // ----------------------------------------------------------- instantiations
 
-template <int KIND, int T, bool HAS_M, bool WANT_D>
-static void *adj_src_ptr()
-{
-    return reinterpret_cast<void *>(&po_adj_src_kernel<KIND, T, HAS_M, WANT_D>);
-}
-
-void *adj_src_kernel(int kind, int t_sign, bool has_m, bool want_d)
-{
-#define PO_ADJ_SEL(K)                                                                                       \
-    if (t_sign < 0) {                                                                                       \
-        if (has_m) return want_d ? adj_src_ptr<K, -1, true, true>() : adj_src_ptr<K, -1, true, false>();    \
-        return want_d ? adj_src_ptr<K, -1, false, true>() : adj_src_ptr<K, -1, false, false>();             \
-    }                                                                                                       \
-    if (has_m) return want_d ? adj_src_ptr<K, 1, true, true>() : adj_src_ptr<K, 1, true, false>();          \
-    return want_d ? adj_src_ptr<K, 1, false, true>() : adj_src_ptr<K, 1, false, false>();
-    if (kind == kKindNF) {
-        PO_ADJ_SEL(kKindNF)
-    }
-    PO_ADJ_SEL(kKindFF)
-#undef PO_ADJ_SEL
-}
-
-void *adj_tgt_kernel(int t_sign, bool has_m)
-{
-    if (t_sign < 0)
-        return has_m ? reinterpret_cast<void *>(&po_adj_tgt_kernel<-1, true>)
-                     : reinterpret_cast<void *>(&po_adj_tgt_kernel<-1, false>);
-    return has_m ? reinterpret_cast<void *>(&po_adj_tgt_kernel<1, true>)
-                 : reinterpret_cast<void *>(&po_adj_tgt_kernel<1, false>);
-}
-
 void *adj_src_fp64_kernel(int kind, int t_sign)
 {
     if (kind == kKindNF)
@@ -1102,7 +503,6 @@ void *adj_tgt_fp64_kernel(int t_sign)
 }
 
 void *adj_cot_kernel() { return reinterpret_cast<void *>(&po_adj_cot_kernel); }
-void *adj_pack_tgt_kernel() { return reinterpret_cast<void *>(&po_adj_pack_tgt_kernel); }
 void *adj_src_epilogue_kernel() { return reinterpret_cast<void *>(&po_adj_src_epilogue_kernel); }
 void *adj_tgt_epilogue_kernel() { return reinterpret_cast<void *>(&po_adj_tgt_epilogue_kernel); }
 

@@ -1,7 +1,7 @@
-// po_adjoint_nf2.cu -- fused, pair-packed near-field adjoint (mixed precision).
+// po_adjoint_pk.cu -- pair-packed adjoint kernels (mixed precision).
 //
-// One kernel computes, for every (source, target) pair, both halves of the
-// near-field adjoint of po_adjoint.cu:
+// Near field: one fused kernel computes, for every (source, target) pair,
+// both halves of the near-field adjoint of po_adjoint.cu:
 //   source side  Jbar', Mbar' (12 accumulators) and n_s . grad_d phi (1);
 //   target side  n_t . grad_d phi, summed over the sources.
 // Both displacement terms share the pair's geometry, phase, coefficients and
@@ -16,6 +16,9 @@
 // every kFlush target pairs, summed over the CTA's sources, and added into
 // an FP64 accumulator per target with atomicAdd (the order of those adds
 // varies from run to run: grad_dt is reproducible to ~1e-16, not bitwise).
+//
+// Far field: the same kernel with the far-field pair (currents and source
+// displacement; far-field targets are directions and do not move).
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -29,14 +32,19 @@ namespace po {
 //   with the target displacement: 18-20 n_t, 21-22 a.n_t, 23-28 n_t x b
 //   (re, im) x y z; with M as well: 29-30 b.n_t, 31-36 n_t x a
 //   (a = conj(gE), b = conj(gH)). A padding target has zero cotangent.
-__host__ __device__ constexpr int adj2_rec(bool has_m, bool want_t) { return want_t ? (has_m ? 19 : 15) : 9; }
+// Far field: 0-2 r_hat hi (on 2^-11), 3-5 r_hat lo, 6-11 gS_J, 12-17 gS_M,
+//   18-20 r_hat = hi + lo (11 float4).
+__host__ __device__ constexpr int adj2_rec(int kind, bool has_m, bool want_t)
+{
+    return kind == kKindFF ? 11 : (want_t ? (has_m ? 19 : 15) : 9);
+}
 
-constexpr int kPairsA2 = 32;   // target pairs per shared-memory stage
+constexpr int kPairsA2 = PO_PAIRS_A;   // target pairs per shared-memory stage
 constexpr int kFlush = 16;     // target pairs per transpose of the target-side values
 static_assert(kThreadsA == 128 && kFlush == 16, "the transpose maps 128 threads onto 16 pairs x 8 segments");
 
 __global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7, const double *__restrict__ gam,
-                                        const Frame *__restrict__ frp, int rec4, float *__restrict__ out)
+                                        const Frame *__restrict__ frp, int far, int rec4, float *__restrict__ out)
 {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long np = (nt + 1) / 2;
@@ -45,11 +53,21 @@ __global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7
     const bool real = i < nt;
     const Frame fr = *frp;
     float v[38];
-    for (int c = 0; c < 3; ++c) {
-        const double x = (tgt7[c * nt + k] - fr.o[c]) * fr.kappa;
-        const double hd = rint(x * fr.inv_q) * fr.q;
-        v[c] = (float)hd;
-        v[3 + c] = (float)(x - hd);
+    if (far) {
+        const double th = tgt7[k], ph = tgt7[nt + k];
+        const double rd[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
+        for (int c = 0; c < 3; ++c) {
+            const double hd = rint(rd[c] * 2048.0) / 2048.0;
+            v[c] = (float)hd;
+            v[3 + c] = (float)(rd[c] - hd);
+        }
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            const double x = (tgt7[c * nt + k] - fr.o[c]) * fr.kappa;
+            const double hd = rint(x * fr.inv_q) * fr.q;
+            v[c] = (float)hd;
+            v[3 + c] = (float)(x - hd);
+        }
     }
     double ge[6], gh[6], n[3];   // (re, im) x y z
     for (int c = 0; c < 3; ++c) {
@@ -57,7 +75,7 @@ __global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7
         ge[2 * c + 1] = real ? gam[(3 + c) * nt + k] : 0.0;
         gh[2 * c] = real ? gam[(6 + c) * nt + k] : 0.0;
         gh[2 * c + 1] = real ? gam[(9 + c) * nt + k] : 0.0;
-        n[c] = real ? tgt7[(3 + c) * nt + k] : 0.0;
+        n[c] = real && !far ? tgt7[(3 + c) * nt + k] : 0.0;
     }
     for (int q = 0; q < 6; ++q) {
         v[6 + q] = (float)ge[q];
@@ -79,7 +97,7 @@ __global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7
             v[cross_at + 2 * c + 1] = (float)ci[c];
         }
     }
-    for (int c = 0; c < 3; ++c) v[18 + c] = (float)n[c];
+    for (int c = 0; c < 3; ++c) v[18 + c] = far ? v[c] + v[3 + c] : (float)n[c];
     v[37] = 0.f;
     float *o = out + (i >> 1) * (long)(rec4 * 4) + (i & 1);
     for (int q = 0; q < 2 * rec4; ++q) o[2 * q] = v[q];
@@ -262,12 +280,58 @@ __device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const floa
     }
 }
 
-template <int T, bool HAS_M, bool WANT_D, bool WANT_T>
-__global__ void __launch_bounds__(kThreadsA, kMinBlocksA2)
-po_adj_nf2_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
-                  double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err)
+// Far-field pair of targets against the thread's source:
+//   Jbar' += conj(G) gS_J, Mbar' += conj(G) gS_M (G = e^{-t j k r'.r_hat}),
+//   source displacement: Re[-t j k G (conj(gS_J).J' + conj(gS_M).M')] (n_s . r_hat),
+// k in turns is 2 pi.
+template <int T, bool HAS_M, bool WANT_D>
+__device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const SrcC &s)
 {
-    constexpr int RT = adj2_rec(HAS_M, WANT_T);
+    const float2 Ph = fma2(dup2(s.sh[2]), r[2], fma2(dup2(s.sh[1]), r[1], mul2(dup2(s.sh[0]), r[0])));
+    const float2 Pl = fma2(dup2(s.sl[2]), r[20], fma2(dup2(s.sl[1]), r[19], fma2(dup2(s.sl[0]), r[18],
+                      fma2(dup2(s.sh[2]), r[5], fma2(dup2(s.sh[1]), r[4], mul2(dup2(s.sh[0]), r[3]))))));
+    const float2 x = sub2(Ph, sub2(add2(Ph, dup2(12582912.0f)), dup2(12582912.0f)));   // frac(Ph), exact
+    float2 sn, cs, tq;
+    ff_phase_sincos2(x, Pl, sn, cs, tq);
+    const float2 ndr = fma2(dup2(s.n[2]), r[20], fma2(dup2(s.n[1]), r[19], mul2(dup2(s.n[0]), r[18])));
+    const float2 one = flip_parity(dup2(1.0f), tq);
+    const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
+    const float2 gc = mul2(cs, m);                          // G = (gc, gs)
+    const float2 gs = mul2(T > 0 ? neg2(sn) : sn, m);
+    // conj(G) g = (gc g.re + gs g.im, gc g.im - gs g.re)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        acc[c] = fma2(gs, r[7 + 2 * c], fma2(gc, r[6 + 2 * c], acc[c]));
+        acc[3 + c] = fma2(neg2(gs), r[6 + 2 * c], fma2(gc, r[7 + 2 * c], acc[3 + c]));
+        acc[6 + c] = fma2(gs, r[13 + 2 * c], fma2(gc, r[12 + 2 * c], acc[6 + c]));
+        acc[9 + c] = fma2(neg2(gs), r[12 + 2 * c], fma2(gc, r[13 + 2 * c], acc[9 + c]));
+    }
+    if (WANT_D) {
+        // X = conj(gS_J).J' (+ conj(gS_M).M'); Z = G X, Im Z = gc X.im + gs X.re
+        float2 xr = dup2(0.f), xi = dup2(0.f);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2 jr = dup2(s.J[2 * c]), ji = dup2(s.J[2 * c + 1]);
+            xr = fma2(r[6 + 2 * c], jr, fma2(r[7 + 2 * c], ji, xr));
+            xi = fma2(r[6 + 2 * c], ji, fma2(neg2(r[7 + 2 * c]), jr, xi));
+            if (HAS_M) {
+                const float2 mr = dup2(s.M[2 * c]), mi = dup2(s.M[2 * c + 1]);
+                xr = fma2(r[12 + 2 * c], mr, fma2(r[13 + 2 * c], mi, xr));
+                xi = fma2(r[12 + 2 * c], mi, fma2(neg2(r[13 + 2 * c]), mr, xi));
+            }
+        }
+        const float2 zi = fma2(gc, xi, mul2(gs, xr));
+        acc[12] = fma2(mul2(zi, ndr), dup2(T > 0 ? 6.28318530717958647f : -6.28318530717958647f), acc[12]);
+    }
+}
+
+template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
+__global__ void __launch_bounds__(kThreadsA, kMinBlocksA2)
+po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
+                 double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err)
+{
+    static_assert(KIND == kKindNF || !WANT_T, "far-field targets do not move");
+    constexpr int RT = adj2_rec(KIND, HAS_M, WANT_T);
     constexpr int NL = 2 * RT;                    // float2 slots read per pair
     extern __shared__ __align__(128) float4 stage[];   // kStages * kPairsA2 * RT, lo, transpose buffer
     __shared__ __align__(8) uint64_t full[kStages];
@@ -358,7 +422,8 @@ po_adj_nf2_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__res
                     rec[2 * c + 1] = make_float2(v.z, v.w);
                 }
                 float2 vt = make_float2(0.f, 0.f);
-                adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s);
+                if (KIND == kKindNF) adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s);
+                else adj_ff_pair2<T, HAS_M, WANT_D>(acc, rec, s);
                 if (WANT_T) vbuf[(p - fb) * kThreadsA + threadIdx.x] = vt;
             }
             if (WANT_T) {
@@ -406,31 +471,33 @@ po_adj_nf2_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__res
         part[((long)blockIdx.y * kAccAdj + a) * ns + si] = (double)hi[a] + (double)lo[a * kThreadsA + threadIdx.x];
 }
 
-int adj_nf2_smem_bytes(bool has_m, bool want_t)
+int adj_pk_smem_bytes(int kind, bool has_m, bool want_t)
 {
-    return kStages * kPairsA2 * adj2_rec(has_m, want_t) * 16 + kAccAdj * kThreadsA * 4 +
+    return kStages * kPairsA2 * adj2_rec(kind, has_m, want_t) * 16 + kAccAdj * kThreadsA * 4 +
            (want_t ? kFlush * kThreadsA * 8 : 0);
 }
 
-int adj_nf2_pairs_per_tile() { return kPairsA2; }
+int adj_pk_pairs_per_tile() { return kPairsA2; }
 
-template <int T, bool HAS_M, bool WANT_D, bool WANT_T>
-static void *adj_nf2_ptr()
+template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
+static void *adj_pk_ptr()
 {
-    return reinterpret_cast<void *>(&po_adj_nf2_kernel<T, HAS_M, WANT_D, WANT_T>);
+    return reinterpret_cast<void *>(&po_adj_pk_kernel<KIND, T, HAS_M, WANT_D, WANT_T>);
 }
 
 template <int T, bool HAS_M>
-static void *adj_nf2_sel(bool want_d, bool want_t)
+static void *adj_pk_sel(int kind, bool want_d, bool want_t)
 {
-    if (want_d) return want_t ? adj_nf2_ptr<T, HAS_M, true, true>() : adj_nf2_ptr<T, HAS_M, true, false>();
-    return want_t ? adj_nf2_ptr<T, HAS_M, false, true>() : adj_nf2_ptr<T, HAS_M, false, false>();
+    if (kind == kKindFF) return want_d ? adj_pk_ptr<kKindFF, T, HAS_M, true, false>()
+                                       : adj_pk_ptr<kKindFF, T, HAS_M, false, false>();
+    if (want_d) return want_t ? adj_pk_ptr<kKindNF, T, HAS_M, true, true>() : adj_pk_ptr<kKindNF, T, HAS_M, true, false>();
+    return want_t ? adj_pk_ptr<kKindNF, T, HAS_M, false, true>() : adj_pk_ptr<kKindNF, T, HAS_M, false, false>();
 }
 
-void *adj_nf2_kernel(int t_sign, bool has_m, bool want_d, bool want_t)
+void *adj_pk_kernel(int kind, int t_sign, bool has_m, bool want_d, bool want_t)
 {
-    if (t_sign < 0) return has_m ? adj_nf2_sel<-1, true>(want_d, want_t) : adj_nf2_sel<-1, false>(want_d, want_t);
-    return has_m ? adj_nf2_sel<1, true>(want_d, want_t) : adj_nf2_sel<1, false>(want_d, want_t);
+    if (t_sign < 0) return has_m ? adj_pk_sel<-1, true>(kind, want_d, want_t) : adj_pk_sel<-1, false>(kind, want_d, want_t);
+    return has_m ? adj_pk_sel<1, true>(kind, want_d, want_t) : adj_pk_sel<1, false>(kind, want_d, want_t);
 }
 
 void *adj_pack_tgt2_kernel() { return reinterpret_cast<void *>(&po_adj_pack_tgt2_kernel); }

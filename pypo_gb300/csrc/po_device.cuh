@@ -73,42 +73,6 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// Round-to-nearest integer of |x| < 2^22 without the conversion pipe.
-__device__ __forceinline__ float rint_magic(float x)
-{
-    return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
-}
-
-// sin(pi f2) and cos(pi f2) for a phase given as f2 = twice its value in turns
-// (|f2| <= about 1). A float pi (or 1/2pi) in the argument is a relative scale
-// error of 3e-8 on every pair; on sums of millions of pairs with spread-out
-// phases it adds up coherently to ~1e-5. Here no scaled argument is formed:
-// f2 = q/2 + y with q = rint(2 f2) and |y| <= 1/4 (both exact), and
-// sin(pi y) = y P(y^2), cos(pi y) = 1 + y^2 Q(y^2) with degree-3 P and Q
-// (least-squares fits on |y| <= 1/4, |error| < 3e-9 before rounding) whose
-// leading coefficients carry a second float for the part the first rounds
-// off. The quadrant q mod 4 is read from the low bits of 1.5*2^23 + q.
-__device__ __forceinline__ void sincos_pi(float f2, float *s, float *c)
-{
-    const float t = fmaf(f2, 2.0f, 12582912.0f);
-    const float q = __fsub_rn(t, 12582912.0f);
-    const float y = fmaf(q, -0.5f, f2);
-    const float y2 = __fmul_rn(y, y);
-    float p = fmaf(y2, -0.5893663167953491f, 2.5497970581054688f);
-    p = fmaf(y2, p, -5.167708873748779f);
-    p = fmaf(y2, p, 3.1415927410125732f);
-    const float sn = fmaf(y, p, __fmul_rn(y, -9.207879969608257e-08f));
-    float r = fmaf(y2, 0.23146405816078186f, -1.3350627422332764f);
-    r = fmaf(y2, r, 4.058708190917969f);
-    r = fmaf(y2, r, -4.934802055358887f);
-    const float cn = fmaf(y2, -1.1989475012796902e-07f, fmaf(y2, r, 1.0f));
-    const unsigned qi = __float_as_uint(t);
-    const float a = (qi & 1u) ? cn : sn;
-    const float b = (qi & 1u) ? sn : cn;
-    *s = __uint_as_float(__float_as_uint(a) ^ ((qi & 2u) << 30));
-    *c = __uint_as_float(__float_as_uint(b) ^ (((qi + 1u) & 2u) << 30));
-}
-
 // ------------------------------------------------- packed FP32x2 arithmetic
 //
 // Blackwell's FFMA2/FADD2/FMUL2 do two FP32 operations per issued
@@ -131,17 +95,19 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
     return r;
 }
 
-// sin(pi y) = y P(y^2) and cos(pi y) = 1 + y^2 Q(y^2) on both lanes for
-// |y| <= 1/2: degree-4 P and Q (near-minimax fits, |error| < 4e-9 before
-// rounding) whose leading coefficients are carried as two floats, so that no
-// rounded pi scales the argument.
+// Phases are reduced exactly to half turns before any sin/cos: the phase in
+// half turns is f = q + y with q an integer and |y| <= 1/2, and sin(pi f),
+// cos(pi f) = (-1)^q sin(pi y), (-1)^q cos(pi y). Why exactly: a rounded pi
+// (or 1/2pi) in the argument is a relative scale error of ~3e-8 on every
+// pair, which on sums of millions of pairs with spread-out phases adds up
+// coherently (the sum grows like sqrt(N), the error like N), to ~1e-5. After
+// the exact reduction any error of the reduced sin/cos flips sign with q, so
+// over phases spread across many turns it averages out instead.
 //
-// sincos_half2: sin(pi f) and cos(pi f) up to a common sign (|f| < 2^22):
-// f = q + y with q = rint(f) and |y| <= 1/2, both exact. The true values are
-// (-1)^q times these; q's parity is the low bit of t = 1.5*2^23 + q, returned
-// for flip_parity(). With the half-turn reduction, any error of the reduced
-// sin/cos flips sign with q, so over phases spread across many turns it
-// averages out instead of adding up.
+// sincos_poly2: sin(pi y) = y P(y^2) and cos(pi y) = 1 + y^2 Q(y^2) on both
+// lanes for |y| <= 1/2, degree-4 P and Q (near-minimax fits, |error| < 4e-9
+// before rounding) whose leading coefficients are carried as two floats, so
+// that no rounded pi scales the argument either.
 __device__ __forceinline__ void sincos_poly2(float2 y, float2 &sn, float2 &cs)
 {
     const float2 y2 = mul2(y, y);
@@ -157,14 +123,8 @@ __device__ __forceinline__ void sincos_poly2(float2 y, float2 &sn, float2 &cs)
     cs = fma2(y2, dup2(-1.0072982092879101e-07f), fma2(y2, r, dup2(1.0f)));
 }
 
-__device__ __forceinline__ void sincos_half2(float2 f, float2 &sn, float2 &cs, float2 &t)
-{
-    t = add2(f, dup2(12582912.0f));
-    const float2 q = sub2(t, dup2(12582912.0f));
-    sincos_poly2(sub2(f, q), sn, cs);
-}
-
-// a * (-1)^q per lane, with t from sincos_half2 (integer pipe, two ops a lane).
+// a * (-1)^q per lane, the parity of q being the low bit of t = 1.5*2^23 + q as
+// the phase helpers below return it (integer pipe, two ops a lane).
 __device__ __forceinline__ float2 flip_parity(float2 a, float2 t)
 {
     return make_float2(__uint_as_float(__float_as_uint(a.x) ^ (__float_as_uint(t.x) << 31)),

@@ -29,7 +29,6 @@ thread_local int t_launches = 0;
 struct DeviceInfo {
     bool ready = false;
     int sms = 0;
-    int occ[3][2][2] = {};   // [kind][t>0][has_m] resident CTAs per SM
     int occ2[3][2][2] = {};  // pair-packed kernels, [kind][t>0][has_m]
 };
 
@@ -86,17 +85,6 @@ static int device_info(DeviceInfo *&out)
     DeviceInfo &di = g_dev[dev];
     if (!di.ready) {
         PO_CK(cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev));
-        for (int kind = 0; kind < 3; ++kind)
-            for (int ts = 0; ts < 2; ++ts)
-                for (int hm = 0; hm < 2; ++hm) {
-                    if (kind == kKindScalar && hm) continue;
-                    void *fn = main_kernel(kind, ts ? 1 : -1, hm != 0);
-                    const int smem = main_smem_bytes(kind);
-                    PO_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-                    int nb = 0;
-                    PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
-                    di.occ[kind][ts][hm] = std::max(nb, 1);
-                }
         for (int kind = 0; kind < 3; ++kind)
             for (int ts = 0; ts < 2; ++ts)
                 for (int hm = 0; hm < 2; ++hm) {
@@ -441,10 +429,9 @@ int run_adjoint(const AdjArgs &a)
     // ---- mixed precision
     double *bbox = nullptr;
     Frame *frame = nullptr;
-    float4 *srcpk = nullptr, *trec = nullptr;
+    float4 *srcpk = nullptr;
     if (!rc && ((rc = salloc(&bbox, (size_t)kBboxBlocks * 6, s, owned)) || (rc = salloc(&frame, 1, s, owned)) ||
-                (rc = salloc(&srcpk, (size_t)ns * kRec, s, owned)) ||
-                (far && (rc = salloc(&trec, (size_t)nt * kRec, s, owned))))) {
+                (rc = salloc(&srcpk, (size_t)ns * kRec, s, owned)))) {
         sfree(owned, s);
         return rc;
     }
@@ -458,115 +445,53 @@ int run_adjoint(const AdjArgs &a)
     if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
     void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&zero_scalar, &srcpk};
     if (!rc) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
-    if (!far) {
-        // Fused near-field adjoint: one pass over the pairs for the currents
-        // and both displacement terms (targets streamed in pairs).
-        const bool want_t = grad_dt != nullptr;
-        const int rec4 = want_t ? (has_m ? 19 : 15) : 9;
-        const long npair = (nt + 1) / 2;
-        float *trec2 = nullptr;
-        double *gt = nullptr;
-        if (!rc && ((rc = salloc(&trec2, (size_t)npair * rec4 * 4, s, owned)) ||
-                    (want_t && (rc = salloc(&gt, (size_t)nt, s, owned))))) {
-            sfree(owned, s);
-            return rc;
-        }
-        void *p2args[] = {&nt, &tgt7, &gam, &frame, (void *)&rec4, &trec2};
-        const unsigned nblk_p = (unsigned)((2 * npair + 255) / 256);
-        if (!rc) rc = launch(adj_pack_tgt2_kernel(), dim3(nblk_p), dim3(256), p2args, 0, s);
-        if (!rc && want_t) PO_CK(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
-        void *fk = adj_nf2_kernel(ts, has_m, want_d, want_t);
-        const int smem2 = adj_nf2_smem_bytes(has_m, want_t);
-        int occ2 = 1;
-        if (!rc) {
-            PO_CK(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
-            PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, fk, kThreadsA, smem2));
-            occ2 = std::max(occ2, 1);
-        }
-        const long tile_t = 2L * adj_nf2_pairs_per_tile();
-        const long nsb = (ns + kThreadsA - 1) / kThreadsA;
-        const long split = choose_split(nsb, nt, (long)di->sms * occ2, ns, kAccAdj, tile_t);
-        const long tiles = std::max(1L, (nt + tile_t - 1) / tile_t);
-        long chunk = ((tiles + split - 1) / split) * tile_t;
-        double *part = nullptr;
-        if (!rc && (rc = salloc(&part, (size_t)split * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
-        const float4 *srcc = srcpk, *trc2 = reinterpret_cast<const float4 *>(trec2);
-        void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err};
-        timing_mark(s, true);
-        if (!rc) rc = launch(fk, dim3((unsigned)nsb, (unsigned)split), dim3(kThreadsA), fargs, smem2, s);
-        timing_mark(s, false);
-        int nspl = (int)split;
-        double dsc = -kappa;
-        void *eargs[] = {(void *)&kind, &nspl, &ns, &part, &src7, &gmode, &ncx, &ncy, &fac_re, &fac_im, &dsc,
-                         &grad_cur, &grad_ds};
-        if (!rc) rc = launch(adj_src_epilogue_kernel(), dim3(nblk_s), dim3(256), eargs, 0, s);
-        if (!rc && want_t) {
-            int one = 1;
-            double dsct = kappa;
-            void *teargs[] = {&one, &nt, &gt, &dsct, &grad_dt};
-            rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
-        }
+    // Pair-packed adjoint: sources in registers, pairs of targets streamed.
+    // Near field fused (currents, source and target displacement in one pass).
+    const bool want_t = grad_dt != nullptr;
+    const int rec4 = far ? 11 : (want_t ? (has_m ? 19 : 15) : 9);
+    const long npair = (nt + 1) / 2;
+    float *trec2 = nullptr;
+    double *gt = nullptr;
+    if (!rc && ((rc = salloc(&trec2, (size_t)npair * rec4 * 4, s, owned)) ||
+                (want_t && (rc = salloc(&gt, (size_t)nt, s, owned))))) {
         sfree(owned, s);
         return rc;
     }
-
-    // far field, source side: sources in registers, targets streamed
-    int farflag = 1;
-    void *paargs[] = {&nt, &tgt7, &gam, &frame, &farflag, &trec};
-    if (!rc) rc = launch(adj_pack_tgt_kernel(), dim3(nblk_t), dim3(256), paargs, 0, s);
-    void *fsrc = adj_src_kernel(kind, ts, has_m, want_d);
-    const int smem = kStages * kTile * kRec * 16 + kAccAdj * kThreadsA * 4;
-    int occ = 1;
+    int farflag = far ? 1 : 0;
+    void *p2args[] = {&nt, &tgt7, &gam, &frame, &farflag, (void *)&rec4, &trec2};
+    const unsigned nblk_p = (unsigned)((2 * npair + 255) / 256);
+    if (!rc) rc = launch(adj_pack_tgt2_kernel(), dim3(nblk_p), dim3(256), p2args, 0, s);
+    if (!rc && want_t) PO_CK(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
+    void *fk = adj_pk_kernel(kind, ts, has_m, want_d, want_t);
+    const int smem2 = adj_pk_smem_bytes(kind, has_m, want_t);
+    int occ2 = 1;
     if (!rc) {
-        PO_CK(cudaFuncSetAttribute(fsrc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fsrc, kThreadsA, smem));
-        occ = std::max(occ, 1);
+        PO_CK(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+        PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, fk, kThreadsA, smem2));
+        occ2 = std::max(occ2, 1);
     }
+    const long tile_t = 2L * adj_pk_pairs_per_tile();
     const long nsb = (ns + kThreadsA - 1) / kThreadsA;
-    const long splitA = choose_split(nsb, nt, (long)di->sms * occ, ns, kAccAdj);
-    const long tilesA = std::max(1L, (nt + kTile - 1) / kTile);
-    long chunkA = ((tilesA + splitA - 1) / splitA) * kTile;
+    const long split = choose_split(nsb, nt, (long)di->sms * occ2, ns, kAccAdj, tile_t);
+    const long tiles = std::max(1L, (nt + tile_t - 1) / tile_t);
+    long chunk = ((tiles + split - 1) / split) * tile_t;
     double *part = nullptr;
-    if (!rc && (rc = salloc(&part, (size_t)splitA * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
-    const float4 *srcc = srcpk, *trc = trec;
-    void *aargs[] = {&srcc, &ns, &trc, &nt, &chunkA, &part, &err};
+    if (!rc && (rc = salloc(&part, (size_t)split * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
+    const float4 *srcc = srcpk, *trc2 = reinterpret_cast<const float4 *>(trec2);
+    void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err};
     timing_mark(s, true);
-    if (!rc) rc = launch(fsrc, dim3((unsigned)nsb, (unsigned)splitA), dim3(kThreadsA), aargs, smem, s);
+    if (!rc) rc = launch(fk, dim3((unsigned)nsb, (unsigned)split), dim3(kThreadsA), fargs, smem2, s);
     timing_mark(s, false);
-    int nspl = (int)splitA;
+    int nspl = (int)split;
     double dsc = far ? kappa : -kappa;
-    void *eargs[] = {(void *)&kind, &nspl, &ns, &part, &src7, &gmode, &ncx, &ncy, &fac_re, &fac_im, &dsc, &grad_cur,
-                     &grad_ds};
+    void *eargs[] = {(void *)&kind, &nspl, &ns, &part, &src7, &gmode, &ncx, &ncy, &fac_re, &fac_im, &dsc,
+                     &grad_cur, &grad_ds};
     if (!rc) rc = launch(adj_src_epilogue_kernel(), dim3(nblk_s), dim3(256), eargs, 0, s);
-
-    // target side (near field): targets in registers, sources streamed
-    if (!rc && grad_dt) {
-        float4 *tgtpk = nullptr;
-        if ((rc = salloc(&tgtpk, (size_t)nt * 2, s, owned))) { sfree(owned, s); return rc; }
-        int zero_far = 0;
-        void *ptargs[] = {&nt, &tgt7, &frame, &zero_far, &tgtpk};
-        rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
-        void *ftgt = adj_tgt_kernel(ts, has_m);
-        if (!rc) {
-            PO_CK(cudaFuncSetAttribute(ftgt, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-            PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ftgt, kThreadsA, smem));
-            occ = std::max(occ, 1);
-        }
-        const long ntb = (nt + kThreadsA - 1) / kThreadsA;
-        const long splitB = choose_split(ntb, ns, (long)di->sms * occ, nt, 1);
-        const long tilesB = std::max(1L, (ns + kTile - 1) / kTile);
-        long chunkB = ((tilesB + splitB - 1) / splitB) * kTile;
-        double *partt = nullptr;
-        if (!rc && (rc = salloc(&partt, (size_t)splitB * nt, s, owned))) { sfree(owned, s); return rc; }
-        const float4 *tgc = tgtpk;
-        void *targs[] = {&srcc, &ns, &chunkB, &tgc, &gam, &tgt7, &nt, &partt, &err};
-        timing_mark(s, true);
-        if (!rc) rc = launch(ftgt, dim3((unsigned)ntb, (unsigned)splitB), dim3(kThreadsA), targs, smem, s);
-        timing_mark(s, false);
-        int nsplB = (int)splitB;
+    if (!rc && want_t) {
+        int one = 1;
         double dsct = kappa;
-        void *teargs[] = {&nsplB, &nt, &partt, &dsct, &grad_dt};
-        if (!rc) rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
+        void *teargs[] = {&one, &nt, &gt, &dsct, &grad_dt};
+        rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
     }
     sfree(owned, s);
     return rc;

@@ -1,22 +1,23 @@
-// po_kernels.cu -- sm_103a kernels of the physical-optics integrator.
+// po_kernels.cu -- sm_103a forward kernels of the physical-optics integrator.
 //
 // The O(Ns*Nt) radiation integral of reference src/CPU/Propagation.h:977-1144
 // (near field), :1656-1781 (far field) and :1279-1331 (scalar), written as an
 // N-body kernel:
 //
-//   * sources are packed once into 96-byte records (po_pack_src): positions
-//     in "turn" units (mm * k / 2 pi) relative to a frame origin, split into
-//     a hi part on a power-of-two quantum q (few significant bits, so that
+//   * sources are packed once, two per record (po_pack_src2): positions in
+//     "turn" units (mm * k / 2 pi) relative to a frame origin, split into a
+//     hi part on a power-of-two quantum q (few significant bits, so that
 //     differences and squares of hi parts are exact in FP32) and a small lo
 //     part; the unit normal; and the currents pre-multiplied by the trapezoid
 //     weight, the area element and the Green's-function prefactor;
-//   * a CTA owns NTH*TPT targets held in registers and walks its share of the
+//   * a CTA owns 128 targets held in registers and walks its share of the
 //     sources tile by tile; tiles are staged into shared memory by 1-D TMA
-//     bulk copies (cp.async.bulk) completing on mbarriers, STAGES deep;
+//     bulk copies (cp.async.bulk) completing on mbarriers, 3 stages deep;
+//   * every arithmetic step is a packed FP32x2 operation over the two
+//     sources of a record;
 //   * per pair: exact hi separation + lo correction, R^2 exact-plus-small,
-//     R = Rh + Rl by one Newton step with an exact FMA residual, phase
-//     reduction mod 1 turn on (Rh, Rl), sin/cos of the reduced angle only,
-//     everything else in FP32;
+//     R = Rh + res / (2 Rh) by one Newton step, one exact half-turn phase
+//     reduction, sin/cos of the reduced angle only, everything else in FP32;
 //   * each tile's FP32 partial is folded into a float-float total (two-sum),
 //     so long oscillatory sums stay compensated;
 //   * a source chunk (blockIdx.y) writes its totals as doubles; the epilogue
@@ -34,303 +35,11 @@
 
 namespace po {
 
-// ------------------------------------------------------------ pair kernels
-//
-// Packed source record, 6 float4 (kRec):
-//   r0 = (sh.x, sh.y, sh.z, n.x)     hi position (turns), normal x
-//   r1 = (sl.x, sl.y, sl.z, n.y)     lo position (turns), normal y
-//   r2 = (Jx.re, Jx.im, Jy.re, Jy.im)
-//   r3 = (Jz.re, Jz.im, Mx.re, Mx.im)
-//   r4 = (My.re, My.im, Mz.re, Mz.im)
-//   r5 = (n.z, 0, 0, 0)
-// Scalar record, 2 float4 (kRecScalar): (sh, S'.re), (sl, S'.im).
-//
 // Accumulators (kAcc = 12): E.re[3], E.im[3], H.re[3], H.im[3] for the near
-// field; for the far field the same slots hold S_J = sum G J' and S_M.
+// field; for the far field the same slots hold S_J = sum G J' and S_M; the
+// scalar kind has 2 (re, im).
 
-template <int T, bool HAS_M>
-__device__ __forceinline__ void nf_pair(float *acc, const float4 &tA, const float4 &tB, const float4 *r)
-{
-    const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
-    // Exact hi differences (hi parts are multiples of q with < 12 bits).
-    const float dhx = __fsub_rn(tA.x, r0.x), dhy = __fsub_rn(tA.y, r0.y), dhz = __fsub_rn(tA.z, r0.z);
-    const float dlx = __fsub_rn(tA.w, r1.x), dly = __fsub_rn(tB.x, r1.y), dlz = __fsub_rn(tB.y, r1.z);
-    // R^2 = S0 (exact) + S1 (small).
-    const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
-    const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
-    const float R2 = __fadd_rn(S0, S1);
-    const float rinv0 = rsqrtf(R2);
-    const float Rh = __fmul_rn(R2, rinv0);
-    const float p = __fmul_rn(Rh, Rh);
-    const float pe = fmaf(Rh, Rh, -p);
-    // R = Rh + res / (2 Rh): res is the exact residual of Rh^2 against S0 + S1.
-    const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
-    // Twice the reduced phase in turns, 2 (Rh - rint(Rh)) + res / Rh, in [-1, 1].
-    const float x = __fsub_rn(Rh, rint_magic(Rh));
-    const float f2 = fmaf(res, rinv0, __fadd_rn(x, x));
-    float sn, cs;
-    sincos_pi(f2, &sn, &cs);
-    // Unnormalised separation and the illumination test n . d >= -tol R:
-    // pairs within rounding of exact tangency count as lit (the reference
-    // keeps n . R_hat == 0). An unlit pair gets 1/R = 0, which zeroes every
-    // coefficient below.
-    const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
-    const float ndd = fmaf(r[5].x, dz, fmaf(r1.w, dy, r0.w * dx));
-    const float rinv = fmaf(kTangentTol32, Rh, ndd) >= 0.0f ? rinv0 : 0.0f;
-    const float ex = dx * rinv, ey = dy * rinv, ez = dz * rinv;   // R_hat
-    // u = 1/(kR), Gu = e^{t j kR} u; then with R_hat instead of d:
-    //   c1  = Gu (t u + j(u^2 - 1))          (s1 = t u^2 + j(u^3 - u))
-    //   c2  = -3 c1 - 2 j Gu                 (s2 R-scaled)
-    //   c3  = Gu (-u + j t)                  (s3 R-scaled)
-    // E = c1 J + c2 (J.R_hat) R_hat + c3 (M x R_hat);  H = c1 M + c2 (M.R_hat) R_hat - c3 (J x R_hat)
-    const float u = rinv * 0.159154943091895336f;
-    const float gur = cs * u;
-    const float gui = (T > 0 ? sn : -sn) * u;
-    const float tu = T > 0 ? u : -u;
-    const float b = fmaf(u, u, -1.0f);
-    const float c1r = fmaf(gur, tu, -gui * b);
-    const float c1i = fmaf(gur, b, gui * tu);
-    const float c2r = fmaf(-3.0f, c1r, gui + gui);
-    const float c2i = fmaf(-3.0f, c1i, -(gur + gur));
-    const float c3r = T > 0 ? fmaf(-gur, u, -gui) : fmaf(-gur, u, gui);
-    const float c3i = T > 0 ? fmaf(-gui, u, gur) : fmaf(-gui, u, -gur);
-
-    const float jxr = r2.x, jxi = r2.y, jyr = r2.z, jyi = r2.w, jzr = r3.x, jzi = r3.y;
-    // P = c2 (J . R_hat)
-    const float jer = fmaf(jzr, ez, fmaf(jyr, ey, jxr * ex));
-    const float jei = fmaf(jzi, ez, fmaf(jyi, ey, jxi * ex));
-    const float Pr = fmaf(c2r, jer, -c2i * jei);
-    const float Pi = fmaf(c2r, jei, c2i * jer);
-    // E += c1 J + P R_hat  (three FMAs into each accumulator)
-    acc[0] = fmaf(Pr, ex, fmaf(-c1i, jxi, fmaf(c1r, jxr, acc[0])));
-    acc[1] = fmaf(Pr, ey, fmaf(-c1i, jyi, fmaf(c1r, jyr, acc[1])));
-    acc[2] = fmaf(Pr, ez, fmaf(-c1i, jzi, fmaf(c1r, jzr, acc[2])));
-    acc[3] = fmaf(Pi, ex, fmaf(c1i, jxr, fmaf(c1r, jxi, acc[3])));
-    acc[4] = fmaf(Pi, ey, fmaf(c1i, jyr, fmaf(c1r, jyi, acc[4])));
-    acc[5] = fmaf(Pi, ez, fmaf(c1i, jzr, fmaf(c1r, jzi, acc[5])));
-    // H -= K x R_hat with K = c3 J
-    const float kxr = fmaf(c3r, jxr, -c3i * jxi), kxi = fmaf(c3r, jxi, c3i * jxr);
-    const float kyr = fmaf(c3r, jyr, -c3i * jyi), kyi = fmaf(c3r, jyi, c3i * jyr);
-    const float kzr = fmaf(c3r, jzr, -c3i * jzi), kzi = fmaf(c3r, jzi, c3i * jzr);
-    acc[6] = fmaf(kzr, ey, fmaf(-kyr, ez, acc[6]));
-    acc[7] = fmaf(kxr, ez, fmaf(-kzr, ex, acc[7]));
-    acc[8] = fmaf(kyr, ex, fmaf(-kxr, ey, acc[8]));
-    acc[9] = fmaf(kzi, ey, fmaf(-kyi, ez, acc[9]));
-    acc[10] = fmaf(kxi, ez, fmaf(-kzi, ex, acc[10]));
-    acc[11] = fmaf(kyi, ex, fmaf(-kxi, ey, acc[11]));
-    if (HAS_M) {
-        const float4 r4 = r[4];
-        const float mxr = r3.z, mxi = r3.w, myr = r4.x, myi = r4.y, mzr = r4.z, mzi = r4.w;
-        const float mer = fmaf(mzr, ez, fmaf(myr, ey, mxr * ex));
-        const float mei = fmaf(mzi, ez, fmaf(myi, ey, mxi * ex));
-        const float Qr = fmaf(c2r, mer, -c2i * mei);
-        const float Qi = fmaf(c2r, mei, c2i * mer);
-        // H += c1 M + Q R_hat
-        acc[6] = fmaf(Qr, ex, fmaf(-c1i, mxi, fmaf(c1r, mxr, acc[6])));
-        acc[7] = fmaf(Qr, ey, fmaf(-c1i, myi, fmaf(c1r, myr, acc[7])));
-        acc[8] = fmaf(Qr, ez, fmaf(-c1i, mzi, fmaf(c1r, mzr, acc[8])));
-        acc[9] = fmaf(Qi, ex, fmaf(c1i, mxr, fmaf(c1r, mxi, acc[9])));
-        acc[10] = fmaf(Qi, ey, fmaf(c1i, myr, fmaf(c1r, myi, acc[10])));
-        acc[11] = fmaf(Qi, ez, fmaf(c1i, mzr, fmaf(c1r, mzi, acc[11])));
-        // E += L x R_hat with L = c3 M
-        const float lxr = fmaf(c3r, mxr, -c3i * mxi), lxi = fmaf(c3r, mxi, c3i * mxr);
-        const float lyr = fmaf(c3r, myr, -c3i * myi), lyi = fmaf(c3r, myi, c3i * myr);
-        const float lzr = fmaf(c3r, mzr, -c3i * mzi), lzi = fmaf(c3r, mzi, c3i * mzr);
-        acc[0] = fmaf(lyr, ez, fmaf(-lzr, ey, acc[0]));
-        acc[1] = fmaf(lzr, ex, fmaf(-lxr, ez, acc[1]));
-        acc[2] = fmaf(lxr, ey, fmaf(-lyr, ex, acc[2]));
-        acc[3] = fmaf(lyi, ez, fmaf(-lzi, ey, acc[3]));
-        acc[4] = fmaf(lzi, ex, fmaf(-lxi, ez, acc[4]));
-        acc[5] = fmaf(lxi, ey, fmaf(-lyi, ex, acc[5]));
-    }
-}
-
-// Far field: target record tA = (rh.x, rh.y, rh.z, rl.x), tB = (rl.y, rl.z, -, -);
-// the full direction r = rh + rl is passed separately (per-target constant).
-template <int T, bool HAS_M>
-__device__ __forceinline__ void ff_pair(float *acc, const float4 &tA, const float4 &tB, const float3 &rr,
-                                        const float4 *r)
-{
-    const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
-    // r' . r_hat in turns: hi products are exact (hi parts have few bits).
-    const float Ph = fmaf(r0.z, tA.z, fmaf(r0.y, tA.y, __fmul_rn(r0.x, tA.x)));
-    const float Pl = fmaf(r1.z, rr.z, fmaf(r1.y, rr.y, fmaf(r1.x, rr.x,
-                     fmaf(r0.z, tB.y, fmaf(r0.y, tB.x, r0.x * tA.w)))));
-    const float f = __fadd_rn(__fsub_rn(Ph, rint_magic(Ph)), Pl);
-    float sn, cs;
-    sincos_pi(f + f, &sn, &cs);
-    const float ndr = fmaf(r[5].x, rr.z, fmaf(r1.w, rr.y, r0.w * rr.x));
-    const bool lit = ndr >= -kTangentTol32;
-    const float gc = lit ? cs : 0.0f;
-    const float gs = lit ? (T > 0 ? -sn : sn) : 0.0f;   // G = e^{-t j theta}
-    acc[0] = fmaf(-gs, r2.y, fmaf(gc, r2.x, acc[0]));
-    acc[3] = fmaf(gs, r2.x, fmaf(gc, r2.y, acc[3]));
-    acc[1] = fmaf(-gs, r2.w, fmaf(gc, r2.z, acc[1]));
-    acc[4] = fmaf(gs, r2.z, fmaf(gc, r2.w, acc[4]));
-    acc[2] = fmaf(-gs, r3.y, fmaf(gc, r3.x, acc[2]));
-    acc[5] = fmaf(gs, r3.x, fmaf(gc, r3.y, acc[5]));
-    if (HAS_M) {
-        const float4 r4 = r[4];
-        acc[6] = fmaf(-gs, r3.w, fmaf(gc, r3.z, acc[6]));
-        acc[9] = fmaf(gs, r3.z, fmaf(gc, r3.w, acc[9]));
-        acc[7] = fmaf(-gs, r4.y, fmaf(gc, r4.x, acc[7]));
-        acc[10] = fmaf(gs, r4.x, fmaf(gc, r4.y, acc[10]));
-        acc[8] = fmaf(-gs, r4.w, fmaf(gc, r4.z, acc[8]));
-        acc[11] = fmaf(gs, r4.z, fmaf(gc, r4.w, acc[11]));
-    }
-}
-
-// Scalar: acc += S' e^{-t j k r} / r (prefactor, weights and k/2pi folded into S').
-template <int T>
-__device__ __forceinline__ void sc_pair(float *acc, const float4 &tA, const float4 &tB, const float4 *r)
-{
-    const float4 r0 = r[0], r1 = r[1];
-    const float dhx = __fsub_rn(tA.x, r0.x), dhy = __fsub_rn(tA.y, r0.y), dhz = __fsub_rn(tA.z, r0.z);
-    const float dlx = __fsub_rn(tA.w, r1.x), dly = __fsub_rn(tB.x, r1.y), dlz = __fsub_rn(tB.y, r1.z);
-    const float S0 = fmaf(dhz, dhz, fmaf(dhy, dhy, __fmul_rn(dhx, dhx)));
-    const float S1 = fmaf(dlz, fmaf(2.0f, dhz, dlz), fmaf(dly, fmaf(2.0f, dhy, dly), dlx * fmaf(2.0f, dhx, dlx)));
-    const float R2 = __fadd_rn(S0, S1);
-    const float rinv = rsqrtf(R2);
-    const float Rh = __fmul_rn(R2, rinv);
-    const float p = __fmul_rn(Rh, Rh);
-    const float pe = fmaf(Rh, Rh, -p);
-    const float res = __fadd_rn(__fsub_rn(__fsub_rn(S0, p), pe), S1);
-    const float x = __fsub_rn(Rh, rint_magic(Rh));
-    const float f2 = fmaf(res, rinv, __fadd_rn(x, x));
-    float sn, cs;
-    sincos_pi(f2, &sn, &cs);
-    const float gr = cs * rinv;
-    const float gi = (T > 0 ? -sn : sn) * rinv;
-    acc[0] = fmaf(-gi, r1.w, fmaf(gr, r0.w, acc[0]));
-    acc[1] = fmaf(gi, r0.w, fmaf(gr, r1.w, acc[1]));
-}
-
-// --------------------------------------------------------------- main kernel
-
-template <int KIND, int T, bool HAS_M, int TPT>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
-po_main_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt,
-               long nt, double *__restrict__ part, int *__restrict__ err)
-{
-    constexpr int REC = (KIND == kKindScalar) ? kRecScalar : kRec;
-    constexpr int NACC = (KIND == kKindScalar) ? 2 : kAcc;
-    extern __shared__ __align__(128) float4 stage[];   // kStages * kTile * REC
-    __shared__ __align__(8) uint64_t full[kStages];
-
-    // Targets of this thread (coalesced: target j sits kThreads apart).
-    const long tbase = (long)blockIdx.x * kThreads * TPT + threadIdx.x;
-    float4 tA[TPT], tB[TPT];
-    float3 rr[TPT];
-#pragma unroll
-    for (int j = 0; j < TPT; ++j) {
-        const long ti = tbase + (long)j * kThreads;
-        if (ti < nt) {
-            tA[j] = tgt[2 * ti];
-            tB[j] = tgt[2 * ti + 1];
-        } else {
-            tA[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-            tB[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (KIND != kKindFF) tA[j].z = 1.0f;  // keep R > 0 for idle lanes
-        }
-        rr[j] = make_float3(tA[j].x + tA[j].w, tA[j].y + tB[j].x, tA[j].z + tB[j].y);
-    }
-
-    // Float-float totals: hi in registers, the compensation words (touched
-    // once per tile) in shared memory, [accumulator][target][thread].
-    float hi[TPT][NACC];
-    float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * kTile * REC);
-#pragma unroll
-    for (int j = 0; j < TPT; ++j)
-#pragma unroll
-        for (int a = 0; a < NACC; ++a) {
-            hi[j][a] = 0.f;
-            lo[(a * TPT + j) * kThreads + threadIdx.x] = 0.f;
-        }
-
-    const long s0 = (long)blockIdx.y * chunk;
-    const long s1 = min(ns, s0 + chunk);
-    const int ntiles = s1 > s0 ? (int)((s1 - s0 + kTile - 1) / kTile) : 0;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-
-    auto issue = [&](int it) {
-        const long first = s0 + (long)it * kTile;
-        const long cnt = min((long)kTile, s1 - first);
-        const uint32_t bytes = (uint32_t)(cnt * REC * sizeof(float4));
-        uint64_t *bar = &full[it % kStages];
-        fence_proxy_async();
-        mbar_expect_tx(bar, bytes);
-        tma_load_1d(stage + (size_t)(it % kStages) * kTile * REC, src + first * REC, bytes, bar);
-    };
-    if (threadIdx.x == 0)
-        for (int it = 0; it < ntiles && it < kStages; ++it) issue(it);
-
-    bool aborted = false;   // block-uniform: decided by __syncthreads_or
-    for (int it = 0; it < ntiles; ++it) {
-        const bool ok = mbar_wait_bounded(&full[it % kStages], (uint32_t)((it / kStages) & 1));
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) atomicExch(err, kErrWaitTimeout);
-            aborted = true;
-            break;
-        }
-        const float4 *tile = stage + (size_t)(it % kStages) * kTile * REC;
-        const int cnt = (int)min((long)kTile, s1 - (s0 + (long)it * kTile));
-        float acc[TPT][NACC];
-#pragma unroll
-        for (int j = 0; j < TPT; ++j)
-#pragma unroll
-            for (int a = 0; a < NACC; ++a) acc[j][a] = 0.f;
-
-#pragma unroll 2
-        for (int s = 0; s < cnt; ++s) {
-            float4 rec[REC];
-#pragma unroll
-            for (int q = 0; q < REC; ++q) rec[q] = tile[s * REC + q];
-#pragma unroll
-            for (int j = 0; j < TPT; ++j) {
-                if (KIND == kKindNF) nf_pair<T, HAS_M>(acc[j], tA[j], tB[j], rec);
-                else if (KIND == kKindFF) ff_pair<T, HAS_M>(acc[j], tA[j], tB[j], rr[j], rec);
-                else sc_pair<T>(acc[j], tA[j], tB[j], rec);
-            }
-        }
-        // Fold this tile's partial into the compensated totals.
-#pragma unroll
-        for (int j = 0; j < TPT; ++j)
-#pragma unroll
-            for (int a = 0; a < NACC; ++a) {
-                float s, e;
-                two_sum(hi[j][a], acc[j][a], s, e);
-                hi[j][a] = s;
-                float &l = lo[(a * TPT + j) * kThreads + threadIdx.x];
-                l = __fadd_rn(l, e);
-            }
-        __syncthreads();   // everyone is done reading this stage
-        if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
-    }
-
-    if (aborted) {
-        // Drain copies still in flight (bounded) before the CTA retires.
-        if (threadIdx.x == 0)
-            for (int s = 0; s < kStages; ++s) (void)mbar_wait_bounded(&full[s], 0);
-        return;
-    }
-
-#pragma unroll
-    for (int j = 0; j < TPT; ++j) {
-        const long ti = tbase + (long)j * kThreads;
-        if (ti >= nt) continue;
-#pragma unroll
-        for (int a = 0; a < NACC; ++a)
-            part[((long)blockIdx.y * NACC + a) * nt + ti] =
-                (double)hi[j][a] + (double)lo[(a * TPT + j) * kThreads + threadIdx.x];
-    }
-}
-
-// ------------------------------------------------ pair-packed near field
+// ------------------------------------------------ pair-packed kernels
 //
 // Pair-packed source record (kRec2 float4 per pair of sources a = 2p and
 // b = 2p + 1; every float2 slot holds (value for a, value for b)):
@@ -472,9 +181,9 @@ __device__ __forceinline__ void sc_pair2(float2 *acc, const float2 *tc, const fl
     acc[1] = fma2(gi, r[6], fma2(gr, r[7], acc[1]));
 }
 
-// Pair-packed main kernel of all three kinds. Same grid and pipeline as
-// po_main_kernel: blockIdx.y picks a source chunk (a multiple of kTile
-// sources, so chunks start on a pair boundary), tiles of kTile/2 pair records
+// Pair-packed main kernel of all three kinds. Grid = (target blocks, source
+// chunks): blockIdx.y picks a chunk of sources (a multiple of kTile, so
+// chunks start on a pair boundary), whose tiles of kTile/2 pair records
 // stream through kStages TMA stages. The thread's target is duplicated into
 // both lanes once: near field and scalar (hi xyz, lo xyz), far field
 // (r_hat hi xyz, lo xyz, full xyz).
@@ -684,6 +393,15 @@ __device__ __forceinline__ void split_hi_lo(double x, const Frame &fr, float &h,
     l = (float)(x - hd);
 }
 
+// One-source records for the adjoint kernels (a thread owns one source),
+// 6 float4 (kRec):
+//   r0 = (sh.x, sh.y, sh.z, n.x)     hi position (turns), normal x
+//   r1 = (sl.x, sl.y, sl.z, n.y)     lo position (turns), normal y
+//   r2 = (Jx.re, Jx.im, Jy.re, Jy.im)
+//   r3 = (Jz.re, Jz.im, Mx.re, Mx.im)
+//   r4 = (My.re, My.im, Mz.re, Mz.im)
+//   r5 = (n.z, 0, 0, 0)
+// Scalar record, 2 float4 (kRecScalar): (sh, S'.re), (sl, S'.im).
 // fac: complex factor folded into the currents (times weight * area).
 __global__ void po_pack_src_kernel(long ns, const double *__restrict__ src7, const double *__restrict__ cur,
                                    int gmode, int ncx, int ncy, const Frame *__restrict__ frp, double fac_re,
@@ -1058,25 +776,6 @@ __global__ void __launch_bounds__(256) po_fp32_probe_kernel(int iters, float see
 }
 
 // ----------------------------------------------------------- instantiations
-
-template <int KIND, int T, bool HAS_M>
-static void *main_kernel_ptr()
-{
-    return reinterpret_cast<void *>(&po_main_kernel<KIND, T, HAS_M, kTPT>);
-}
-
-void *main_kernel(int kind, int t_sign, bool has_m)
-{
-    if (kind == kKindNF) {
-        if (t_sign < 0) return has_m ? main_kernel_ptr<kKindNF, -1, true>() : main_kernel_ptr<kKindNF, -1, false>();
-        return has_m ? main_kernel_ptr<kKindNF, 1, true>() : main_kernel_ptr<kKindNF, 1, false>();
-    }
-    if (kind == kKindFF) {
-        if (t_sign < 0) return has_m ? main_kernel_ptr<kKindFF, -1, true>() : main_kernel_ptr<kKindFF, -1, false>();
-        return has_m ? main_kernel_ptr<kKindFF, 1, true>() : main_kernel_ptr<kKindFF, 1, false>();
-    }
-    return t_sign < 0 ? main_kernel_ptr<kKindScalar, -1, false>() : main_kernel_ptr<kKindScalar, 1, false>();
-}
 
 void *fp64_kernel(int kind)
 {

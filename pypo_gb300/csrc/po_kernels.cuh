@@ -18,9 +18,6 @@ constexpr int kKindScalar = 2;  // scalar Green's function
 #ifndef PO_THREADS
 #define PO_THREADS 128
 #endif
-#ifndef PO_TPT
-#define PO_TPT 2
-#endif
 #ifndef PO_TILE
 #define PO_TILE 128
 #endif
@@ -30,11 +27,7 @@ constexpr int kKindScalar = 2;  // scalar Green's function
 #ifndef PO_THREADS_A
 #define PO_THREADS_A 128
 #endif
-#ifndef PO_MINB_A
-#define PO_MINB_A 1
-#endif
 constexpr int kThreads = PO_THREADS;   // threads per CTA
-constexpr int kTPT = PO_TPT;           // targets per thread (registers)
 constexpr int kTile = PO_TILE;         // sources per shared-memory stage
 constexpr int kMinBlocks = PO_MINB;    // resident CTAs per SM asked of ptxas
 constexpr int kStages = 3;             // TMA pipeline depth
@@ -55,7 +48,9 @@ constexpr uint32_t kWaitLimit = 1u << 24;   // bounded mbarrier polls
 // Adjoint kernels: one source (or target) per thread; 12 current
 // accumulators + 1 displacement accumulator.
 constexpr int kThreadsA = PO_THREADS_A;
-constexpr int kMinBlocksA = PO_MINB_A;
+#ifndef PO_PAIRS_A
+#define PO_PAIRS_A 32            // target pairs per stage of the pair-packed adjoint
+#endif
 #ifndef PO_MINB_A2
 #define PO_MINB_A2 2
 #endif
@@ -88,13 +83,6 @@ struct Frame {
     double inv_q;
 };
 
-// Tile stages plus the per-thread compensation words of the totals.
-inline int main_smem_bytes(int kind)
-{
-    const int nacc = kind == kKindScalar ? 2 : kAcc;
-    return kStages * kTile * (kind == kKindScalar ? kRecScalar : kRec) * 16 + nacc * kTPT * kThreads * 4;
-}
-
 // Pair-packed main kernel: stages plus the compensation words.
 inline int pk_smem_bytes(int kind)
 {
@@ -102,7 +90,6 @@ inline int pk_smem_bytes(int kind)
     return kStages * (kTile / 2) * (sc ? kRec2Scalar : kRec2) * 16 + (sc ? 2 : kAcc) * kTPT2 * kThreads * 4;
 }
 
-void *main_kernel(int kind, int t_sign, bool has_m);
 void *pk_kernel(int kind, int t_sign, bool has_m);
 void *pack_src2_kernel();
 void *fp64_kernel(int kind);
@@ -113,18 +100,16 @@ void *pack_tgt_kernel();
 void *pack_src_d_kernel();
 void *epilogue_kernel();
 void *fp32_probe_kernel();
-void *adj_src_kernel(int kind, int t_sign, bool has_m, bool want_d);
-void *adj_tgt_kernel(int t_sign, bool has_m);
 void *adj_src_fp64_kernel(int kind, int t_sign);
 void *adj_tgt_fp64_kernel(int t_sign);
 void *adj_cot_kernel();
-void *adj_pack_tgt_kernel();
 void *adj_src_epilogue_kernel();
-// Fused pair-packed near-field adjoint (currents, source and target displacement).
-void *adj_nf2_kernel(int t_sign, bool has_m, bool want_d, bool want_t);
+// Pair-packed adjoint: near field fused (currents, source and target
+// displacement), far field (currents, source displacement).
+void *adj_pk_kernel(int kind, int t_sign, bool has_m, bool want_d, bool want_t);
 void *adj_pack_tgt2_kernel();
-int adj_nf2_smem_bytes(bool has_m, bool want_t);
-int adj_nf2_pairs_per_tile();
+int adj_pk_smem_bytes(int kind, bool has_m, bool want_t);
+int adj_pk_pairs_per_tile();
 void *adj_tgt_epilogue_kernel();
 
 }  // namespace po

@@ -78,8 +78,8 @@ int setup(StaticSetup *&out)
             for (int ts = 0; ts < 2; ++ts)
                 for (int hm = 0; hm < 2; ++hm) {
                     if (kind == po::kKindScalar && hm) continue;
-                    void *fn = po::main_kernel(kind, ts ? 1 : -1, hm != 0);
-                    const int smem = po::main_smem_bytes(kind);
+                    void *fn = po::pk_kernel(kind, ts ? 1 : -1, hm != 0);
+                    const int smem = po::pk_smem_bytes(kind);
                     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
                     if (e != cudaSuccess) return fail(2, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
                     int nb = 0;
@@ -94,10 +94,10 @@ int setup(StaticSetup *&out)
     return 0;
 }
 
-// Scratch bytes for a given chunk count.
-size_t need_bytes(long ns, long nt, int rec, int nacc, long chunks)
+// Scratch bytes for a given chunk count (rec2: float4 per pair-packed record).
+size_t need_bytes(long ns, long nt, int rec2, int nacc, long chunks)
 {
-    return kFixed + up((size_t)std::max(ns, 1L) * rec * 16) + up((size_t)nt * 32) +
+    return kFixed + up((size_t)((std::max(ns, 1L) + 1) / 2) * rec2 * 16) + up((size_t)nt * 32) +
            up((size_t)chunks * nacc * nt * sizeof(double));
 }
 
@@ -157,12 +157,12 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
     const int kind = mode == po::kFF ? po::kKindFF : (mode == po::kScalar ? po::kKindScalar : po::kKindNF);
     const int scalar = kind == po::kKindScalar;
     const int nacc = scalar ? 2 : po::kAcc;
-    const int rec = scalar ? po::kRecScalar : po::kRec;
-    const size_t minimum = need_bytes(ns, nt, rec, nacc, 1);
+    const int rec2 = scalar ? po::kRec2Scalar : po::kRec2;
+    const size_t minimum = need_bytes(ns, nt, rec2, nacc, 1);
     if (minimum > kStaticScratchBytes)
         return fail(5, "po_run_dev_static: this problem needs " + std::to_string(minimum) +
                            " bytes of scratch, more than the " + std::to_string(kStaticScratchBytes) +
-                           "-byte static array (about 96*ns + 128*nt bytes are needed)");
+                           "-byte static array (about 88*ns + 128*nt bytes are needed)");
     StaticSetup *st = nullptr;
     if (int rc = setup(st)) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -173,8 +173,8 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
 
     const int ts = t_direction > 0 ? 1 : -1;
     const bool has_m = kind != po::kKindScalar && !(flags & 1);
-    const long ntb = (nt + (long)po::kThreads * po::kTPT - 1) / ((long)po::kThreads * po::kTPT);
-    const size_t part_room = kStaticScratchBytes - (need_bytes(ns, nt, rec, nacc, 0));
+    const long ntb = (nt + (long)po::kThreads * po::kTPT2 - 1) / ((long)po::kThreads * po::kTPT2);
+    const size_t part_room = kStaticScratchBytes - (need_bytes(ns, nt, rec2, nacc, 0));
     const long max_chunks = std::max(1L, (long)(part_room / ((size_t)nacc * nt * sizeof(double))));
     const long nsplit = choose_chunks(ntb, ns, (long)st->sms * st->occ[kind][ts > 0][has_m ? 1 : 0], max_chunks);
     const long tiles = std::max(1L, (ns + po::kTile - 1) / po::kTile);
@@ -185,7 +185,7 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
     double *bbox = reinterpret_cast<double *>(b + kOffBbox);
     size_t off = kFixed;
     float4 *srcpk = reinterpret_cast<float4 *>(b + off);
-    off += up((size_t)std::max(ns, 1L) * rec * 16);
+    off += up((size_t)((std::max(ns, 1L) + 1) / 2) * rec2 * 16);
     float4 *tgtpk = reinterpret_cast<float4 *>(b + off);
     off += up((size_t)nt * 32);
     double *part = reinterpret_cast<double *>(b + off);
@@ -201,7 +201,7 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
     if (scalar) fac_re = -pref * kappa;
     const bool far = kind == po::kKindFF;
     long nb = far ? 0 : nt;
-    const unsigned nblk_s = (unsigned)((ns + 255) / 256), nblk_t = (unsigned)((nt + 255) / 256);
+    const unsigned nblk_t = (unsigned)((nt + 255) / 256);
     int rc = 0;
     void *bargs[] = {&src7, &ns, &tgt7, &nb, &bbox};
     rc = launch(po::bbox_kernel(), dim3(po::kBboxBlocks), dim3(po::kBboxThreads), bargs, 0, s);
@@ -210,16 +210,18 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
     int centred = far ? 0 : 1;
     void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
     if (!rc) rc = launch(po::frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
-    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcpk};
-    if (!rc && ns > 0) rc = launch(po::pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
+    float *srcf = reinterpret_cast<float *>(srcpk);
+    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcf};
+    const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
+    if (!rc && ns > 0) rc = launch(po::pack_src2_kernel(), dim3(nblk_p), dim3(256), psargs, 0, s);
     int farflag = far ? 1 : 0;
     void *ptargs[] = {&nt, &tgt7, &frame, &farflag, &tgtpk};
     if (!rc) rc = launch(po::pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
     const float4 *srcc = srcpk, *tgtc = tgtpk;
     void *margs[] = {&srcc, &ns, &chunk, &tgtc, &nt, &part, &err};
     if (!rc)
-        rc = launch(po::main_kernel(kind, ts, has_m), dim3((unsigned)ntb, (unsigned)nsplit), dim3(po::kThreads),
-                    margs, po::main_smem_bytes(kind), s);
+        rc = launch(po::pk_kernel(kind, ts, has_m), dim3((unsigned)ntb, (unsigned)nsplit), dim3(po::kThreads),
+                    margs, po::pk_smem_bytes(kind), s);
     int nspl = (int)nsplit;
     double t = t_direction;
     void *eargs[] = {&mode, &nspl, &nt, &part, &tgt7, &t, &zeta_inv, &out};

@@ -154,3 +154,48 @@ def test_autograd_chain_feed_dish_farfield(cuda, lib, oracle_mod):
         cm[r, c] -= 1e-3
         fdc.append((chain_loss(pert, cp) - chain_loss(pert, cm)) / 2e-3)
     assert _rel(np.array([g_cur[r, c] for r, c in ent]), np.array(fdc)) <= 1e-4
+
+
+@pytest.mark.parametrize("mode", ["EH", "JMEH", "FF"])
+def test_adjoint_odd_counts_and_padding(cuda, lib, mode):
+    """Odd source and target counts (a padded lane in the last source pair and
+    target pair of the packed kernels), M != 0, against the FP64 adjoint."""
+    from pypo_gb300 import engine, surfaces as SF
+    rng = np.random.default_rng(77)
+    s7 = engine.generate_grid(SF.paraboloid(3.0, [9, 11], gmode=1, lims_a=[0.2, 2.0]))   # 99 sources
+    if mode == "FF":
+        t7 = engine.generate_grid(SF.farfield([7, 5], [-20, 20], [-15, 15]))            # 35 directions
+    else:
+        t7 = engine.generate_grid(SF.translate(SF.plane([7, 5], gmode=0, lims_a=[-1, 1]), dz=3.0))
+        t7[3:6] *= -1.0
+    cur = rng.standard_normal((12, s7.shape[1]))
+    cot = rng.standard_normal((engine.n_out(mode), t7.shape[1]))
+    args = (mode, s7, cur, 1, 9, 11, t7, 2 * np.pi / 0.9, cot)
+    gm = engine.adjoint(*args, precision="mixed")
+    gd = engine.adjoint(*args, precision="fp64")
+    assert _rel(gm["cur"], gd["cur"]) <= 1e-5
+    assert _rel(gm["ds"], gd["ds"]) <= 1e-4
+    if mode != "FF":
+        assert _rel(gm["dt"], gd["dt"]) <= 1e-4
+
+
+def test_adjoint_many_chunks_and_determinism(cuda, lib):
+    """Many more targets than one source block streams (several target chunks,
+    atomic target-side sums across source blocks): against the FP64 adjoint,
+    and two runs agree (bitwise except the atomically summed target side)."""
+    from pypo_gb300 import engine, surfaces as SF
+    rng = np.random.default_rng(5)
+    s7 = engine.generate_grid(SF.paraboloid(20.0, [31, 29], gmode=1, lims_a=[0.5, 15.0]))   # 899 sources
+    t7 = engine.generate_grid(SF.translate(SF.plane([67, 61], gmode=0, lims_a=[-4, 4]), dz=20.0))   # 4087
+    t7[3:6] *= -1.0
+    cur = rng.standard_normal((12, s7.shape[1]))
+    cot = rng.standard_normal((12, t7.shape[1]))
+    args = ("EH", s7, cur, 1, 31, 29, t7, 2 * np.pi / 1.3, cot)
+    g1 = engine.adjoint(*args, precision="mixed")
+    g2 = engine.adjoint(*args, precision="mixed")
+    gd = engine.adjoint(*args, precision="fp64")
+    assert np.array_equal(g1["cur"], g2["cur"]) and np.array_equal(g1["ds"], g2["ds"])
+    assert _rel(g1["dt"], g2["dt"]) <= 1e-14
+    assert _rel(g1["cur"], gd["cur"]) <= 1e-5
+    assert _rel(g1["ds"], gd["ds"]) <= 1e-4
+    assert _rel(g1["dt"], gd["dt"]) <= 1e-4

@@ -61,7 +61,7 @@ def test_static_scratch_entry_matches_allocating_entry(cuda, lib):
 
 def test_static_scratch_rejects_oversized_problems(cuda, lib):
     import torch
-    big_ns = 1_000_000   # 96 MB of packed sources alone
+    big_ns = 1_000_000   # 88 MB of packed sources alone
     s7 = torch.zeros((7, 1), dtype=torch.float64, device=cuda)
     out = torch.zeros((12, 1), dtype=torch.float64, device=cuda)
     rc = lib.po_run_dev_static(1, big_ns, s7.data_ptr(), -1, 0, 0, s7.data_ptr(), 1, s7.data_ptr(),
