@@ -1,9 +1,20 @@
 """Multi-GPU use of the integrator (one process per GPU, torch.distributed).
 
-Target points are independent, so one large propagation splits into
-contiguous target shards: every rank holds the (replicated) sources, computes
-its shard, and the shards are gathered at the end. No other collective sits
-on the data path. `max_over_ranks` is the timing reduction used by bench.py.
+Forward: target points are independent, so one large propagation splits into
+contiguous target shards. Every rank holds the (replicated) sources, computes
+its shard, and the shards are gathered at the end; no other collective sits
+on the data path.
+
+Adjoint: the gradients with respect to the currents and the source
+displacement are sums over targets per source, the target-displacement
+gradient a sum over sources per target. One pass covers both: every rank
+takes a contiguous source shard against all targets (the fused adjoint), the
+source-side gradients are gathered, and the per-rank partial sums of the
+target side are added with one all_reduce (the one real exchange step).
+A source shard is not a grid any more, so it goes as a point cloud
+(gmode -1) with the trapezoid weights folded into its area row.
+
+`max_over_ranks` is the timing reduction used by bench.py.
 """
 import numpy as np
 
@@ -45,6 +56,79 @@ def propagate_sharded(mode, src7, cur, gmode, ncx, ncy, tgt7, k, epsilon=1.0, t_
     for r in range(world):
         rb, re = shard_range(nt, r, world)
         out[:, rb:re] = gathered[r][:, :re - rb].cpu().numpy()
+    return out
+
+
+def trapezoid_weights(n, gmode, ncx, ncy):
+    """Per-point trapezoid weights of a grid, as the reference's field sums
+    apply them (src/CPU/Propagation.h:1109-1126): x/u ends 0.5; y/v ends 0.5
+    unless gmode == 1 (uv); 1 everywhere for a point cloud (gmode < 0)."""
+    w = np.ones(n)
+    if gmode < 0:
+        return w
+    i = np.arange(n)
+    xu, yv = i // ncy, i % ncy
+    w[(xu == 0) | (xu == ncx - 1)] *= 0.5
+    if gmode != 1:
+        w[(yv == 0) | (yv == ncy - 1)] *= 0.5
+    return w
+
+
+def as_point_cloud(src7, gmode, ncx, ncy):
+    """src7 as a point cloud (gmode -1): the trapezoid weights move into row 6."""
+    out = np.array(src7, dtype=np.float64, copy=True)
+    out[6] *= trapezoid_weights(out.shape[1], gmode, ncx, ncy)
+    return out
+
+
+def _gather_rows(local, n, rank, world, dist, backend):
+    """All-gather a (rows, shard) float64 array of contiguous shards into (rows, n)."""
+    import torch
+    rows = local.shape[0]
+    width = n // world + (1 if n % world else 0)
+    b, e = shard_range(n, rank, world)
+    buf = torch.zeros((rows, width), dtype=torch.float64)
+    buf[:, :e - b] = torch.from_numpy(np.ascontiguousarray(local))
+    if backend == "nccl":
+        buf = buf.cuda()
+    gathered = [torch.empty_like(buf) for _ in range(world)]
+    dist.all_gather(gathered, buf)
+    out = np.empty((rows, n))
+    for r in range(world):
+        rb, re = shard_range(n, r, world)
+        out[:, rb:re] = gathered[r][:, :re - rb].cpu().numpy()
+    return out
+
+
+def adjoint_sharded(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-1.0, compute=None):
+    """Adjoint with the sources sharded over the default process group.
+
+    Arguments as pypo_gb300.engine.adjoint (host float64 arrays, identical on
+    every rank). `compute` (default engine.adjoint on this rank's GPU) maps
+    (mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon, t_dir) to the
+    dict {"cur", "ds", "dt"} of that sub-problem. Returns the full gradients on
+    every rank ("dt" is None for the far field).
+    """
+    import torch
+    import torch.distributed as dist
+    from . import engine
+    if compute is None:
+        compute = engine.adjoint
+    rank, world = dist.get_rank(), dist.get_world_size()
+    backend = dist.get_backend()
+    ns, nt = src7.shape[1], tgt7.shape[1]
+    b, e = shard_range(ns, rank, world)
+    pts = as_point_cloud(src7, gmode, ncx, ncy)
+    g = compute(mode, np.ascontiguousarray(pts[:, b:e]), np.ascontiguousarray(cur[:, b:e]), -1, 0, 0, tgt7, k, cot,
+                epsilon, t_dir)
+    out = {"cur": _gather_rows(g["cur"], ns, rank, world, dist, backend),
+           "ds": _gather_rows(g["ds"][None, :], ns, rank, world, dist, backend)[0], "dt": None}
+    if mode != "FF":
+        dt = torch.from_numpy(np.ascontiguousarray(g["dt"], dtype=np.float64))
+        if backend == "nccl":
+            dt = dt.cuda()
+        dist.all_reduce(dt, op=dist.ReduceOp.SUM)
+        out["dt"] = dt.cpu().numpy()
     return out
 
 
