@@ -145,6 +145,29 @@ int callKernelf_scalar(arrC1f *res, reflparamsf source, reflparamsf target,
  */
 int po_generate_grid(reflparams refl, reflcontainer *container, int transform, int spheric);
 
+/* The same FP64 grid, generated on the device into `out7`: a device buffer
+ * of 7 rows x n_cells[0]*n_cells[1] doubles (x, y, z, nx, ny, nz, area), the
+ * layout po_run_dev takes, queued on `stream`. The reflparams arrays are host
+ * memory, read during the call. With rms > 0 the surface-error deviates are
+ * drawn on the host in the reference's sequence (mt19937, Random.h:112-116)
+ * and the call synchronises `stream`. Replaces the host loops of
+ * InterfaceReflector.cpp:882-1081 when the grid is only needed on the GPU. */
+int po_generate_grid_dev(reflparams refl, double *out7, int transform, int spheric, void *stream);
+
+/* ---- source producers on the device --------------------------------------
+ * po_gauss_beam_dev: the vector Gaussian feed of makeGaussBeam
+ * (BeamInit.h:407-596 initGaussBeam, BindBeam.py:160-199) on the n points of
+ * a device grid (7 rows, the layout above): fields E, H and equivalent
+ * currents J, M as 12 rows x n (c2Bundle order); either output may be NULL.
+ * lam, w0, z (waist position), power as the reference's GPODict; mode 0
+ * J = n x H, M = -n x E; 1 (PMC) M only, doubled; 2 (PEC) J only, doubled.
+ * po_calc_jm_dev: the equivalent currents of given fields (12 x n) on a
+ * device grid, calcCurrents (BeamInit.h:660-843, BindBeam.py:236-280), modes
+ * 0-2 as above and 3: J = 2 n x E. Both queue on `stream`. */
+int po_gauss_beam_dev(long n, const double *grid7, double lam, double w0, double z, double power, int mode,
+                      double *fields, double *currents, void *stream);
+int po_calc_jm_dev(long n, const double *grid7, const double *fields, int mode, double *currents, void *stream);
+
 /* ---- explicit-grid, double-precision entry (host buffers) ---------------
  * New; the reference has no equivalent (its C-ABI regenerates grids inside
  * every call, Kernelsf.cu:1643-1644, so it cannot take perturbed surfaces or

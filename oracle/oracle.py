@@ -112,6 +112,8 @@ class Reference:
         lib.generateGrid.restype = None
         lib.makeGaussBeam.argtypes = [S.vecGPODict, S.reflparams, P(S.c2Bundle), P(S.c2Bundle)]
         lib.makeGaussBeam.restype = None
+        lib.calcCurrents.argtypes = [P(S.c2Bundle), P(S.c2Bundle), S.reflparams, ctypes.c_int]
+        lib.calcCurrents.restype = None
         self.lib = lib
 
     def grid(self, refl, transform=True, spheric=True):
@@ -163,3 +165,15 @@ class Reference:
         self.lib.makeGaussBeam(g, rp, ctypes.byref(M.bundle(S.c2Bundle, f, ctypes.c_double)),
                                ctypes.byref(M.bundle(S.c2Bundle, c, ctypes.c_double)))
         return f, c
+
+    def calc_currents(self, fields, surface, mode):
+        """Reference calcCurrents (BeamInit.h:660-843, calcJM): equivalent
+        currents (12, n) of fields (12, n) on the surface's grid."""
+        from pypo_gb300 import marshal as M
+        S = self.S
+        rp, keep = M.fill_reflparams(surface, ctypes.c_double)
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        c = np.zeros_like(f)
+        self.lib.calcCurrents(ctypes.byref(M.bundle(S.c2Bundle, f, ctypes.c_double)),
+                              ctypes.byref(M.bundle(S.c2Bundle, c, ctypes.c_double)), rp, int(mode))
+        return c

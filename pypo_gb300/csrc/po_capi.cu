@@ -223,6 +223,26 @@ int po_generate_grid(reflparams refl, reflcontainer *container, int transform, i
     return 0;
 }
 
+int po_generate_grid_dev(reflparams refl, double *out7, int transform, int spheric, void *stream)
+{
+    po::clear_error();
+    return po::generate_grid_dev(refl, out7, transform != 0, spheric != 0, static_cast<cudaStream_t>(stream));
+}
+
+int po_gauss_beam_dev(long n, const double *grid7, double lam, double w0, double z, double power, int mode,
+                      double *fields, double *currents, void *stream)
+{
+    po::clear_error();
+    return po::gauss_beam_dev(n, grid7, lam, w0, z, power, mode, fields, currents,
+                              static_cast<cudaStream_t>(stream));
+}
+
+int po_calc_jm_dev(long n, const double *grid7, const double *fields, int mode, double *currents, void *stream)
+{
+    po::clear_error();
+    return po::calc_jm_dev(n, grid7, fields, mode, currents, static_cast<cudaStream_t>(stream));
+}
+
 int po_run_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
              const double *tgt7, double k, double epsilon, double t_direction, int precision, double *out)
 {

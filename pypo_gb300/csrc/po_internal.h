@@ -55,6 +55,14 @@ int timing_collect(float *ms, int max);
 // Synchronises `s`, returns and clears the device error word (wait timeouts).
 int read_device_error(cudaStream_t s, int *code);
 
+// FP64 grid generation on the device into a 7-row layout (po_grid_dev.cu).
+int generate_grid_dev(const reflparams &r, double *out7, bool transform, bool spheric, cudaStream_t s);
+
+// Source producers on the device (po_sources_dev.cu).
+int gauss_beam_dev(long n, const double *g7, double lam, double w0, double z, double power, int mode,
+                   double *fields, double *cur, cudaStream_t s);
+int calc_jm_dev(long n, const double *g7, const double *fields, int mode, double *cur, cudaStream_t s);
+
 }  // namespace po
 
 int po_grid_fill(const reflparams &r, reflcontainer *c, bool transform, bool spheric);

@@ -38,6 +38,22 @@ def generate_grid(refl, transform=True, spheric=True):
     return block
 
 
+def generate_grid_dev(refl, transform=True, spheric=True, device=None, stream=None):
+    """(7, n) float64 CUDA tensor of a reflector dict, generated on the device
+    (po_generate_grid_dev; the same FP64 formulas as generate_grid), queued
+    on `stream` (default: torch's current stream)."""
+    import torch
+    lib = load()
+    dev = torch.device("cuda") if device is None else torch.device(device)
+    rp, keep = M.fill_reflparams(refl, ctypes.c_double)
+    n = int(np.prod(refl["gridsize"]))
+    out = torch.empty((7, n), dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream(dev) if stream is None else stream
+    check(lib.po_generate_grid_dev(rp, ctypes.c_void_p(out.data_ptr()), int(transform), int(spheric),
+                                   ctypes.c_void_p(st.cuda_stream)))
+    return out
+
+
 def _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy):
     if mode not in MODE_ID:
         raise POError(f"unknown mode {mode!r}; expected one of {tuple(MODE_ID)}")

@@ -51,10 +51,27 @@ def cases():
     ]
 
 
+def calcjm(ref):
+    """Reference calcCurrents on a rotated, shifted uv paraboloid with seeded
+    random fields, every mode (0 full, 1 PMC, 2 PEC, 3 source)."""
+    surf = SF.translate(SF.rotate_x(SF.paraboloid(0.4, [9, 8], gmode=1, lims_a=[0.1, 1.2]), 30.0), dz=0.5)
+    n = int(np.prod(surf["gridsize"]))
+    fields = np.random.default_rng(4242).standard_normal((12, n))
+    out = {"surface_json": dict_to_json(surf), "fields": fields}
+    for mode in range(4):
+        out[f"currents{mode}"] = ref.calc_currents(fields, surf, mode)
+    np.savez_compressed(HERE / "golden_calcjm.npz", **out)
+    print("wrote calcjm")
+
+
 def main():
     if not O.REF_PATH.exists():
         subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
     ref = O.Reference()
+    if "--only-calcjm" in sys.argv:
+        calcjm(ref)
+        return
+    calcjm(ref)
     rng = np.random.default_rng(20261203)
     k = 2 * np.pi / 0.7
     for name, src, tgt, modes in cases():

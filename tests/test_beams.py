@@ -1,5 +1,6 @@
-"""The vector Gaussian feed (pypo_gb300.beams) against the reference's
-makeGaussBeam outputs (golden vectors), full and PEC modes."""
+"""Source producers (pypo_gb300.beams) against the reference's outputs
+(golden vectors): makeGaussBeam in full and PEC modes, calcCurrents in every
+mode."""
 import numpy as np
 
 from tests.common import GOLDEN, from_json
@@ -16,3 +17,15 @@ def test_gauss_beam_matches_reference(lib):
     f2, c2 = beams.gauss_beam(s7b, 1.0, 5.0, 50.0, 1.0, mode=2)
     np.testing.assert_allclose(c2, g["currents2"], rtol=0, atol=1e-13 * np.abs(g["currents2"]).max())
     assert np.all(c2[6:] == 0)   # PEC mode: no magnetic current
+
+
+def test_calc_jm_matches_reference(lib):
+    """Equivalent currents of seeded fields on a rotated, shifted uv paraboloid
+    against the reference's calcCurrents, every mode."""
+    from pypo_gb300 import beams, engine
+    g = np.load(GOLDEN / "golden_calcjm.npz")
+    s7 = engine.generate_grid(from_json(str(g["surface_json"])))
+    for mode in range(4):
+        ref = g[f"currents{mode}"]
+        got = beams.calc_jm(s7, g["fields"], mode)
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-14 * np.abs(ref).max(), err_msg=f"mode {mode}")
