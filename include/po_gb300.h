@@ -168,6 +168,21 @@ int po_gauss_beam_dev(long n, const double *grid7, double lam, double w0, double
                       double *fields, double *currents, void *stream);
 int po_calc_jm_dev(long n, const double *grid7, const double *fields, int mode, double *currents, void *stream);
 
+/* ---- efficiencies on the device --------------------------------------------
+ * The sums behind Efficiencies.py calcSpillover / calcTaper / calcXpol /
+ * calcMainBeam (Efficiencies.py:90-177) over the n points of a device grid
+ * (7 rows; x, y and area are read), for one field component f (device rows
+ * f_re, f_im) and an optional second one g (cross-polar or fitted Gaussian;
+ * NULL, NULL if unused). Aperture (_generateMask, Efficiencies.py:11-41):
+ * shape 0 none, 1 ellipse (aperture = cx, cy, outer_x, outer_y), 2 rectangle
+ * (cx, cy, x_lo, x_hi, y_lo, y_hi relative to the centre); host memory.
+ * Writes 10 doubles to the device buffer `sums`: sum |f|^2 A, then over the
+ * aperture sum |f|^2 A, sum Re f A, sum Im f A, sum A; then sum |f|^2,
+ * sum |g|^2, max |f|^2, max |g|^2, aperture point count. Queued on `stream`,
+ * deterministic. */
+int po_efficiency_sums_dev(long n, const double *grid7, const double *f_re, const double *f_im, const double *g_re,
+                           const double *g_im, int shape, const double *aperture, double *sums, void *stream);
+
 /* ---- explicit-grid, double-precision entry (host buffers) ---------------
  * New; the reference has no equivalent (its C-ABI regenerates grids inside
  * every call, Kernelsf.cu:1643-1644, so it cannot take perturbed surfaces or

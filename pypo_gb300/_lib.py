@@ -11,7 +11,8 @@ from . import Structs as S
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "libpo_gb300.so"
 
 #: every symbol declared in include/po_gb300.h
-EXPORTS = ("po_last_error", "po_n_out", "po_last_launches", "po_generate_grid", "po_generate_grid_dev", "po_gauss_beam_dev", "po_calc_jm_dev", "po_run_d",
+EXPORTS = ("po_last_error", "po_n_out", "po_last_launches", "po_generate_grid", "po_generate_grid_dev", "po_gauss_beam_dev", "po_calc_jm_dev",
+           "po_efficiency_sums_dev", "po_run_d",
            "po_run_dev", "po_run_dev_static", "po_adjoint_dev", "po_adjoint_d", "po_device_error", "po_timing_enable", "po_timing_collect", "po_fp32_probe",
            "callKernelf_JM", "callKernelf_EH", "callKernelf_JMEH", "callKernelf_EHP",
            "callKernelf_FF", "callKernelf_scalar")
@@ -55,6 +56,9 @@ def load():
                                       c_void_p, c_void_p]
     lib.po_calc_jm_dev.restype = c_int
     lib.po_calc_jm_dev.argtypes = [c_long, c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+    lib.po_efficiency_sums_dev.restype = c_int
+    lib.po_efficiency_sums_dev.argtypes = [c_long, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                           c_void_p, c_void_p]
     lib.po_run_d.restype = c_int
     lib.po_run_d.argtypes = [c_int, c_long, c_void_p, c_int, c_int, c_int, c_void_p, c_long, c_void_p,
                              c_double, c_double, c_double, c_int, c_void_p]

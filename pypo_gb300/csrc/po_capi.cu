@@ -243,6 +243,14 @@ int po_calc_jm_dev(long n, const double *grid7, const double *fields, int mode, 
     return po::calc_jm_dev(n, grid7, fields, mode, currents, static_cast<cudaStream_t>(stream));
 }
 
+int po_efficiency_sums_dev(long n, const double *grid7, const double *f_re, const double *f_im, const double *g_re,
+                           const double *g_im, int shape, const double *aperture, double *sums, void *stream)
+{
+    po::clear_error();
+    return po::efficiency_sums_dev(n, grid7, f_re, f_im, g_re, g_im, shape, aperture, sums,
+                                   static_cast<cudaStream_t>(stream));
+}
+
 int po_run_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
              const double *tgt7, double k, double epsilon, double t_direction, int precision, double *out)
 {

@@ -63,6 +63,10 @@ int gauss_beam_dev(long n, const double *g7, double lam, double w0, double z, do
                    double *fields, double *cur, cudaStream_t s);
 int calc_jm_dev(long n, const double *g7, const double *fields, int mode, double *cur, cudaStream_t s);
 
+// Efficiency sums on the device (po_eff_dev.cu).
+int efficiency_sums_dev(long n, const double *g7, const double *fr, const double *fi, const double *gr,
+                        const double *gi, int shape, const double *aper, double *sums, cudaStream_t s);
+
 }  // namespace po
 
 int po_grid_fill(const reflparams &r, reflcontainer *c, bool transform, bool spheric);

@@ -64,6 +64,46 @@ def calcjm(ref):
     print("wrote calcjm")
 
 
+def efficiencies(ref):
+    """The reference's own Efficiencies.py (calcSpillover, calcTaper,
+    calcXpol, calcMainBeam) on a seeded aperture field, with its grid binding
+    served by the reference's compiled generateGrid."""
+    sys.path.insert(0, "/root/reference/src")
+    import PyPO.Efficiencies as E
+    from PyPO.Enums import AperShapes
+
+    class Grid:
+        pass
+
+    def generate(refl, transform=True, spheric=True):
+        b = ref.grid(refl, transform, spheric)
+        g = Grid()
+        g.x, g.y, g.z, g.area = b[0], b[1], b[2], b[6]
+        return g
+
+    E.BRefl.generateGrid = generate
+    surf = SF.plane([41, 37], gmode=0, lims_a=[-20.0, 20.0])
+    b = ref.grid(surf)
+    rng = np.random.default_rng(909)
+    amp = np.exp(-(b[0] ** 2 + (1.3 * b[1]) ** 2) / (2 * 6.0 ** 2))
+    co = amp * np.exp(1j * rng.normal(0, 0.3, amp.size))
+    xp = 0.05 * amp * np.exp(1j * rng.uniform(0, 2 * np.pi, amp.size))
+    fit = np.exp(-(b[0] ** 2 + b[1] ** 2) / (2 * 5.5 ** 2)).astype(complex)
+    ell = {"shape": AperShapes.ELL, "center": np.array([1.0, -0.5]), "outer": np.array([12.0, 9.0]),
+           "inner": np.array([0.0, 0.0])}
+    rect = {"shape": AperShapes.RECT, "center": np.array([0.5, 0.0]), "outer_x": np.array([-10.0, 12.0]),
+            "outer_y": np.array([-8.0, 7.0]), "inner_x": np.array([0.0, 0.0]), "inner_y": np.array([0.0, 0.0])}
+    out = {"surface_json": dict_to_json(surf), "co": co, "xp": xp, "fit": fit,
+           "ell": np.r_[ell["center"], ell["outer"], ell["inner"]],
+           "rect": np.r_[rect["center"], rect["outer_x"], rect["outer_y"]],
+           "spill_ell": E.calcSpillover(co, surf, ell), "spill_rect": E.calcSpillover(co, surf, rect),
+           "taper_ell": E.calcTaper(co, surf, ell), "taper_rect": E.calcTaper(co, surf, rect),
+           "taper_all": E.calcTaper(co, surf, None), "xpol": E.calcXpol(co, xp),
+           "mainbeam": E.calcMainBeam(co, surf, fit)}
+    np.savez_compressed(HERE / "golden_eff.npz", **out)
+    print("wrote efficiencies", {k: v for k, v in out.items() if np.ndim(v) == 0 and not isinstance(v, str)})
+
+
 def main():
     if not O.REF_PATH.exists():
         subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
@@ -71,7 +111,11 @@ def main():
     if "--only-calcjm" in sys.argv:
         calcjm(ref)
         return
+    if "--only-eff" in sys.argv:
+        efficiencies(ref)
+        return
     calcjm(ref)
+    efficiencies(ref)
     rng = np.random.default_rng(20261203)
     k = 2 * np.pi / 0.7
     for name, src, tgt, modes in cases():

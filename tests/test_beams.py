@@ -29,3 +29,22 @@ def test_calc_jm_matches_reference(lib):
         ref = g[f"currents{mode}"]
         got = beams.calc_jm(s7, g["fields"], mode)
         np.testing.assert_allclose(got, ref, rtol=0, atol=1e-14 * np.abs(ref).max(), err_msg=f"mode {mode}")
+
+
+def test_efficiencies_match_reference():
+    """Spillover, taper, cross-polar and main-beam efficiencies against the
+    reference's Efficiencies.py run on the same field (golden vectors)."""
+    from pypo_gb300 import efficiencies as E, engine
+    g = np.load(GOLDEN / "golden_eff.npz")
+    b = engine.generate_grid(from_json(str(g["surface_json"])), transform=False)
+    x, y, a = b[0], b[1], b[6]
+    e, r = g["ell"], g["rect"]
+    ell = {"shape": "ell", "center": e[0:2], "outer": e[2:4]}
+    rect = {"shape": "rect", "center": r[0:2], "outer_x": r[2:4], "outer_y": r[4:6]}
+    assert abs(E.spillover(g["co"], x, y, a, ell) - g["spill_ell"]) <= 1e-13
+    assert abs(E.spillover(g["co"], x, y, a, rect) - g["spill_rect"]) <= 1e-13
+    assert abs(E.taper(g["co"], x, y, a, ell) - g["taper_ell"]) <= 1e-13
+    assert abs(E.taper(g["co"], x, y, a, rect) - g["taper_rect"]) <= 1e-13
+    assert abs(E.taper(g["co"], x, y, a, None) - g["taper_all"]) <= 1e-13
+    assert abs(E.xpol(g["co"], g["xp"]) - g["xpol"]) <= 1e-13
+    assert abs(E.main_beam(g["co"], g["fit"]) - g["mainbeam"]) <= 1e-13
