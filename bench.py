@@ -20,6 +20,16 @@ path, the FP64 GPU path's own step rate, the FP32 roofline of each kernel
 (CUDA events around every launch on its stream), the clocks during the timed
 region, and the FP64 CPU oracle on a bounded sample.
 
+`--workload cassegrain` benchmarks configuration 5 instead: the Cassegrain
+chain feed (201x201) -> hyperboloid (401x401, JM) -> paraboloid (1001x1001,
+JM) -> far field (201x201, FF), ~2.1e11 pairs; a step is the forward chain
+plus its backward pass (the currents' cotangents through every stage and the
+displacement gradients of both reflectors), through torch autograd on device
+tensors (value) and through the host-buffer C-ABI with the chain rule applied
+stage by stage (e2e). The FP64 GPU chain is timed per stage on source
+subsamples and combined by pairs; the accuracy is the mixed chain against
+the FP64 chain at scale 0.2.
+
 `--impl reference` times the reference's CPU path (its compiled library when
 it loads here, else the oracle's C restatement of it) on the same workload.
 The reference has no adjoint, so that arm times the forward pass.
@@ -161,13 +171,62 @@ def reference_lib_rate(w, seconds, threads):
     return ns * rows * ncy / dt, rows * ncy, dt
 
 
+def chain_stage_workloads(c):
+    """The three stages of the Cassegrain chain as workload dicts (cpu_oracle_rate's
+    inputs); the source currents of the JM -> JM -> FF stages are seeded random
+    rows (the forward rate does not depend on their values)."""
+    rng = np.random.default_rng(11)
+    out = []
+    for mode, skey, gkey, tkey in (("JM", "feed7", "feed_grid", "sec7"), ("JM", "sec7", "sec_grid", "prim7"),
+                                   ("FF", "prim7", "prim_grid", "ff7")):
+        g = c[gkey]
+        cur = c["feed_cur"] if skey == "feed7" else rng.standard_normal((12, c[skey].shape[1]))
+        out.append(dict(mode=mode, s7=c[skey], cur=cur, gmode=g[0], ncx=g[1], ncy=g[2], t7=c[tkey], k=c["k"]))
+    return out
+
+
+def run_reference_chain(args, threads):
+    """Reference arm of the Cassegrain chain: the FP64 CPU oracle's forward rate
+    per stage on bounded target samples, combined by pairs."""
+    from pypo_gb300 import configs
+    c = configs.cassegrain()
+    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup)) / 3
+    rates = []
+    for i in range(args.warmup + args.steps):
+        total_s, pairs, parts = 0.0, 0, []
+        for w in chain_stage_workloads(c):
+            rate, n, dt = cpu_oracle_rate(w, per_step, threads)
+            sp = w["s7"].shape[1] * w["t7"].shape[1]
+            total_s += sp / rate
+            pairs += sp
+            parts.append(f"{n} targets x {w['s7'].shape[1]} sources")
+        if i >= args.warmup:
+            rates.append(pairs / total_s)
+    value = float(np.mean(rates)) / 1e9
+    sample = "per stage " + "; ".join(parts) + ", combined by pairs, forward only"
+    return value, pairs, sample, c["desc"]
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from pypo_gb300 import configs
-    w = configs.WORKLOADS[args.workload]()
     threads = os.cpu_count() or 1
+    if args.workload == "cassegrain":
+        value, pairs, sample, desc = run_reference_chain(args, threads)
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs / (value * 1e9) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": "cassegrain", "desc": desc, "pairs_per_step": pairs,
+                                                "device": "cpu", "threads": threads,
+                                                "step": "forward chain (the reference has no adjoint)"},
+                "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": threads, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    w = configs.WORKLOADS[args.workload]()
     per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
     kind = "port"
     try:
@@ -318,8 +377,11 @@ def run_ours(args):
     sel = np.abs(rc) >= np.abs(rc).max() * 0.1
     max_phase = float(np.abs(np.angle(gcx[sel] / rc[sel])).max())
 
-    # ---- adjoint accuracy and FP64 step rate on a sub-problem (every 16th source, all targets)
-    sub = slice(0, ns, 16)
+    # ---- adjoint accuracy and FP64 step rate on a sub-problem: all targets and
+    # every fstep-th source, with fstep chosen so that the FP64 kernels, one
+    # thread per source or per target, still get >= 65536 threads (a full GPU)
+    fstep = max(1, ns // 65536)
+    sub = slice(0, ns, fstep)
     s7f, curf = s7[:, sub].contiguous(), cur[:, sub].contiguous()
     nsf = s7f.shape[1]
 
@@ -399,9 +461,9 @@ def run_ours(args):
                      "forward_against": f"plain FP64 GPU sum on {idx.size} random targets (all sources)",
                      "phase_on": "E components within 20 dB of the sampled peak",
                      "adjoint": adj_acc,
-                     "adjoint_against": f"plain FP64 GPU adjoint, all targets x every 16th source ({nsf})"},
+                     "adjoint_against": f"plain FP64 GPU adjoint, all targets x every {fstep}th source ({nsf})"},
         "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (fwd+adjoint step)", "speedup": value / world / fp64_rate,
-                     "sample": f"all {nt} targets x every 16th source ({nsf})"},
+                     "sample": f"all {nt} targets x every {fstep}th source ({nsf})"},
         "roofline": {"bound": "fp32", "kernel": dom["kernel"], "achieved": dom["achieved_tflops"], "peak": peak,
                      "unit": "TFLOP/s", "frac": dom["frac"], "traffic": traffic,
                      "flops_per_pair": dom["flops_per_pair"],
@@ -419,13 +481,195 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_chain(args):
+    """Configuration 5 (Cassegrain chain with adjoint); see the module docstring."""
+    import torch
+    from pypo_gb300 import build as B
+    B.build()
+    from pypo_gb300 import autograd as A, configs, engine
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    c = configs.cassegrain(scale=args.scale)
+    k = c["k"]
+    T = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
+    stages = [("JM", "feed7", "feed_grid", "sec7"), ("JM", "sec7", "sec_grid", "prim7"),
+              ("FF", "prim7", "prim_grid", "ff7")]
+    n = {key: c[key].shape[1] for key in ("feed7", "sec7", "prim7", "ff7")}
+    stage_pairs = [n[s] * n[t] for _, s, _, t in stages]
+    pairs = sum(stage_pairs)
+    f7, fcur, s7, p7, ff7 = T(c["feed7"]), T(c["feed_cur"]), T(c["sec7"]), T(c["prim7"]), T(c["ff7"])
+    fg, sg, pg = c["feed_grid"], c["sec_grid"], c["prim_grid"]
+    cot_np = np.random.default_rng(7).standard_normal((12, n["ff7"]))
+    cot = T(cot_np)
+    ds = torch.zeros(n["sec7"], dtype=torch.float64, device=dev, requires_grad=True)
+    dp = torch.zeros(n["prim7"], dtype=torch.float64, device=dev, requires_grad=True)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(precision="mixed", feed7=f7, feed_cur=fcur, sec=s7, prim=p7, far=ff7, ct=cot, d1=ds, d2=dp):
+        flush.zero_()
+        d1.grad, d2.grad = None, None
+        j1 = A.propagate("JM", feed7, feed_cur, *fg, sec, k, dt=d1, precision=precision)
+        j2 = A.propagate("JM", sec, j1, *sg, prim, k, ds=d1, dt=d2, precision=precision)
+        ff = A.propagate("FF", prim, j2, *pg, far, k, ds=d2, precision=precision)
+        (ff * ct).sum().backward()
+        return ff
+
+    for _ in range(args.warmup):
+        step()
+    # kernel launches of one step: every device call of the chain reports its own
+    launches = [0]
+    real_fwd, real_adj = engine.propagate_dev, engine.adjoint_dev
+
+    def counted(fn):
+        def wrap(*a, **kw):
+            r = fn(*a, **kw)
+            launches[0] += engine.last_launches()
+            return r
+        return wrap
+    engine.propagate_dev, engine.adjoint_dev = counted(real_fwd), counted(real_adj)
+    step()
+    engine.propagate_dev, engine.adjoint_dev = real_fwd, real_adj
+    torch.cuda.synchronize()
+    sampler = ClockSampler(gpu_index(local))
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        from pypo_gb300.dist import max_over_ranks
+        ms = max_over_ranks(ms)
+    value = world * pairs * args.steps / (ms * 1e-3) / 1e9
+    g_auto = (ds.grad.cpu().numpy(), dp.grad.cpu().numpy())
+
+    # ---- e2e: host buffers through the C-ABI, chain rule stage by stage
+    h = {key: np.ascontiguousarray(c[key]) for key in ("feed7", "feed_cur", "sec7", "prim7", "ff7")}
+    io_bytes = []
+
+    def host_step():
+        j1 = engine.propagate("JM", h["feed7"], h["feed_cur"], *fg, h["sec7"], k)
+        j2 = engine.propagate("JM", h["sec7"], j1, *sg, h["prim7"], k)
+        engine.propagate("FF", h["prim7"], j2, *pg, h["ff7"], k)
+        g3 = engine.adjoint("FF", h["prim7"], j2, *pg, h["ff7"], k, cot_np, want=("cur", "ds"))
+        g2 = engine.adjoint("JM", h["sec7"], j1, *sg, h["prim7"], k, g3["cur"])
+        g1 = engine.adjoint("JM", h["feed7"], h["feed_cur"], *fg, h["sec7"], k, g2["cur"], want=("dt",))
+        if not io_bytes:
+            b_in = 8 * (3 * (h["feed7"].size + h["feed_cur"].size + h["sec7"].size + j1.size + h["prim7"].size
+                             + j2.size + h["ff7"].size) + cot_np.size + g3["cur"].size + g2["cur"].size)
+            b_out = 8 * (j1.size + j2.size + 12 * n["ff7"] + g3["cur"].size + g3["ds"].size + g2["cur"].size
+                         + g2["ds"].size + g2["dt"].size + g1["dt"].size)
+            io_bytes.extend([b_in, b_out])
+        return g2["ds"] + g1["dt"], g3["ds"] + g2["dt"]
+
+    g_host = host_step()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        host_step()
+    e2e_s = (time.perf_counter() - t0) / max(1, args.steps)
+    e2e = pairs / e2e_s / 1e9
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    host_vs_autograd = max(rel(g_host[0], g_auto[0]), rel(g_host[1], g_auto[1]))
+
+    # ---- FP64 GPU chain: each stage's forward + adjoint on a subsample, combined by
+    # pairs; every s-th source and t-th target with >= 65536 of each kept where a
+    # stage has that many (the FP64 kernels run one thread per source or target)
+    fp64_s = 0.0
+    for (mode, skey, gkey, tkey), sp in zip(stages, stage_pairs):
+        s_step, t_step = max(1, n[skey] // 65536), max(1, n[tkey] // 65536)
+        src_sub = np.ascontiguousarray(c[skey][:, ::s_step])
+        tgt_sub = np.ascontiguousarray(c[tkey][:, ::t_step])
+        cur_sub = np.random.default_rng(1).standard_normal((12, src_sub.shape[1]))
+        s_t, c_t, t_t = T(src_sub), T(cur_sub), T(tgt_sub)
+        nts = tgt_sub.shape[1]
+        cot_t = T(np.random.default_rng(2).standard_normal((12, nts)))
+        gcur = torch.empty((12, src_sub.shape[1]), dtype=torch.float64, device=dev)
+        gs = torch.empty(src_sub.shape[1], dtype=torch.float64, device=dev)
+        gt = None if mode == "FF" else torch.empty(nts, dtype=torch.float64, device=dev)
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        engine.propagate_dev(mode, s_t, c_t, -1, 0, 0, t_t, k, precision="fp64")
+        engine.adjoint_dev(mode, s_t, c_t, -1, 0, 0, t_t, k, cot_t, precision="fp64", grad_cur=gcur, grad_ds=gs,
+                           grad_dt=gt)
+        q1.record(stream)
+        torch.cuda.synchronize()
+        rate = src_sub.shape[1] * nts / (q0.elapsed_time(q1) * 1e-3)
+        fp64_s += sp / rate
+    fp64_rate = pairs / fp64_s / 1e9
+
+    # ---- accuracy: the mixed chain against the FP64 chain at scale 0.2
+    cs = configs.cassegrain(scale=0.2)
+    Ts = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
+    acc = {}
+    outs = {}
+    for precision in ("fp64", "mixed"):
+        d1 = torch.zeros(cs["sec7"].shape[1], dtype=torch.float64, device=dev, requires_grad=True)
+        d2 = torch.zeros(cs["prim7"].shape[1], dtype=torch.float64, device=dev, requires_grad=True)
+        ct = Ts(np.random.default_rng(3).standard_normal((12, cs["ff7"].shape[1])))
+        j1 = A.propagate("JM", Ts(cs["feed7"]), Ts(cs["feed_cur"]), *cs["feed_grid"], Ts(cs["sec7"]), k, dt=d1,
+                         precision=precision)
+        j2 = A.propagate("JM", Ts(cs["sec7"]), j1, *cs["sec_grid"], Ts(cs["prim7"]), k, ds=d1, dt=d2,
+                         precision=precision)
+        ff = A.propagate("FF", Ts(cs["prim7"]), j2, *cs["prim_grid"], Ts(cs["ff7"]), k, ds=d2, precision=precision)
+        (ff * ct).sum().backward()
+        outs[precision] = (ff.detach().cpu().numpy(), d1.grad.cpu().numpy(), d2.grad.cpu().numpy())
+    acc["ff_rel_l2"] = rel(outs["mixed"][0], outs["fp64"][0])
+    acc["grad_secondary_rel_l2"] = rel(outs["mixed"][1], outs["fp64"][1])
+    acc["grad_primary_rel_l2"] = rel(outs["mixed"][2], outs["fp64"][2])
+
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    cpu_s, cpu_pairs, cpu_parts = 0.0, 0, []
+    for w in chain_stage_workloads(c):
+        rate, nsmp, _ = cpu_oracle_rate(w, 3.0, threads)
+        sp = w["s7"].shape[1] * w["t7"].shape[1]
+        cpu_s += sp / rate
+        cpu_pairs += sp
+        cpu_parts.append(f"{nsmp} targets x {w['s7'].shape[1]} sources")
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (Gaussian feed of the configuration; random cotangent on the far field)",
+        "config": {"workload": "cassegrain" + ("" if args.scale == 1.0 else f" (scale {args.scale})"),
+                   "desc": c["desc"], "stage_pairs": stage_pairs, "pairs_per_step": pairs,
+                   "step": "forward chain + backward (currents' cotangents, displacement of both reflectors)",
+                   "l2": "flushed before every step (256 MB write inside the timed loop)",
+                   "parallelism": f"replica per GPU x{world}"},
+        "accuracy": dict(acc, against="FP64 GPU chain, configuration at scale 0.2"),
+        "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (chain fwd+adjoint)", "speedup": value / world / fp64_rate,
+                     "sample": "each stage timed on every s-th source x every t-th target (>= 65536 of each where available), combined by pairs"},
+        "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": io_bytes[0], "d2h_bytes_per_step": io_bytes[1],
+                "path": "po_run_d / po_adjoint_d per stage from host arrays, chain rule on the host",
+                "host_vs_autograd_grad_rel": host_vs_autograd},
+        "cpu_baseline": {"value": cpu_pairs / cpu_s / 1e9, "unit": "Gpairs/s (forward chain)", "cores": threads,
+                         "kind": "port", "sample": "per stage " + "; ".join(cpu_parts) + ", FP64 oracle, combined by pairs"},
+        "gpu_launches": launches[0] * args.steps, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dish_eh", choices=["dish_eh", "dish_ff"])
+    ap.add_argument("--workload", default="dish_eh", choices=["dish_eh", "dish_ff", "cassegrain"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink both grids (profiling runs only; the bench line is the full size)")
     args = ap.parse_args()
@@ -433,6 +677,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "cassegrain":
+        run_chain(args)
     else:
         run_ours(args)
 

@@ -412,7 +412,7 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
         for (int a = 0; a < kAccAdj; ++a) acc[a] = make_float2(0.f, 0.f);
         for (int fb = 0; fb < cnt; fb += kFlush) {
             const int fend = min(cnt, fb + kFlush);
-#pragma unroll 1
+#pragma unroll kUnrollA
             for (int p = fb; p < fend; ++p) {
                 float2 rec[NL];
 #pragma unroll

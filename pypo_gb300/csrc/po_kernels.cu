@@ -270,7 +270,7 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
 #pragma unroll
             for (int a = 0; a < NACC; ++a) acc[j][a] = make_float2(0.f, 0.f);
 
-#pragma unroll 1
+#pragma unroll kUnrollF
         for (int s = 0; s < cnt; ++s) {
             float2 rec[2 * NLD];
 #pragma unroll

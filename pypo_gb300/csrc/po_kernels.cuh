@@ -48,13 +48,21 @@ constexpr uint32_t kWaitLimit = 1u << 24;   // bounded mbarrier polls
 // Adjoint kernels: one source (or target) per thread; 12 current
 // accumulators + 1 displacement accumulator.
 constexpr int kThreadsA = PO_THREADS_A;
+#ifndef PO_UNROLL_F
+#define PO_UNROLL_F 1            // pair records per iteration of the forward pair loop
+#endif
+#ifndef PO_UNROLL_A
+#define PO_UNROLL_A 1            // target pairs per iteration of the adjoint pair loop
+#endif
 #ifndef PO_PAIRS_A
 #define PO_PAIRS_A 32            // target pairs per stage of the pair-packed adjoint
 #endif
 #ifndef PO_MINB_A2
 #define PO_MINB_A2 2
 #endif
-constexpr int kMinBlocksA2 = PO_MINB_A2;   // fused near-field adjoint: resident CTAs asked of ptxas
+constexpr int kMinBlocksA2 = PO_MINB_A2;
+constexpr int kUnrollF = PO_UNROLL_F;
+constexpr int kUnrollA = PO_UNROLL_A;   // fused near-field adjoint: resident CTAs asked of ptxas
 constexpr int kAccAdj = 13;
 
 // FP64 comparison kernel.
