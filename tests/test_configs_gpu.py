@@ -86,7 +86,7 @@ def test_c4_chain_gradients_against_finite_differences(cuda, lib):
         ff = A.propagate("FF", T(d7), jm, *dg, T(ff7), k, ds=dd, precision=precision)
         loss = ((ff[0:6] - T(ideal)[0:6]) ** 2).sum()
         loss.backward()
-        return dd.grad.cpu().numpy(), fc.grad.cpu().numpy(), float(loss)
+        return dd.grad.cpu().numpy(), fc.grad.cpu().numpy(), float(loss.detach())
 
     g_mixed, gf_mixed, loss_mixed = grads("mixed")
     g_fp64, gf_fp64, loss_fp64 = grads("fp64")
