@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -30,6 +31,7 @@ struct DeviceInfo {
     bool ready = false;
     int sms = 0;
     int occ2[3][2][2] = {};  // pair-packed kernels, [kind][t>0][has_m]
+    std::map<void *, int> occ_adj;   // adjoint kernels: resident CTAs, attribute set
 };
 
 std::mutex g_mu;
@@ -69,6 +71,15 @@ int n_out(int mode)
     static const int n[6] = {12, 12, 24, 15, 12, 2};
     return (mode >= 0 && mode < 6) ? n[mode] : -1;
 }
+
+// Record a CUDA failure in rc (once) and carry on to the caller's cleanup.
+#define PO_CK_RC(expr)                                                                      \
+    do {                                                                                    \
+        if (!rc) {                                                                          \
+            cudaError_t e_ = (expr);                                                        \
+            if (e_ != cudaSuccess) rc = fail(2, std::string(#expr) + ": " + err_str(e_));   \
+        }                                                                                   \
+    } while (0)
 
 #define PO_CK(expr)                                                                         \
     do {                                                                                    \
@@ -461,14 +472,22 @@ int run_adjoint(const AdjArgs &a)
     void *p2args[] = {&nt, &tgt7, &gam, &frame, &farflag, (void *)&rec4, &trec2};
     const unsigned nblk_p = (unsigned)((2 * npair + 255) / 256);
     if (!rc) rc = launch(adj_pack_tgt2_kernel(), dim3(nblk_p), dim3(256), p2args, 0, s);
-    if (!rc && want_t) PO_CK(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
+    if (want_t) PO_CK_RC(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
     void *fk = adj_pk_kernel(kind, ts, has_m, want_d, want_t);
     const int smem2 = adj_pk_smem_bytes(kind, has_m, want_t);
     int occ2 = 1;
-    if (!rc) {
-        PO_CK(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
-        PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, fk, kThreadsA, smem2));
-        occ2 = std::max(occ2, 1);
+    {
+        // once per device and kernel: the shared-memory attribute and the occupancy
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = di->occ_adj.find(fk);
+        if (it != di->occ_adj.end()) {
+            occ2 = it->second;
+        } else {
+            PO_CK_RC(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+            PO_CK_RC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, fk, kThreadsA, smem2));
+            occ2 = std::max(occ2, 1);
+            if (!rc) di->occ_adj[fk] = occ2;
+        }
     }
     const long tile_t = 2L * adj_pk_pairs_per_tile();
     const long nsb = (ns + kThreadsA - 1) / kThreadsA;
