@@ -55,11 +55,13 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Gpairs/s fwd+adjoint, mixed-prec vs FP64 sum, 1 GB300 at ≤1e-5 rel err vs FP64"
 #: algorithmic FP32 flops per pair (FMA = 2; split-precision overhead not counted)
 FWD_FLOPS = {("EH", True): 234, ("EH", False): 140, ("FF", True): 61, ("FF", False): 37}
-# Adjoint, M = 0 sources. Near field: the fused kernel (currents 12 rows, source
-# displacement 416 flops/pair, plus 62 for the target displacement sharing the
-# pair's geometry, phase, coefficients and S). Far field: currents + source
-# displacement.
-ADJ_FLOPS = {("EH", False): 478, ("FF", False): 99}
+# Adjoint. Near field: the fused kernel (currents 12 rows, source displacement
+# 416 flops/pair, plus 62 for the target displacement sharing the pair's
+# geometry, phase, coefficients and S); sources with M add 134 (source side:
+# alpha 24, M.R_hat 10, beta 8, M x R_hat 18, W.R_hat 24, W.n_s 24, b.n_s 10,
+# grad(beta).n_s 16) and 50 (target side: M.n_t 10, grad(beta).n_t 16,
+# W.n_t 24). Far field: currents + source displacement, 99; with M, +24.
+ADJ_FLOPS = {("EH", False): 478, ("EH", True): 662, ("FF", False): 99, ("FF", True): 123}
 
 
 def dist_env():
@@ -171,14 +173,32 @@ def reference_lib_rate(w, seconds, threads):
     return ns * rows * ncy / dt, rows * ncy, dt
 
 
-def chain_stage_workloads(c):
-    """The three stages of the Cassegrain chain as workload dicts (cpu_oracle_rate's
-    inputs); the source currents of the JM -> JM -> FF stages are seeded random
-    rows (the forward rate does not depend on their values)."""
+#: chain workloads: config builder, stages (mode, source, source grid, target),
+#: displaced reflectors (their normal displacement is a differentiated input)
+CHAINS = {
+    "cassegrain": ("cassegrain", [("JM", "feed7", "feed_grid", "sec7"), ("JM", "sec7", "sec_grid", "prim7"),
+                                  ("FF", "prim7", "prim_grid", "ff7")], ["sec7", "prim7"]),
+    "dish_chain": ("dish_chain", [("JM", "feed7", "feed_grid", "dish7"), ("FF", "dish7", "dish_grid", "ff7")],
+                   ["dish7"]),
+}
+
+
+def chain_config(name, scale=1.0):
+    from pypo_gb300 import configs
+    builder, stages, refl = CHAINS[name]
+    c = getattr(configs, builder)(scale=scale)
+    # initial normal displacement of each reflector: the configuration's surface error, if it has one
+    disp = {r: (c["delta"] if "delta" in c else np.zeros(c[r].shape[1])) for r in refl}
+    return c, stages, refl, disp
+
+
+def chain_stage_workloads(c, stages):
+    """The chain's stages as workload dicts (cpu_oracle_rate's inputs); the
+    source currents after the feed are seeded random rows (the forward rate
+    does not depend on their values)."""
     rng = np.random.default_rng(11)
     out = []
-    for mode, skey, gkey, tkey in (("JM", "feed7", "feed_grid", "sec7"), ("JM", "sec7", "sec_grid", "prim7"),
-                                   ("FF", "prim7", "prim_grid", "ff7")):
+    for mode, skey, gkey, tkey in stages:
         g = c[gkey]
         cur = c["feed_cur"] if skey == "feed7" else rng.standard_normal((12, c[skey].shape[1]))
         out.append(dict(mode=mode, s7=c[skey], cur=cur, gmode=g[0], ncx=g[1], ncy=g[2], t7=c[tkey], k=c["k"]))
@@ -186,15 +206,14 @@ def chain_stage_workloads(c):
 
 
 def run_reference_chain(args, threads):
-    """Reference arm of the Cassegrain chain: the FP64 CPU oracle's forward rate
-    per stage on bounded target samples, combined by pairs."""
-    from pypo_gb300 import configs
-    c = configs.cassegrain()
-    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup)) / 3
+    """Reference arm of a chain: the FP64 CPU oracle's forward rate per stage on
+    bounded target samples, combined by pairs."""
+    c, stages, _, _ = chain_config(args.workload)
+    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup)) / len(stages)
     rates = []
     for i in range(args.warmup + args.steps):
         total_s, pairs, parts = 0.0, 0, []
-        for w in chain_stage_workloads(c):
+        for w in chain_stage_workloads(c, stages):
             rate, n, dt = cpu_oracle_rate(w, per_step, threads)
             sp = w["s7"].shape[1] * w["t7"].shape[1]
             total_s += sp / rate
@@ -213,12 +232,12 @@ def run_reference(args):
         return
     from pypo_gb300 import configs
     threads = os.cpu_count() or 1
-    if args.workload == "cassegrain":
+    if args.workload in CHAINS:
         value, pairs, sample, desc = run_reference_chain(args, threads)
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs / (value * 1e9) * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": "cassegrain", "desc": desc, "pairs_per_step": pairs,
+                "data": "synthetic", "config": {"workload": args.workload, "desc": desc, "pairs_per_step": pairs,
                                                 "device": "cpu", "threads": threads,
                                                 "step": "forward chain (the reference has no adjoint)"},
                 "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": threads, "kind": "port",
@@ -280,9 +299,9 @@ def run_ours(args):
     far = mode == "FF"
     rng = np.random.default_rng(7)
     cot_np = rng.standard_normal((nout, nt))
-    s7 = torch.tensor(w["s7"], device=dev)
-    cur = torch.tensor(w["cur"], device=dev)
-    t7 = torch.tensor(w["t7"], device=dev)
+    s7 = torch.tensor(np.ascontiguousarray(w["s7"]), device=dev)
+    cur = torch.tensor(np.ascontiguousarray(w["cur"]), device=dev)
+    t7 = torch.tensor(np.ascontiguousarray(w["t7"]), device=dev)
     cot = torch.tensor(cot_np, device=dev)
     out = torch.empty((nout, nt), dtype=torch.float64, device=dev)
     g_cur = torch.empty((12, ns), dtype=torch.float64, device=dev)
@@ -424,7 +443,7 @@ def run_ours(args):
     mk = ("EH" if not far else "FF", not m_zero)
     # pair-packed forward and adjoint (near field: the fused adjoint)
     names = ["forward po_pk_kernel", "adjoint po_adj_pk_kernel"]
-    flops = [FWD_FLOPS[mk], ADJ_FLOPS.get((mk[0], False))]
+    flops = [FWD_FLOPS[mk], ADJ_FLOPS[mk]]
     kernels = []
     for j in range(kernels_per_step):
         lm = float(launch_ms[:, j].mean())
@@ -482,11 +501,11 @@ def run_ours(args):
 
 
 def run_chain(args):
-    """Configuration 5 (Cassegrain chain with adjoint); see the module docstring."""
+    """A chain workload (configuration 4 or 5); see the module docstring."""
     import torch
     from pypo_gb300 import build as B
     B.build()
-    from pypo_gb300 import autograd as A, configs, engine
+    from pypo_gb300 import autograd as A, engine
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -494,31 +513,36 @@ def run_chain(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    c = configs.cassegrain(scale=args.scale)
+    c, stages, refl, disp0 = chain_config(args.workload, args.scale)
     k = c["k"]
     T = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
-    stages = [("JM", "feed7", "feed_grid", "sec7"), ("JM", "sec7", "sec_grid", "prim7"),
-              ("FF", "prim7", "prim_grid", "ff7")]
-    n = {key: c[key].shape[1] for key in ("feed7", "sec7", "prim7", "ff7")}
-    stage_pairs = [n[s] * n[t] for _, s, _, t in stages]
+    keys = sorted({sk for _, sk, _, _ in stages} | {tk for _, _, _, tk in stages})
+    n = {key: c[key].shape[1] for key in keys}
+    stage_pairs = [n[sk] * n[tk] for _, sk, _, tk in stages]
     pairs = sum(stage_pairs)
-    f7, fcur, s7, p7, ff7 = T(c["feed7"]), T(c["feed_cur"]), T(c["sec7"]), T(c["prim7"]), T(c["ff7"])
-    fg, sg, pg = c["feed_grid"], c["sec_grid"], c["prim_grid"]
-    cot_np = np.random.default_rng(7).standard_normal((12, n["ff7"]))
-    cot = T(cot_np)
-    ds = torch.zeros(n["sec7"], dtype=torch.float64, device=dev, requires_grad=True)
-    dp = torch.zeros(n["prim7"], dtype=torch.float64, device=dev, requires_grad=True)
+    nff = n[stages[-1][3]]
+    cot_np = np.random.default_rng(7).standard_normal((12, nff))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step(precision="mixed", feed7=f7, feed_cur=fcur, sec=s7, prim=p7, far=ff7, ct=cot, d1=ds, d2=dp):
+    def forward_backward(cc, dv, precision, ct):
+        """Forward chain and backward pass; dv: reflector -> displacement tensor (requires grad)."""
+        pts = {key: torch.tensor(np.ascontiguousarray(cc[key]), device=dev) for key in keys}
+        cur = torch.tensor(np.ascontiguousarray(cc["feed_cur"]), device=dev)
+        for mode, sk, gk, tk in stages:
+            cur = A.propagate(mode, pts[sk], cur, *cc[gk], pts[tk], k, ds=dv.get(sk),
+                              dt=dv.get(tk) if mode != "FF" else None, precision=precision)
+        (cur * ct).sum().backward()
+        return cur
+
+    dvars = {r: torch.tensor(disp0[r], device=dev, requires_grad=True) for r in refl}
+    cot = T(cot_np)
+
+    def step():
         flush.zero_()
-        d1.grad, d2.grad = None, None
-        j1 = A.propagate("JM", feed7, feed_cur, *fg, sec, k, dt=d1, precision=precision)
-        j2 = A.propagate("JM", sec, j1, *sg, prim, k, ds=d1, dt=d2, precision=precision)
-        ff = A.propagate("FF", prim, j2, *pg, far, k, ds=d2, precision=precision)
-        (ff * ct).sum().backward()
-        return ff
+        for v in dvars.values():
+            v.grad = None
+        forward_backward(c, dvars, "mixed", cot)
 
     for _ in range(args.warmup):
         step()
@@ -554,26 +578,41 @@ def run_chain(args):
         from pypo_gb300.dist import max_over_ranks
         ms = max_over_ranks(ms)
     value = world * pairs * args.steps / (ms * 1e-3) / 1e9
-    g_auto = (ds.grad.cpu().numpy(), dp.grad.cpu().numpy())
+    g_auto = {r: v.grad.cpu().numpy() for r, v in dvars.items()}
 
     # ---- e2e: host buffers through the C-ABI, chain rule stage by stage
-    h = {key: np.ascontiguousarray(c[key]) for key in ("feed7", "feed_cur", "sec7", "prim7", "ff7")}
+    host = {key: np.ascontiguousarray(c[key]) for key in keys}
+    for r in refl:                                   # displaced reflector points (normals, areas frozen)
+        host[r] = host[r].copy()
+        host[r][:3] += disp0[r][None, :] * host[r][3:6]
     io_bytes = []
 
     def host_step():
-        j1 = engine.propagate("JM", h["feed7"], h["feed_cur"], *fg, h["sec7"], k)
-        j2 = engine.propagate("JM", h["sec7"], j1, *sg, h["prim7"], k)
-        engine.propagate("FF", h["prim7"], j2, *pg, h["ff7"], k)
-        g3 = engine.adjoint("FF", h["prim7"], j2, *pg, h["ff7"], k, cot_np, want=("cur", "ds"))
-        g2 = engine.adjoint("JM", h["sec7"], j1, *sg, h["prim7"], k, g3["cur"])
-        g1 = engine.adjoint("JM", h["feed7"], h["feed_cur"], *fg, h["sec7"], k, g2["cur"], want=("dt",))
+        curs = [np.ascontiguousarray(c["feed_cur"])]
+        for mode, sk, gk, tk in stages[:-1]:
+            curs.append(engine.propagate(mode, host[sk], curs[-1], *c[gk], host[tk], k))
+        mode, sk, gk, tk = stages[-1]
+        engine.propagate(mode, host[sk], curs[-1], *c[gk], host[tk], k)
+        grads = {r: np.zeros(n[r]) for r in refl}
+        ct = cot_np
+        b_in = b_out = 0
+        for i in range(len(stages) - 1, -1, -1):
+            mode, sk, gk, tk = stages[i]
+            want = (("cur",) if i > 0 else ()) + (("ds",) if sk in refl else ()) + \
+                (("dt",) if tk in refl and mode != "FF" else ())
+            g = engine.adjoint(mode, host[sk], curs[i], *c[gk], host[tk], k, ct, want=want)
+            if sk in refl:
+                grads[sk] += g["ds"]
+            if tk in refl and mode != "FF":
+                grads[tk] += g["dt"]
+            b_in += 8 * (host[sk].size + curs[i].size + host[tk].size + ct.size)
+            b_out += 8 * sum(v.size for v in g.values() if v is not None)
+            ct = g.get("cur")
         if not io_bytes:
-            b_in = 8 * (3 * (h["feed7"].size + h["feed_cur"].size + h["sec7"].size + j1.size + h["prim7"].size
-                             + j2.size + h["ff7"].size) + cot_np.size + g3["cur"].size + g2["cur"].size)
-            b_out = 8 * (j1.size + j2.size + 12 * n["ff7"] + g3["cur"].size + g3["ds"].size + g2["cur"].size
-                         + g2["ds"].size + g2["dt"].size + g1["dt"].size)
-            io_bytes.extend([b_in, b_out])
-        return g2["ds"] + g1["dt"], g3["ds"] + g2["dt"]
+            fwd_in = sum(8 * (host[sk].size + curs[j].size + host[tk].size) for j, (_, sk, _, tk) in enumerate(stages))
+            fwd_out = sum(8 * x.size for x in curs[1:]) + 8 * 12 * nff
+            io_bytes.extend([fwd_in + b_in, fwd_out + b_out])
+        return grads
 
     g_host = host_step()
     t0 = time.perf_counter()
@@ -582,7 +621,7 @@ def run_chain(args):
     e2e_s = (time.perf_counter() - t0) / max(1, args.steps)
     e2e = pairs / e2e_s / 1e9
     rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
-    host_vs_autograd = max(rel(g_host[0], g_auto[0]), rel(g_host[1], g_auto[1]))
+    host_vs_autograd = max(rel(g_host[r], g_auto[r]) for r in refl)
 
     # ---- FP64 GPU chain: each stage's forward + adjoint on a subsample, combined by
     # pairs; every s-th source and t-th target with >= 65536 of each kept where a
@@ -611,30 +650,22 @@ def run_chain(args):
     fp64_rate = pairs / fp64_s / 1e9
 
     # ---- accuracy: the mixed chain against the FP64 chain at scale 0.2
-    cs = configs.cassegrain(scale=0.2)
-    Ts = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
-    acc = {}
+    cs, _, _, ds0 = chain_config(args.workload, 0.2)
+    ct_s = T(np.random.default_rng(3).standard_normal((12, cs[stages[-1][3]].shape[1])))
     outs = {}
     for precision in ("fp64", "mixed"):
-        d1 = torch.zeros(cs["sec7"].shape[1], dtype=torch.float64, device=dev, requires_grad=True)
-        d2 = torch.zeros(cs["prim7"].shape[1], dtype=torch.float64, device=dev, requires_grad=True)
-        ct = Ts(np.random.default_rng(3).standard_normal((12, cs["ff7"].shape[1])))
-        j1 = A.propagate("JM", Ts(cs["feed7"]), Ts(cs["feed_cur"]), *cs["feed_grid"], Ts(cs["sec7"]), k, dt=d1,
-                         precision=precision)
-        j2 = A.propagate("JM", Ts(cs["sec7"]), j1, *cs["sec_grid"], Ts(cs["prim7"]), k, ds=d1, dt=d2,
-                         precision=precision)
-        ff = A.propagate("FF", Ts(cs["prim7"]), j2, *cs["prim_grid"], Ts(cs["ff7"]), k, ds=d2, precision=precision)
-        (ff * ct).sum().backward()
-        outs[precision] = (ff.detach().cpu().numpy(), d1.grad.cpu().numpy(), d2.grad.cpu().numpy())
-    acc["ff_rel_l2"] = rel(outs["mixed"][0], outs["fp64"][0])
-    acc["grad_secondary_rel_l2"] = rel(outs["mixed"][1], outs["fp64"][1])
-    acc["grad_primary_rel_l2"] = rel(outs["mixed"][2], outs["fp64"][2])
+        dv = {r: torch.tensor(ds0[r], device=dev, requires_grad=True) for r in refl}
+        ff = forward_backward(cs, dv, precision, ct_s)
+        outs[precision] = (ff.detach().cpu().numpy(), {r: v.grad.cpu().numpy() for r, v in dv.items()})
+    acc = {"ff_rel_l2": rel(outs["mixed"][0], outs["fp64"][0])}
+    for r in refl:
+        acc[f"grad_{r[:-1]}_rel_l2"] = rel(outs["mixed"][1][r], outs["fp64"][1][r])
 
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     cpu_s, cpu_pairs, cpu_parts = 0.0, 0, []
-    for w in chain_stage_workloads(c):
+    for w in chain_stage_workloads(c, stages):
         rate, nsmp, _ = cpu_oracle_rate(w, 3.0, threads)
         sp = w["s7"].shape[1] * w["t7"].shape[1]
         cpu_s += sp / rate
@@ -645,14 +676,15 @@ def run_chain(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (Gaussian feed of the configuration; random cotangent on the far field)",
-        "config": {"workload": "cassegrain" + ("" if args.scale == 1.0 else f" (scale {args.scale})"),
+        "config": {"workload": args.workload + ("" if args.scale == 1.0 else f" (scale {args.scale})"),
                    "desc": c["desc"], "stage_pairs": stage_pairs, "pairs_per_step": pairs,
-                   "step": "forward chain + backward (currents' cotangents, displacement of both reflectors)",
+                   "step": "forward chain + backward (currents' cotangents, displacement of every reflector)",
                    "l2": "flushed before every step (256 MB write inside the timed loop)",
                    "parallelism": f"replica per GPU x{world}"},
         "accuracy": dict(acc, against="FP64 GPU chain, configuration at scale 0.2"),
         "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (chain fwd+adjoint)", "speedup": value / world / fp64_rate,
-                     "sample": "each stage timed on every s-th source x every t-th target (>= 65536 of each where available), combined by pairs"},
+                     "sample": "each stage timed on every s-th source x every t-th target (>= 65536 of each where "
+                               "available), combined by pairs"},
         "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": io_bytes[0], "d2h_bytes_per_step": io_bytes[1],
                 "path": "po_run_d / po_adjoint_d per stage from host arrays, chain rule on the host",
                 "host_vs_autograd_grad_rel": host_vs_autograd},
@@ -662,14 +694,14 @@ def run_chain(args):
     }
     print(json.dumps(line), flush=True)
 
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dish_eh", choices=["dish_eh", "dish_ff", "cassegrain"])
+    ap.add_argument("--workload", default="dish_eh",
+                    choices=["dish_eh", "dish_ff", "feed_dish_jm", "cassegrain", "dish_chain"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink both grids (profiling runs only; the bench line is the full size)")
     args = ap.parse_args()
@@ -677,7 +709,7 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "cassegrain":
+    elif args.workload in CHAINS:
         run_chain(args)
     else:
         run_ours(args)

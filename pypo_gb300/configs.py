@@ -80,7 +80,7 @@ def feed_plane(lam, w0, half_width, n, power=4 * np.pi, z_shift=0.0):
     s7 = engine.generate_grid(plane)
     _, cur = beams.gauss_beam(s7, lam, w0, 0.0, power)
     s7[2] += z_shift
-    return plane, s7, cur
+    return plane, s7, np.ascontiguousarray(cur)
 
 
 def dish_facing_feed(f, D, n, gmode=1):
