@@ -22,9 +22,11 @@ region, and the FP64 CPU oracle on a bounded sample.
 
 `--workload cassegrain` benchmarks configuration 5 instead: the Cassegrain
 chain feed (201x201) -> hyperboloid (401x401, JM) -> paraboloid (1001x1001,
-JM) -> far field (201x201, FF), ~2.1e11 pairs; a step is the forward chain
+JM) -> far field (201x201, FF), ~2.1e11 pairs; `--workload dish_chain`
+configuration 4: feed (101x101) -> dish (301x301, JM, with its seeded surface
+error) -> far field (101x101, FF). For a chain, a step is the forward chain
 plus its backward pass (the currents' cotangents through every stage and the
-displacement gradients of both reflectors), through torch autograd on device
+displacement gradients of every reflector), through torch autograd on device
 tensors (value) and through the host-buffer C-ABI with the chain rule applied
 stage by stage (e2e). The FP64 GPU chain is timed per stage on source
 subsamples and combined by pairs; the accuracy is the mixed chain against
