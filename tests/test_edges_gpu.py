@@ -129,6 +129,44 @@ def test_large_phase_farfield(cuda, lib, oracle_mod):
     _check("FF", s7, cur, 1, 41, 40, ff, 2 * np.pi, oracle_mod)
 
 
+def test_large_scene_nearfield_within_limit(cuda, lib, oracle_mod):
+    """Targets 30 m from a 2 m dish at 0.5 mm wavelength: R ~ 1.2e5 turns
+    (kR ~ 7.5e5 rad), frame half-extent 3e4 wavelengths, inside the mixed
+    path's measured range. Forward against the oracle, adjoint against the
+    FP64 adjoint."""
+    from pypo_gb300 import engine, surfaces as SF
+    s7 = engine.generate_grid(SF.paraboloid(800.0, [41, 40], gmode=1, lims_a=[0, 1000]))
+    t7 = engine.generate_grid(SF.translate(SF.plane([7, 7], gmode=0, lims_a=[-2000, 2000]), dz=3.0e4))
+    t7[3:6] *= -1.0
+    rng = np.random.default_rng(21)
+    cur = rng.standard_normal((12, s7.shape[1]))
+    k = 2 * np.pi / 0.5
+    assert engine.mixed_extent("EH", s7, t7, k) <= engine.MIXED_EXTENT_LIMIT
+    for mode in ("EH", "JM"):
+        _check(mode, s7, cur, 1, 41, 40, t7, k, oracle_mod)
+    cot = rng.standard_normal((12, t7.shape[1]))
+    gm = engine.adjoint("EH", s7, cur, 1, 41, 40, t7, k, cot, precision="mixed")
+    gd = engine.adjoint("EH", s7, cur, 1, 41, 40, t7, k, cot, precision="fp64")
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel(gm["cur"], gd["cur"]) <= REL_L2_TOL
+    assert rel(gm["ds"], gd["ds"]) <= 1e-4 and rel(gm["dt"], gd["dt"]) <= 1e-4
+
+
+def test_large_scene_farfield_within_limit(cuda, lib, oracle_mod):
+    """A 2 m dish 27 m from the coordinate origin (the far field's phase
+    reference) at 0.5 mm wavelength: source coordinates up to 4.6e4
+    wavelengths, inside the mixed path's measured range."""
+    from pypo_gb300 import engine, surfaces as SF
+    src = SF.translate(SF.paraboloid(800.0, [41, 40], gmode=1, lims_a=[0, 1000]), 2.2e4, -1.4e4, 8.0e3)
+    s7 = engine.generate_grid(src)
+    ff = engine.generate_grid(SF.farfield([9, 9], [-1.0, 1.0], [-1.0, 1.0]))
+    k = 2 * np.pi / 0.5
+    assert engine.mixed_extent("FF", s7, ff, k) <= engine.MIXED_EXTENT_LIMIT
+    cur = np.random.default_rng(22).standard_normal((12, s7.shape[1]))
+    for t in (-1.0, 1.0):
+        _check("FF", s7, cur, 1, 41, 40, ff, k, oracle_mod, t)
+
+
 def test_deterministic_and_clean_error_word(cuda, lib):
     import torch
     from pypo_gb300 import engine

@@ -109,3 +109,27 @@ def test_runpodict_validation():
                 {"mode": "EH", "s_current": 1}):
         with pytest.raises(RunPOError):
             check_runPODict_gpu(dict(bad))
+
+
+def test_mixed_extent_and_warning():
+    """The frame half-extent that sets the mixed path's precision, and the
+    host-side warning beyond the measured limit."""
+    import warnings
+    from pypo_gb300 import engine
+    s7 = np.zeros((7, 2))
+    s7[0] = [-1.0, 1.0]
+    t7 = np.zeros((7, 1))
+    t7[2] = 1000.0                                        # mm
+    k = 2 * np.pi / 0.5                                   # 2 wavelengths per mm
+    assert engine.mixed_extent("EH", s7, t7, k) == 1000.0   # half of the 1000 mm z side, x 2
+    assert engine.mixed_extent("FF", s7, t7, k) == 2.0      # largest source coordinate only
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        engine._extent_warning("EH", s7, t7, k, "mixed")   # 1e3 wavelengths: no warning
+    far = t7.copy()
+    far[2] = 1.0e5
+    with pytest.warns(RuntimeWarning, match="fp64"):
+        engine._extent_warning("EH", s7, far, k, "mixed")
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        engine._extent_warning("EH", s7, far, k, "fp64")
