@@ -20,11 +20,10 @@ path, the FP64 GPU path's own step rate, the FP32 roofline of each kernel
 (CUDA events around every launch on its stream), the clocks during the timed
 region, and the FP64 CPU oracle on a bounded sample.
 
-`--workload cassegrain` benchmarks configuration 5 instead: the Cassegrain
-chain feed (201x201) -> hyperboloid (401x401, JM) -> paraboloid (1001x1001,
-JM) -> far field (201x201, FF), ~2.1e11 pairs; `--workload dish_chain`
-configuration 4: feed (101x101) -> dish (301x301, JM, with its seeded surface
-error) -> far field (101x101, FF). For a chain, a step is the forward chain
+`--workload cassegrain` benchmarks the Cassegrain chain instead: feed (201x201) -> hyperboloid (401x401, JM) -> paraboloid (1001x1001,
+JM) -> far field (201x201, FF), ~2.1e11 pairs; `--workload dish_chain` the
+perturbed-dish chain: feed (101x101) -> dish (301x301, JM, with its seeded
+surface error) -> far field (101x101, FF). For a chain, a step is the forward chain
 plus its backward pass (the currents' cotangents through every stage and the
 displacement gradients of every reflector), through torch autograd on device
 tensors (value) and through the host-buffer C-ABI with the chain rule applied
@@ -503,7 +502,7 @@ def run_ours(args):
 
 
 def run_chain(args):
-    """A chain workload (configuration 4 or 5); see the module docstring."""
+    """A chain workload (the perturbed-dish or the Cassegrain chain); see the module docstring."""
     import torch
     from pypo_gb300 import build as B
     B.build()

@@ -1,11 +1,12 @@
-"""The benchmark configurations as parity cases (GPU).
+"""The benchmark workloads as parity cases (GPU).
 
-C1 feed -> dish JM (full size) against the oracle; C2 dish EH and C3 dish far
-field (full size, 2.3e10 and 1.6e11 pairs) against the plain FP64 GPU sum on
-sampled targets and the oracle on a few; C4 feed -> perturbed dish -> far
-field with gradients of sum |E_ff - E_ideal|^2 against central finite
-differences (h = 1e-6 lambda) on 64 random dish nodes; C5 Cassegrain chain
-(reduced grids) against the FP64 chain, forward and gradients.
+Gaussian feed -> dish, JM (full size, 1e8 pairs) against the oracle; the
+D 1000 mm dish to its focal plane (EH, 2.3e10 pairs) and the D 2000 mm dish to
+its far field (FF, 1.6e11 pairs), full size, against the plain FP64 GPU sum on
+sampled targets and the oracle on a few; feed -> perturbed dish -> far field
+with gradients of sum |E_ff - E_ideal|^2 against central finite differences
+(h = 1e-6 lambda) on 64 random dish nodes; the Cassegrain chain (reduced
+grids) against the FP64 chain, forward and gradients.
 """
 import numpy as np
 import pytest
@@ -19,7 +20,7 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def test_c1_feed_to_dish_full_size(cuda, lib, oracle_mod):
+def test_feed_to_dish_jm_full_size(cuda, lib, oracle_mod):
     from pypo_gb300 import configs, engine
     w = configs.feed_dish_jm()
     args = (w["mode"], w["s7"], w["cur"], w["gmode"], w["ncx"], w["ncy"], w["t7"], w["k"])
@@ -30,7 +31,7 @@ def test_c1_feed_to_dish_full_size(cuda, lib, oracle_mod):
 
 
 @pytest.mark.parametrize("name", ["dish_eh", "dish_ff"])
-def test_c2_c3_full_size_sampled(cuda, lib, oracle_mod, name):
+def test_dish_workloads_full_size_sampled(cuda, lib, oracle_mod, name):
     """Full-size run; per-point error on a 2 % random target sample against the
     FP64 GPU sum, and on 16 targets against the oracle."""
     import torch
@@ -61,7 +62,7 @@ def _trap_weight(i, gmode, ncx, ncy):
     return w
 
 
-def test_c4_chain_gradients_against_finite_differences(cuda, lib):
+def test_perturbed_dish_chain_gradients_against_finite_differences(cuda, lib):
     """feed -> dish (JM) -> far field (FF), dish displaced by a correlated surface
     error; L = sum |E_ff - E_ideal|^2 (E rows). Autograd (mixed) gradients against
     central FD of the FP64 GPU chain on 64 random nodes, and against the FP64
@@ -121,7 +122,7 @@ def test_c4_chain_gradients_against_finite_differences(cuda, lib):
     assert _rel(g_fp64[nodes], fd) <= 1e-6
 
 
-def test_c5_cassegrain_chain_against_fp64(cuda, lib):
+def test_cassegrain_chain_against_fp64(cuda, lib):
     """feed -> hyperboloid (JM) -> paraboloid (JM) -> far field on reduced grids:
     the mixed chain and its displacement gradients against the FP64 chain."""
     import torch

@@ -45,7 +45,7 @@ def test_calc_jm_dev_matches_reference(cuda, lib):
 
 
 def test_device_feed_chain_matches_host_chain(cuda, lib):
-    """Grid, feed currents and propagation all on the device (config 1 shapes,
+    """Grid, feed currents and propagation all on the device (the feed -> dish workload,
     reduced) equal the host-built chain."""
     import torch
     from pypo_gb300 import beams, configs, engine
