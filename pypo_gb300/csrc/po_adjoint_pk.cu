@@ -290,9 +290,8 @@ __device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const
     const float2 Ph = fma2(dup2(s.sh[2]), r[2], fma2(dup2(s.sh[1]), r[1], mul2(dup2(s.sh[0]), r[0])));
     const float2 Pl = fma2(dup2(s.sl[2]), r[20], fma2(dup2(s.sl[1]), r[19], fma2(dup2(s.sl[0]), r[18],
                       fma2(dup2(s.sh[2]), r[5], fma2(dup2(s.sh[1]), r[4], mul2(dup2(s.sh[0]), r[3]))))));
-    const float2 x = sub2(Ph, sub2(add2(Ph, dup2(12582912.0f)), dup2(12582912.0f)));   // frac(Ph), exact
     float2 sn, cs, tq;
-    ff_phase_sincos2(x, Pl, sn, cs, tq);
+    ff_phase_sincos2(Ph, Pl, sn, cs, tq);
     const float2 ndr = fma2(dup2(s.n[2]), r[20], fma2(dup2(s.n[1]), r[19], mul2(dup2(s.n[0]), r[18])));
     const float2 one = flip_parity(dup2(1.0f), tq);
     const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);

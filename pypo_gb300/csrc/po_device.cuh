@@ -144,34 +144,40 @@ __device__ __forceinline__ void sincos_reduced2(float2 y, float2 &sn, float2 &cs
 #endif
 }
 
-// Far-field phase 2 pi (x + p) in turns, x = frac(hi projection) exact with
-// |x| <= 1/2, p the small lo projection: in half turns 2x + 2p, q = rint of
-// its rounded value, y = (2x - q) + 2p with 2x - q exact. sin/cos up to
-// (-1)^q, q's parity in t as for phase_sincos2.
-__device__ __forceinline__ void ff_phase_sincos2(float2 x, float2 p, float2 &sn, float2 &cs, float2 &t)
+// Far-field phase 2 pi (P + p) in turns, P the exact hi projection (|P| below
+// 2^21), p the lo projection. In half turns: q1 = rint(2P) from one fma
+// against 1.5*2^23, x = 2P - q1 exact (Sterbenz, |x| <= 1/2); y1 = x + 2p
+// rounded once; q2 = rint(y1), y = y1 - q2 exact, so |y| <= 1/2 for any
+// size of p. sin/cos up to (-1)^(q1 + q2); the parity of q1 + q2 is the low
+// bit of t (t1's bits with t2's low bit xor-ed in, one logic op a lane).
+__device__ __forceinline__ void ff_phase_sincos2(float2 P, float2 p, float2 &sn, float2 &cs, float2 &t)
 {
-    const float2 two = dup2(2.0f);
-    t = add2(fma2(p, two, add2(x, x)), dup2(12582912.0f));
-    const float2 q = sub2(t, dup2(12582912.0f));
-    sincos_reduced2(fma2(p, two, fma2(x, two, neg2(q))), sn, cs);
+    const float2 two = dup2(2.0f), magic = dup2(12582912.0f);
+    const float2 t1 = fma2(P, two, magic);
+    const float2 y1 = fma2(p, two, fma2(P, two, neg2(sub2(t1, magic))));
+    const float2 t2 = add2(y1, magic);
+    sincos_reduced2(sub2(y1, sub2(t2, magic)), sn, cs);
+    t = make_float2(__uint_as_float(__float_as_uint(t1.x) ^ (__float_as_uint(t2.x) & 1u)),
+                    __uint_as_float(__float_as_uint(t1.y) ^ (__float_as_uint(t2.y) & 1u)));
 }
 
 // Phase of a pair from the split separation, and its sin/cos up to (-1)^q.
 // R^2 = S0 + S1 (S0 exact, S1 small), Rh = R^2 rinv0 ~ R (turns). The
 // residual res = (S0 - Rh^2) + S1 gives R = Rh + res / (2 Rh); the fma
 // rounds S0 - Rh^2 once, an error of ~2^-47 R turns. In half turns,
-// 2R = 2 Rh + res rinv0: q = rint(2R) is taken from a rounded 2R (good to
-// +-1 near the half-way points, which only moves y to the other end of its
-// range), y = (2 Rh - q) + res rinv0 with 2 Rh - q exact (Sterbenz), so
-// |y| <= 1/2 plus a rounding for any R below 2^21 turns.
+// 2R = 2 Rh + res rinv0: q = rint(2 Rh) from one fma against 1.5*2^23,
+// y = (2 Rh - q) + res rinv0 with 2 Rh - q exact (Sterbenz). |y| <= 1/2 +
+// |res rinv0|, and |res rinv0| ~ 2 |R - Rh| <= 2^-22 R from the rsqrt
+// estimate: below 0.03 for R up to 2e5 turns, where both the hardware
+// sin/cos and the polynomials (error 3e-8 at |y| = 0.52) are still exact
+// to FP32 level. R below 2^21 turns.
 __device__ __forceinline__ void phase_sincos2(float2 S0, float2 S1, float2 Rh, float2 rinv0, float2 &sn, float2 &cs,
                                               float2 &t)
 {
+    const float2 two = dup2(2.0f), magic = dup2(12582912.0f);
     const float2 res = add2(fma2(neg2(Rh), Rh, S0), S1);
-    const float2 two_r = fma2(res, rinv0, add2(Rh, Rh));
-    t = add2(two_r, dup2(12582912.0f));
-    const float2 q = sub2(t, dup2(12582912.0f));
-    sincos_reduced2(fma2(res, rinv0, fma2(Rh, dup2(2.0f), neg2(q))), sn, cs);
+    t = fma2(Rh, two, magic);
+    sincos_reduced2(fma2(res, rinv0, fma2(Rh, two, neg2(sub2(t, magic)))), sn, cs);
 }
 
 }  // namespace po

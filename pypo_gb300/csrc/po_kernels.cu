@@ -134,9 +134,8 @@ __device__ __forceinline__ void ff_pair2(float2 *acc, const float2 *tc, const fl
     const float2 Ph = fma2(r[2], tc[2], fma2(r[1], tc[1], mul2(r[0], tc[0])));
     const float2 Pl = fma2(r[5], tc[8], fma2(r[4], tc[7], fma2(r[3], tc[6], fma2(r[2], tc[5],
                       fma2(r[1], tc[4], mul2(r[0], tc[3]))))));
-    const float2 x = sub2(Ph, sub2(add2(Ph, dup2(12582912.0f)), dup2(12582912.0f)));   // frac(Ph), exact
     float2 sn, cs, tq;
-    ff_phase_sincos2(x, Pl, sn, cs, tq);
+    ff_phase_sincos2(Ph, Pl, sn, cs, tq);
     const float2 ndr = fma2(r[8], tc[8], fma2(r[7], tc[7], mul2(r[6], tc[6])));
     // G = e^{-t j theta}; (-1)^q and the illumination mask in one per-lane factor
     const float2 one = flip_parity(dup2(1.0f), tq);
