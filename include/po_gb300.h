@@ -172,8 +172,9 @@ int po_calc_jm_dev(long n, const double *grid7, const double *fields, int mode, 
  * The sums behind Efficiencies.py calcSpillover / calcTaper / calcXpol /
  * calcMainBeam (Efficiencies.py:90-177) over the n points of a device grid
  * (7 rows; x, y and area are read), for one field component f (device rows
- * f_re, f_im) and an optional second one g (cross-polar or fitted Gaussian;
- * NULL, NULL if unused). Aperture (_generateMask, Efficiencies.py:11-41):
+ * f_re, f_im; f_im NULL for a real f) and an optional second one g (cross-polar or fitted Gaussian;
+ * NULL, NULL if unused; g_im NULL alone for a real g such as a fitted
+ * Gaussian). Aperture (_generateMask, Efficiencies.py:11-41):
  * shape 0 none, 1 ellipse (aperture = cx, cy, outer_x, outer_y), 2 rectangle
  * (cx, cy, x_lo, x_hi, y_lo, y_hi relative to the centre); host memory.
  * Writes 10 doubles to the device buffer `sums`: sum |f|^2 A, then over the
@@ -182,6 +183,36 @@ int po_calc_jm_dev(long n, const double *grid7, const double *fields, int mode, 
  * deterministic. */
 int po_efficiency_sums_dev(long n, const double *grid7, const double *f_re, const double *f_im, const double *g_re,
                            const double *g_im, int shape, const double *aperture, double *sums, void *stream);
+
+/* ---- Gaussian beam fit on the device ---------------------------------------
+ * po_fit_gauss_abs_dev: FitGauss.py fitGaussAbs (:67-163) as System.fitGaussAbs
+ * and System.calcMainBeam call it (System.py:1828-1906), on the ncx x ncy
+ * points of a device grid made without transform or spherical mapping (7
+ * rows as above; x and y are read) and the field component f (device rows
+ * f_re, f_im; f_im NULL for a real amplitude). thres in dB (the reference's
+ * default is -11), scale as the reference's Scales (0 LIN, 2 dB; 1 AMP has
+ * no Gaussian in the reference and is rejected). use_ratio = 0 is ratio
+ * None; otherwise the fit is repeated with a rising threshold until the
+ * fitted power over the pattern's falls below `ratio` (FitGauss.py:126-161).
+ * Writes the 6 parameters (x0, y0, xs, ys, theta, amp) to host memory
+ * `popt`, and where p0 is not NULL the simplex's starting point there (the
+ * image-moment estimates of calcEstimates, FitGauss.py:13-65, and the
+ * pattern's maximum as amp). Synchronises `stream` once per objective value. Status 4: the
+ * ratio rounds would repeat for ever (the reference never returns there).
+ * po_generate_gauss_dev: generateGauss (FitGauss.py:197-228) of host
+ * parameters popt on the n points of a device grid into the device buffer
+ * out (n doubles), scale 0 LIN or 2 dB; queued on `stream`.
+ * po_fmin: the downhill-simplex minimiser behind both, scipy.optimize.fmin's
+ * method (FitGauss.py:128, :150), with a host objective f(x, &fx, ctx)
+ * returning 0 (a non-zero return aborts with that status). maxiter or maxfun
+ * <= 0 stands for None (the default 200 n). Writes xopt (n), and fopt,
+ * iterations and function calls where those pointers are not NULL. */
+typedef int (*po_objective)(const double *x, double *fx, void *ctx);
+int po_fit_gauss_abs_dev(int ncx, int ncy, const double *grid7, const double *f_re, const double *f_im, double thres,
+                         int scale, int use_ratio, double ratio, double *popt, double *p0, void *stream);
+int po_generate_gauss_dev(long n, const double *grid7, const double *popt, int scale, double *out, void *stream);
+int po_fmin(int n, const double *x0, double xtol, double ftol, long maxiter, long maxfun, po_objective f, void *ctx,
+            double *xopt, double *fopt, long *iterations, long *fcalls);
 
 /* ---- explicit-grid, double-precision entry (host buffers) ---------------
  * New; the reference has no equivalent (its C-ABI regenerates grids inside

@@ -12,10 +12,14 @@ LIB_PATH = pathlib.Path(__file__).resolve().parent / "libpo_gb300.so"
 
 #: every symbol declared in include/po_gb300.h
 EXPORTS = ("po_last_error", "po_n_out", "po_last_launches", "po_generate_grid", "po_generate_grid_dev", "po_gauss_beam_dev", "po_calc_jm_dev",
-           "po_efficiency_sums_dev", "po_run_d",
+           "po_efficiency_sums_dev", "po_fit_gauss_abs_dev", "po_generate_gauss_dev", "po_fmin", "po_run_d",
            "po_run_dev", "po_run_dev_static", "po_adjoint_dev", "po_adjoint_d", "po_device_error", "po_timing_enable", "po_timing_collect", "po_fp32_probe",
            "callKernelf_JM", "callKernelf_EH", "callKernelf_JMEH", "callKernelf_EHP",
            "callKernelf_FF", "callKernelf_scalar")
+
+#: po_objective: int f(const double *x, double *fx, void *ctx)
+OBJECTIVE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                             ctypes.c_void_p)
 
 MODE_ID = {"JM": 0, "EH": 1, "JMEH": 2, "EHP": 3, "FF": 4, "scalar": 5}
 
@@ -59,6 +63,14 @@ def load():
     lib.po_efficiency_sums_dev.restype = c_int
     lib.po_efficiency_sums_dev.argtypes = [c_long, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
                                            c_void_p, c_void_p]
+    lib.po_fit_gauss_abs_dev.restype = c_int
+    lib.po_fit_gauss_abs_dev.argtypes = [c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int,
+                                         c_double, c_void_p, c_void_p, c_void_p]
+    lib.po_generate_gauss_dev.restype = c_int
+    lib.po_generate_gauss_dev.argtypes = [c_long, c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+    lib.po_fmin.restype = c_int
+    lib.po_fmin.argtypes = [c_int, c_void_p, c_double, c_double, c_long, c_long, OBJECTIVE, c_void_p, c_void_p,
+                            c_void_p, c_void_p, c_void_p]
     lib.po_run_d.restype = c_int
     lib.po_run_d.argtypes = [c_int, c_long, c_void_p, c_int, c_int, c_int, c_void_p, c_long, c_void_p,
                              c_double, c_double, c_double, c_int, c_void_p]

@@ -15,7 +15,7 @@ INCLUDE = HERE.parent / "include"
 LIB = HERE / "libpo_gb300.so"
 BUILD = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["po_kernels.cu", "po_adjoint.cu", "po_adjoint_pk.cu", "po_engine.cu", "po_capi.cu", "po_grid.cpp", "po_grid_dev.cu", "po_sources_dev.cu", "po_eff_dev.cu", "po_noalloc.cu"]
+SOURCES = ["po_kernels.cu", "po_adjoint.cu", "po_adjoint_pk.cu", "po_engine.cu", "po_capi.cu", "po_grid.cpp", "po_grid_dev.cu", "po_sources_dev.cu", "po_eff_dev.cu", "po_noalloc.cu", "po_fmin.cpp", "po_fitgauss_dev.cu"]
 
 
 def nvcc():
@@ -27,7 +27,7 @@ def nvcc():
 
 def _compile(src, verbose=False, defines=(), build_dir=None):
     obj = (build_dir or BUILD) / (src + ".o")
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off",
            *[f"-D{d}" for d in defines], "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
     if verbose and src.endswith(".cu"):
         cmd.insert(1, "-Xptxas=-v")

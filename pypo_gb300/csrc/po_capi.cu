@@ -251,6 +251,32 @@ int po_efficiency_sums_dev(long n, const double *grid7, const double *f_re, cons
                                    static_cast<cudaStream_t>(stream));
 }
 
+int po_fit_gauss_abs_dev(int ncx, int ncy, const double *grid7, const double *f_re, const double *f_im, double thres,
+                         int scale, int use_ratio, double ratio, double *popt, double *p0, void *stream)
+{
+    po::clear_error();
+    return po::fit_gauss_abs_dev(ncx, ncy, grid7, f_re, f_im, thres, scale, use_ratio, ratio, popt, p0,
+                                 static_cast<cudaStream_t>(stream));
+}
+
+int po_generate_gauss_dev(long n, const double *grid7, const double *popt, int scale, double *out, void *stream)
+{
+    po::clear_error();
+    return po::generate_gauss_dev(n, grid7, popt, scale, out, static_cast<cudaStream_t>(stream));
+}
+
+int po_fmin(int n, const double *x0, double xtol, double ftol, long maxiter, long maxfun, po_objective f, void *ctx,
+            double *xopt, double *fopt, long *iterations, long *fcalls)
+{
+    po::clear_error();
+    if (!f) return po::fail(1, "fmin: null objective");
+    const po::Objective obj = [&](const double *x, double *fx) {
+        const int rc = f(x, fx, ctx);
+        return rc == 0 ? 0 : po::fail(rc, "fmin: the objective returned a non-zero status");
+    };
+    return po::fmin_nm(n, x0, xtol, ftol, maxiter, maxfun, obj, xopt, fopt, iterations, fcalls);
+}
+
 int po_run_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
              const double *tgt7, double k, double epsilon, double t_direction, int precision, double *out)
 {

@@ -50,13 +50,14 @@ po_eff_partial_kernel(long n, const double *__restrict__ g7, const double *__res
     double s[kEffSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const double x = g7[i], y = g7[n + i], A = g7[6 * n + i];
-        const double re = fr[i], im = fi[i];
+        const double re = fr[i], im = fi ? fi[i] : 0.0;
         const double f2 = re * re + im * im;
         s[0] += f2 * A;
         s[5] += f2;
         s[7] = fmax(s[7], f2);
         if (gr) {
-            const double g2 = gr[i] * gr[i] + gi[i] * gi[i];
+            const double gim = gi ? gi[i] : 0.0;
+            const double g2 = gr[i] * gr[i] + gim * gim;
             s[6] += g2;
             s[8] = fmax(s[8], g2);
         }
@@ -99,8 +100,8 @@ int efficiency_sums_dev(long n, const double *g7, const double *fr, const double
 {
     if (n < 0) return fail(1, "negative point count");
     if (!sums) return fail(1, "null output buffer");
-    if (n > 0 && (!g7 || !fr || !fi)) return fail(1, "null grid or field");
-    if ((gr == nullptr) != (gi == nullptr)) return fail(1, "second field needs both real and imaginary rows");
+    if (n > 0 && (!g7 || !fr)) return fail(1, "null grid or field");
+    if (!gr && gi) return fail(1, "second field: imaginary row without a real row");
     if (shape < 0 || shape > 2) return fail(1, "aperture shape must be 0 (none), 1 (ellipse) or 2 (rectangle)");
     if (shape != 0 && !aper) return fail(1, "null aperture parameters");
     Aperture ap{};

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <string>
 
 #include "../../include/po_gb300.h"
@@ -66,6 +67,17 @@ int calc_jm_dev(long n, const double *g7, const double *fields, int mode, double
 // Efficiency sums on the device (po_eff_dev.cu).
 int efficiency_sums_dev(long n, const double *g7, const double *fr, const double *fi, const double *gr,
                         const double *gi, int shape, const double *aper, double *sums, cudaStream_t s);
+
+// Downhill-simplex minimiser (po_fmin.cpp). The objective writes f(x) and
+// returns 0, or a non-zero status that aborts the minimisation.
+using Objective = std::function<int(const double *x, double *fx)>;
+int fmin_nm(int n, const double *x0, double xatol, double fatol, long maxiter, long maxfun, const Objective &func,
+            double *xopt, double *fopt, long *nit, long *nfev);
+
+// Gaussian beam fit on the device (po_fitgauss_dev.cu).
+int fit_gauss_abs_dev(int ncx, int ncy, const double *g7, const double *fr, const double *fi, double thres,
+                      int scale, int use_ratio, double ratio, double *popt, double *p0, cudaStream_t s);
+int generate_gauss_dev(long n, const double *g7, const double *popt, int scale, double *out, cudaStream_t s);
 
 }  // namespace po
 

@@ -9,7 +9,7 @@ vector Gaussian feed (makeGaussBeam). Outputs go to golden_*.npz beside this
 script. Needs the reference sources (this container); the fixtures then
 travel without them.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--only-calcjm | --only-eff | --only-fitgauss]
 """
 import json
 import pathlib
@@ -104,6 +104,110 @@ def efficiencies(ref):
     print("wrote efficiencies", {k: v for k, v in out.items() if np.ndim(v) == 0 and not isinstance(v, str)})
 
 
+def fitgauss(ref):
+    """The reference's own FitGauss.fitGaussAbs (and System.calcMainBeam's use
+    of it) on seeded beam patterns, with its grid binding served by the
+    reference's compiled generateGrid (reshaped to the grid, as its binding
+    returns it). Cases: an offset rotated Gaussian with phase noise on the
+    reference's 13x13 test plane; a centred one at the reference test's
+    -100 dB threshold; an elliptical Airy pattern on a 61x61 far-field grid;
+    a peak narrower than the grid spacing (empty fit window, the fallback to
+    grid row 1) on an xy grid and on a uv grid. Error cases are recorded as expectations: the offset
+    Gaussian at -100 dB (IndexError in the reference) and the narrow peak
+    with a ratio (the reference's ratio loop never ends)."""
+    import signal
+    from scipy.special import j1
+    sys.path.insert(0, "/root/reference/src")
+    import PyPO.Efficiencies as E
+    import PyPO.FitGauss as FG
+    from PyPO.Enums import Scales
+
+    class Grid:
+        pass
+
+    def generate(refl, transform=True, spheric=True):
+        b = ref.grid(refl, transform, spheric)
+        shp = tuple(int(v) for v in refl["gridsize"])
+        g = Grid()
+        g.x, g.y, g.z, g.area = (b[k].reshape(shp) for k in (0, 1, 2, 6))
+        return g
+
+    FG.BRefl.generateGrid = generate
+
+    def beam(g, xs, ys, wx, wy, th, kind):
+        c, s = np.cos(th), np.sin(th)
+        u = ((g.x - xs) * c + (g.y - ys) * s) / wx
+        v = (-(g.x - xs) * s + (g.y - ys) * c) / wy
+        r = np.sqrt(u * u + v * v)
+        if kind == "gauss":
+            return np.exp(-r * r / 2)
+        r = np.where(r == 0, 1e-30, r)
+        return np.abs(2 * j1(r) / r)
+
+    rng = np.random.default_rng(5)
+    pl13 = SF.plane([13, 13], gmode=0, lims_a=[-1.0, 1.0])
+    g13 = generate(pl13, False, False)
+    gauss_xy = beam(g13, 0.1, -0.15, 0.35, 0.25, 0.4, "gauss") * np.exp(1j * rng.normal(0, 0.2, g13.x.shape)) \
+        + 1e-3 * rng.standard_normal(g13.x.shape)
+    centred = beam(g13, 0.0, 0.0, 0.3, 0.4, 0.0, "gauss").astype(complex)
+    ff = SF.farfield([61, 61], [-0.5, 0.5], [-0.5, 0.5])
+    gff = generate(ff, False, False)
+    airy = beam(gff, 0.03, -0.02, 0.045, 0.06, 0.3, "airy") * np.exp(1j * rng.normal(0, 0.1, gff.x.shape))
+    pl15 = SF.plane([15, 15], gmode=0, lims_a=[-1.0, 1.0])
+    narrow = (beam(generate(pl15, False, False), 0.0, 0.0, 0.02, 0.02, 0.0, "gauss") + 0.05).astype(complex)
+    # on a uv grid the fallback's row 1 is a ring, where x and y both vary
+    uv = SF.plane([15, 16], gmode=1, lims_a=[0.05, 1.0])
+    guv = generate(uv, False, False)
+    ring = 0.05 + 0.01 * np.cos(3 * np.arctan2(guv.y, guv.x)) + 0.02 * guv.x
+    narrow_uv = (ring + np.where((np.arange(guv.x.size) == 9 * 16 + 5).reshape(guv.x.shape), 1.0, 0.0)).astype(complex)
+
+    out = {}
+    every = [(sid, t, r) for sid in (0, 2) for t in (-11.0, -25.0) for r in (None, 1.0)]
+    # (the centred dB fit at -100 dB with a ratio, and the narrow peak with
+    # one, never end in the reference: recorded below, not run)
+    runs = [("gauss_xy", pl13, gauss_xy, every),
+            ("centred_xy", pl13, centred, [(0, -100.0, None), (0, -100.0, 1.0), (2, -100.0, None)]),
+            ("airy_ff", ff, airy, every),
+            ("narrow_xy", pl15, narrow, [(0, -11.0, None), (2, -11.0, None)]),
+            ("narrow_uv", uv, narrow_uv, [(0, -11.0, None), (2, -11.0, None)])]
+    scales = {0: Scales.LIN, 2: Scales.dB}
+    for name, surf, field, combos in runs:
+        g = generate(surf, False, False)
+        out[name + "__surface_json"] = dict_to_json(surf)
+        out[name + "__field"] = field
+        out[name + "__x"], out[name + "__y"] = g.x, g.y
+        for sid, thres, ratio in combos:
+            key = f"{name}__s{sid}__t{thres:g}__r{'none' if ratio is None else f'{ratio:g}'}"
+            out[key] = FG.fitGaussAbs(np.abs(field), surf, thres, scales[sid], ratio)
+    # System.calcMainBeam (System.py:1886-1908): fit at ratio 1, Gaussian in LIN, efficiency
+    for scale, sid in ((Scales.LIN, 0), (Scales.dB, 2)):
+        popt = FG.fitGaussAbs(np.abs(airy), ff, -11.0, scale, 1)
+        psi = FG.generateGauss(popt, ff, scale=Scales.LIN)
+        out[f"airy_ff__mainbeam_s{sid}"] = E.calcMainBeam(airy, ff, psi)
+    # expected failures
+    try:
+        FG.fitGaussAbs(np.abs(gauss_xy), pl13, -100.0, Scales.LIN, None)
+        raise SystemExit("expected the reference to raise IndexError")
+    except IndexError as e:
+        out["gauss_xy__t-100__error"] = str(e)
+
+    def _alarm(*_):
+        raise TimeoutError
+
+    signal.signal(signal.SIGALRM, _alarm)
+    signal.alarm(20)
+    try:
+        FG.fitGaussAbs(np.abs(narrow), pl15, -11.0, Scales.LIN, 1)
+        raise SystemExit("expected the reference's ratio loop not to end")
+    except TimeoutError:
+        out["narrow_xy__ratio_loop"] = "no end within 20 s (the threshold stops at -3 dB and every round repeats)"
+        out["centred_xy__s2__t-100__r1__loop"] = "the same: no end (24,578 rounds in 120 s with oracle/fitgauss.py, which follows it)"
+    finally:
+        signal.alarm(0)
+    np.savez_compressed(HERE / "golden_fitgauss.npz", **out)
+    print("wrote fitgauss", len(out), "entries")
+
+
 def main():
     if not O.REF_PATH.exists():
         subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
@@ -114,8 +218,12 @@ def main():
     if "--only-eff" in sys.argv:
         efficiencies(ref)
         return
+    if "--only-fitgauss" in sys.argv:
+        fitgauss(ref)
+        return
     calcjm(ref)
     efficiencies(ref)
+    fitgauss(ref)
     rng = np.random.default_rng(20261203)
     k = 2 * np.pi / 0.7
     for name, src, tgt, modes in cases():

@@ -42,4 +42,7 @@ def test_device_efficiency_rejects_bad_arguments(cuda, lib):
     p = lambda t: ctypes.c_void_p(t.data_ptr())
     assert lib.po_efficiency_sums_dev(4, p(g7), p(g7), p(g7), None, None, 5, None, p(sums), st) != 0
     assert b"shape" in lib.po_last_error()
-    assert lib.po_efficiency_sums_dev(4, p(g7), p(g7), p(g7), p(g7), None, 0, None, p(sums), st) != 0
+    assert lib.po_efficiency_sums_dev(4, p(g7), p(g7), p(g7), None, p(g7), 0, None, p(sums), st) != 0
+    assert b"imaginary row without a real row" in lib.po_last_error()
+    # a real second field (a fitted Gaussian) needs no imaginary row
+    assert lib.po_efficiency_sums_dev(4, p(g7), p(g7), p(g7), p(g7), None, 0, None, p(sums), st) == 0

@@ -1,0 +1,196 @@
+"""Gaussian beam fit on the device against the reference's own fits
+(tests/golden/golden_fitgauss.npz, from the reference's FitGauss.py) and the
+oracle restatement (oracle/fitgauss.py), on the same grids and fields."""
+import pathlib
+
+import numpy as np
+import pytest
+
+from oracle import fitgauss as OF
+
+pytestmark = [pytest.mark.gpu, pytest.mark.filterwarnings("ignore::RuntimeWarning")]
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "golden_fitgauss.npz"
+
+# Device sums and numpy's pairwise sums differ in the last bits, and so do the
+# device's and numpy's exp and log10, so the simplex's path can part from the
+# reference's near convergence; in LIN the fitted shape (x0, y0, xs, ys,
+# theta) then still agrees far inside the simplex's own stopping tolerance
+# (1e-4 absolute; measured on a GB300: 2e-6 relative at most). amp (index 5)
+# is never read by the misfit (generateGauss ignores it), so the simplex moves
+# it freely and its final value only records the path: not compared. In dB
+# the reference's misfit is flat along the beam's scale (see
+# test_fitgauss.py), so a dB fit is checked through its start point and
+# the misfit it reaches from there.
+SHAPE = slice(0, 5)
+RTOL, ATOL = 1e-5, 1e-7
+
+
+def _golden():
+    return np.load(GOLDEN)
+
+
+def _device_case(name):
+    import torch
+    g = _golden()
+    field, x, y = g[name + "__field"], g[name + "__x"], g[name + "__y"]
+    ncx, ncy = field.shape
+    g7 = torch.zeros((7, ncx * ncy), dtype=torch.float64)
+    g7[0], g7[1] = torch.from_numpy(x.ravel()), torch.from_numpy(y.ravel())
+    f12 = torch.zeros((12, ncx * ncy), dtype=torch.float64)
+    f12[0], f12[3] = torch.from_numpy(field.real.ravel()), torch.from_numpy(field.imag.ravel())
+    return g7.cuda(), f12.cuda(), ncx, ncy, field, x, y
+
+
+def _keys():
+    g = _golden()
+    return sorted(k for k in g.files if "__s" in k and "__r" in k and not k.endswith("__loop")
+                  and not k.startswith("narrow_xy"))
+
+
+def _parse(key):
+    name, s, t, r = key.split("__")
+    return name, int(s[1:]), float(t[1:]), None if r == "rnone" else float(r[1:])
+
+
+@pytest.mark.parametrize("key", [k for k in _keys() if "__s0__" in k])
+def test_device_lin_fit_matches_reference(key):
+    from pypo_gb300 import fitgauss as FG
+    name, scale, thres, ratio = _parse(key)
+    g7, f12, ncx, ncy, *_ = _device_case(name)
+    popt = FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, thres, scale, ratio)
+    np.testing.assert_allclose(popt[SHAPE], _golden()[key][SHAPE], rtol=RTOL, atol=ATOL)
+
+
+@pytest.mark.parametrize("key", _keys())
+def test_device_start_point_matches_oracle(key):
+    """The fit region and its moment estimates, closed-form and well
+    conditioned in both scales."""
+    from pypo_gb300 import fitgauss as FG
+    name, scale, thres, ratio = _parse(key)
+    g7, f12, ncx, ncy, field, x, y = _device_case(name)
+    _, p0 = FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, thres, scale, ratio, full_output=True)
+    ref = OF.start_point(np.abs(field), x, y, thres, scale)
+    np.testing.assert_allclose(p0, ref, rtol=1e-10, atol=1e-13)
+
+
+@pytest.mark.parametrize("key", [k for k in _keys() if "__s2__" in k and k.endswith("__rnone")])
+def test_device_db_fit_improves_on_its_start(key):
+    """dB: the simplex's end point depends on its path (the misfit is flat
+    along the beam's scale, and in these cases the simplex also stops in
+    other shallow places), so the reference's own end point is not a target;
+    the fit must lower the misfit from the shared start."""
+    from pypo_gb300 import fitgauss as FG
+    name, scale, thres, ratio = _parse(key)
+    g7, f12, ncx, ncy, field, x, y = _device_case(name)
+    popt, p0 = FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, thres, scale, ratio, full_output=True)
+    pat, sel = OF.fit_region(field, x, y, thres, scale)
+    ours, start = OF.misfit(popt, x, y, pat, sel, scale), OF.misfit(p0, x, y, pat, sel, scale)
+    assert np.isfinite(ours) and ours <= start
+
+
+@pytest.mark.parametrize("key", [k for k in _keys() if "__s2__" in k and not k.endswith("__rnone")])
+def test_device_db_fit_with_ratio_completes(key):
+    """dB with ratio rounds: each round's misfit is flat along the beam's
+    scale, and the scale decides the power ratio that ends the rounds, so the
+    rounds themselves follow the path; the fit runs to its end with finite
+    parameters."""
+    from pypo_gb300 import fitgauss as FG
+    name, scale, thres, ratio = _parse(key)
+    g7, f12, ncx, ncy, *_ = _device_case(name)
+    popt = FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, thres, scale, ratio)
+    assert np.all(np.isfinite(popt))
+
+
+def test_device_fit_of_a_real_amplitude_equals_the_complex_component():
+    """System.fitGaussAbs passes |E_c|; a real amplitude row gives the same fit."""
+    from pypo_gb300 import fitgauss as FG
+    g7, f12, ncx, ncy, field, *_ = _device_case("airy_ff")
+    amp = f12.new_tensor(np.abs(field).ravel())
+    a = FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, -11.0, "LIN", 1.0)
+    b = FG.fit_gauss_abs_dev(g7, ncx, ncy, amp, None, -11.0, "LIN", 1.0)
+    np.testing.assert_allclose(b[SHAPE], a[SHAPE], rtol=RTOL, atol=ATOL)
+
+
+def test_device_fit_is_deterministic():
+    from pypo_gb300 import fitgauss as FG
+    g7, f12, ncx, ncy, *_ = _device_case("airy_ff")
+    a = FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, -11.0, "dB", 1.0)
+    b = FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, -11.0, "dB", 1.0)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_device_main_beam_matches_reference():
+    """System.calcMainBeam with its default LIN scale (a dB fit's scale, and so
+    its main-beam efficiency, is not determined by the pattern)."""
+    from pypo_gb300 import fitgauss as FG
+    g7, f12, ncx, ncy, *_ = _device_case("airy_ff")
+    eff = FG.calc_main_beam_dev(g7, ncx, ncy, f12, 0, -11.0, "LIN")
+    assert eff == pytest.approx(float(_golden()["airy_ff__mainbeam_s0"]), rel=1e-5)
+
+
+@pytest.mark.parametrize("scale", [0, 2])
+def test_device_gaussian_matches_oracle(scale):
+    from pypo_gb300 import fitgauss as FG
+    g7, _, ncx, ncy, _, x, y = _device_case("airy_ff")
+    p = np.array([0.11, 0.08, 0.03, -0.02, 1.86, 1.0])
+    psi = FG.generate_gauss_dev(g7, p, scale).cpu().numpy()
+    ref = OF.gaussian(p, x, y, scale).ravel()
+    np.testing.assert_allclose(psi, ref, rtol=1e-13, atol=1e-13 * np.max(np.abs(ref)))
+
+
+def test_window_past_the_grid_is_an_error_as_in_the_reference():
+    from pypo_gb300 import fitgauss as FG
+    from pypo_gb300._lib import POError
+    assert "out of bounds" in str(_golden()["gauss_xy__t-100__error"])
+    g7, f12, ncx, ncy, *_ = _device_case("gauss_xy")
+    with pytest.raises(POError, match="IndexError"):
+        FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, -100.0, "LIN", None)
+
+
+def test_ratio_rounds_that_never_end_in_the_reference_are_an_error():
+    from pypo_gb300 import fitgauss as FG
+    from pypo_gb300._lib import POError
+    assert "no end" in str(_golden()["narrow_xy__ratio_loop"])
+    g7, f12, ncx, ncy, *_ = _device_case("narrow_xy")
+    with pytest.raises(POError, match="status 4"):
+        FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, -11.0, "LIN", 1.0)
+
+
+def test_invalid_fit_arguments():
+    import torch
+    from pypo_gb300 import fitgauss as FG
+    from pypo_gb300._lib import POError
+    g7, f12, ncx, ncy, *_ = _device_case("gauss_xy")
+    with pytest.raises(POError, match="AMP"):
+        FG.fit_gauss_abs_dev(g7, ncx, ncy, f12, 0, -11.0, "AMP", None)
+    with pytest.raises(POError, match="zero"):
+        FG.fit_gauss_abs_dev(g7, ncx, ncy, torch.zeros_like(f12), 0, -11.0, "LIN", None)
+    with pytest.raises(ValueError):
+        FG.fit_gauss_abs_dev(g7, ncx + 1, ncy, f12, 0, -11.0, "LIN", None)
+
+
+def test_dish_far_field_fitted_on_the_device(cuda):
+    """The chain kept on the device: a dish's far field (FF) on directions
+    generated on the device, then its Gaussian fit and main-beam efficiency,
+    with no host copy in between; checked against the oracle on the same
+    field and grid read back afterwards."""
+    import torch
+    from pypo_gb300 import configs, engine, fitgauss as FG
+    from pypo_gb300 import surfaces as SF
+    src = SF.paraboloid(80.0, [40, 40], gmode=1, lims_a=[0.0, 100.0])
+    ff = SF.farfield([41, 41], [-1.5, 1.5], [-1.5, 1.5])
+    s7 = engine.generate_grid_dev(src, device=cuda)
+    t7 = engine.generate_grid_dev(ff, device=cuda)                                 # (polar, azimuth)
+    g7 = engine.generate_grid_dev(ff, transform=False, spheric=False, device=cuda)   # (az, el) degrees
+    cur = torch.tensor(configs.tapered_currents(s7.cpu().numpy(), 100.0), device=cuda)
+    out = engine.propagate_dev("FF", s7, cur, 1, 40, 40, t7, 2 * np.pi / 1.0, m_zero=True)
+    popt = FG.fit_gauss_abs_dev(g7, 41, 41, out, 0)
+    eff = FG.calc_main_beam_dev(g7, 41, 41, out, 0)
+    e = out.cpu().numpy()
+    field = (e[0] + 1j * e[3]).reshape(41, 41)
+    x, y = (g7[r].cpu().numpy().reshape(41, 41) for r in (0, 1))
+    ref = OF.fit_gauss_abs(np.abs(field), x, y, -11.0, OF.LIN, 1.0)
+    np.testing.assert_allclose(popt[SHAPE], ref[SHAPE], rtol=RTOL, atol=ATOL)
+    assert eff == pytest.approx(OF.main_beam(field, OF.gaussian(ref, x, y, OF.LIN)), rel=1e-5)
+    assert 0.05 < eff < 1.5 and 0.02 < abs(popt[0]) < 1.0   # a main lobe of a few tenths of a degree

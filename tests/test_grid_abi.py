@@ -18,6 +18,7 @@ HEADER = ROOT / "include" / "po_gb300.h"
 def declared_functions():
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"^\s*typedef\b[^;]*;", "", text, flags=re.M)   # function-pointer types are not entry points
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", text, flags=re.M)))
 
 
