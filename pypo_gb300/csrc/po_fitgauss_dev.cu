@@ -11,7 +11,7 @@
 //      it are the fit region (:99-120);
 //   3. initial parameters from the region's image moments (calcEstimates,
 //      FitGauss.py:13-65);
-//   4. a downhill-simplex minimisation (po_fmin.cpp) of the overlap misfit
+//   4. a downhill-simplex minimisation (po_nm.h, scipy's fmin) of the misfit
 //      |1 - (sum f Psi)^2 / (sum f^2 sum Psi^2)| over the region (GaussAbs,
 //      :165-195), Psi the rotated elliptical Gaussian of generateGauss
 //      (:197-228), in the pattern's scale;
@@ -24,8 +24,15 @@
 // of the 7-row device layout). Every pass over the points is one kernel with
 // FP64 per-thread sums, a block tree, and the block partials added in block
 // order by whichever block finishes last (a fixed grid, so each sum is
-// deterministic). The host runs the simplex and the scalar algebra; each
-// objective value is one kernel and one 24-byte read-back.
+// deterministic). The host does the window's run lengths, the moment
+// algebra and the simplex (po_nm.h, the code of po_fmin): its few hundred
+// dependent FP64 operations per step run far faster on the host than on one
+// GPU thread (GB300's FP64 units are few, and a lone thread waits out each
+// latency). The fit region's points are compacted once per minimisation;
+// each launch then evaluates every point the current simplex step may ask
+// for (reflection with its expansion and both contractions; all of a
+// shrink's vertices; the whole initial simplex), so a step costs one round
+// trip. A point's sums do not depend on the batch it is in.
 //
 // Kept from the reference on purpose, with their effects:
 //   * the window's corners are read as x[min(cols), i0], x[max(cols), i0],
@@ -35,7 +42,8 @@
 //     an error, as numpy's are;
 //   * an empty window region falls back to an integer array of ones used as
 //     an index, which selects grid row 1 (repeated; the repetition cancels
-//     in every ratio), so the fit then runs on row 1;
+//     in every ratio), so the fit then runs on row 1 (on an xy grid x is
+//     constant along a row and that fit is decided by rounding residue);
 //   * the ratio rounds use the plain mask in round 0 and the windowed one
 //     after; a pattern whose ratio never drops below the limit loops for
 //     ever in the reference; here the call returns an error once a round
@@ -48,6 +56,7 @@
 #include <vector>
 
 #include "po_internal.h"
+#include "po_nm.h"
 
 namespace po {
 
@@ -273,24 +282,6 @@ fg_moments_kernel(long n, const double *__restrict__ g7, const double *__restric
     finish_sums<6>(s, part, res, count);
 }
 
-// Overlap sums of the selection: sum f Psi, sum Psi^2, sum f^2.
-__global__ void __launch_bounds__(kFgThreads)
-fg_overlap_kernel(long n, const double *__restrict__ g7, const double *__restrict__ fit,
-                  const unsigned char *__restrict__ sel, Gauss g, int scale, double *part, double *res,
-                  unsigned *count)
-{
-    double s[3] = {0, 0, 0};
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        if (!sel[i]) continue;
-        const double f = fit[i];
-        const double p = gauss_at(g, scale, g7[i], g7[n + i]);
-        s[0] += __dmul_rn(f, p);
-        s[1] += __dmul_rn(p, p);
-        s[2] += __dmul_rn(f, f);
-    }
-    finish_sums<3>(s, part, res, count);
-}
-
 // Power of the linear Gaussian over every point: sum Psi^2.
 __global__ void __launch_bounds__(kFgThreads)
 fg_power_kernel(long n, const double *__restrict__ g7, Gauss g, double *part, double *res, unsigned *count)
@@ -301,6 +292,107 @@ fg_power_kernel(long n, const double *__restrict__ g7, Gauss g, double *part, do
         s[0] += __dmul_rn(p, p);
     }
     finish_sums<1>(s, part, res, count);
+}
+
+// Order-preserving compaction of the selected points into (x, y, pattern)
+// arrays; *count = how many. One CTA; thread t takes a contiguous chunk.
+constexpr int kCompactThreads = 1024;
+
+__global__ void __launch_bounds__(kCompactThreads)
+fg_compact_kernel(long n, const unsigned char *__restrict__ sel, const double *__restrict__ g7,
+                  const double *__restrict__ fit, double *__restrict__ cx, double *__restrict__ cy,
+                  double *__restrict__ cf, long *__restrict__ count)
+{
+    __shared__ long offs[kCompactThreads];
+    const long per = (n + kCompactThreads - 1) / kCompactThreads;
+    const long b = min(n, (long)threadIdx.x * per), e = min(n, b + per);
+    long c = 0;
+    for (long i = b; i < e; ++i) c += sel[i] ? 1 : 0;
+    offs[threadIdx.x] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long acc = 0;
+        for (int t = 0; t < kCompactThreads; ++t) {
+            const long v = offs[t];
+            offs[t] = acc;
+            acc += v;
+        }
+        *count = acc;
+    }
+    __syncthreads();
+    long o = offs[threadIdx.x];
+    for (long i = b; i < e; ++i)
+        if (sel[i]) {
+            cx[o] = g7[i];
+            cy[o] = g7[n + i];
+            cf[o] = fit[i];
+            ++o;
+        }
+}
+
+// Overlap sums of up to kBatch Gaussians over the m compacted points: rows
+// (sum f Psi, sum Psi^2, sum f^2) per Gaussian, the block that finishes last
+// adding the block partials in block order. Each Gaussian's sums follow the
+// same per-thread, per-block and cross-block order whatever else is in the
+// batch.
+constexpr int kBatch = 8;
+
+struct GaussBatch {
+    Gauss g[kBatch];
+    int k;
+};
+
+__global__ void __launch_bounds__(kFgThreads)
+fg_overlap_kernel(const long *__restrict__ count, const double *__restrict__ cx, const double *__restrict__ cy,
+                  const double *__restrict__ cf, int scale, GaussBatch b, double *part, double *res,
+                  unsigned *done)
+{
+    constexpr int kWarps = kFgThreads / 32;
+    __shared__ double ws[3 * kBatch][kWarps];
+    __shared__ bool last;
+    const long m = *count;
+    const int nq = 3 * b.k, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double s[3 * kBatch];
+#pragma unroll
+    for (int q = 0; q < 3 * kBatch; ++q) s[q] = 0.0;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long)gridDim.x * blockDim.x) {
+        const double f = cf[i], x = cx[i], y = cy[i];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) {
+            if (k < b.k) {
+                const double p = gauss_at(b.g[k], scale, x, y);
+                s[3 * k] += __dmul_rn(f, p);
+                s[3 * k + 1] += __dmul_rn(p, p);
+                s[3 * k + 2] += __dmul_rn(f, f);
+            }
+        }
+    }
+    // per warp: a fixed shuffle tree; per block: warps in order
+#pragma unroll
+    for (int q = 0; q < 3 * kBatch; ++q) {
+        if (q < nq) {
+            double v = s[q];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) ws[q][wid] = v;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < nq) {
+        double v = 0.0;
+        for (int w = 0; w < kWarps; ++w) v += ws[threadIdx.x][w];
+        part[(long)blockIdx.x * 3 * kBatch + threadIdx.x] = v;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    if (threadIdx.x < nq) {
+        double v = 0.0;
+        for (unsigned bb = 0; bb < gridDim.x; ++bb) v += __ldcg(&part[(long)bb * 3 * kBatch + threadIdx.x]);
+        res[threadIdx.x] = v;
+    }
+    if (threadIdx.x == 0) *done = 0u;
 }
 
 __global__ void fg_generate_kernel(long n, const double *__restrict__ g7, Gauss g, int scale, double *__restrict__ out)
@@ -320,6 +412,8 @@ bool np_index(long r, long dim, long &out)
 // Scratch of one fit, one allocation.
 struct FitScratch {
     double *a = nullptr, *fit = nullptr, *part = nullptr, *res = nullptr;
+    double *cx = nullptr, *cy = nullptr, *cf = nullptr, *opart = nullptr, *ores = nullptr;
+    long *ncomp = nullptr;
     unsigned char *sel = nullptr, *lines = nullptr;
     unsigned *count = nullptr;
     void *base = nullptr;
@@ -337,7 +431,8 @@ public:
     {
         const size_t nd = (size_t)n_ * sizeof(double);
         const size_t parts = sizeof(double) * kFgBlocks * kFgMaxSums;
-        const size_t bytes = 2 * nd + parts + 256 + 256 + 2 * ((size_t)n_ + 256) + (size_t)ncx_ + ncy_ + 256;
+        const size_t bytes = 5 * (nd + 256) + parts + sizeof(double) * (kFgBlocks + 1) * 3 * kBatch + 8 * 256 +
+                             2 * ((size_t)n_ + 256) + (size_t)ncx_ + ncy_ + 256;
         cudaError_t e = cudaMallocAsync(&sc_.base, bytes, s_);
         if (e != cudaSuccess) return fail(3, std::string("fit scratch: ") + cudaGetErrorString(e));
         char *p = static_cast<char *>(sc_.base);
@@ -351,6 +446,12 @@ public:
         sc_.part = reinterpret_cast<double *>(take(parts));
         sc_.res = reinterpret_cast<double *>(take(sizeof(double) * 8));
         sc_.count = reinterpret_cast<unsigned *>(take(sizeof(unsigned)));
+        sc_.cx = reinterpret_cast<double *>(take(nd));
+        sc_.cy = reinterpret_cast<double *>(take(nd));
+        sc_.cf = reinterpret_cast<double *>(take(nd));
+        sc_.ncomp = reinterpret_cast<long *>(take(sizeof(long)));
+        sc_.opart = reinterpret_cast<double *>(take(sizeof(double) * kFgBlocks * 3 * kBatch));
+        sc_.ores = reinterpret_cast<double *>(take(sizeof(double) * 3 * kBatch));
         sc_.sel = reinterpret_cast<unsigned char *>(take((size_t)n_));
         sc_.lines = reinterpret_cast<unsigned char *>(take((size_t)ncx_ + ncy_));
         e = cudaMemsetAsync(sc_.count, 0, sizeof(unsigned), s_);
@@ -428,16 +529,78 @@ public:
         return read(m6, 6, "moments");
     }
 
-    // GaussAbs (FitGauss.py:165-195) of parameters p over the selection.
-    int misfit(const double *p, int scale, double *eps)
+    // The simplex from p0 over the current selection (fmin(GaussAbs, p0)).
+    int fmin(const double *p0, int scale, double *popt)
     {
-        double h[3];
-        fg_overlap_kernel<<<kFgBlocks, kFgThreads, 0, s_>>>(n_, g7_, sc_.fit, sc_.sel, gauss_of(p), scale, sc_.part,
-                                                             sc_.res, sc_.count);
+        fg_compact_kernel<<<1, kCompactThreads, 0, s_>>>(n_, sc_.sel, g7_, sc_.fit, sc_.cx, sc_.cy, sc_.cf, sc_.ncomp);
         note_launches(1);
-        if (int rc = read(h, 3, "overlap")) return rc;
-        const double c00 = h[0] * h[0] / h[2] / h[1];
-        *eps = std::fabs(1 - std::fabs(c00));
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(2, std::string("fit region compaction: ") + cudaGetErrorString(e));
+        NMState st;
+        nm_init(st, 6, p0, 1e-4, 1e-4, 0, 0);
+        double pts[kBatch][6], val[kBatch];
+        int npts = 0;
+        while (nm_next(st)) {
+            int hit = -1;
+            for (int q = 0; q < npts && hit < 0; ++q) {
+                bool same = true;
+                for (int c = 0; c < 6; ++c) same = same && pts[q][c] == st.x[c];
+                if (same) hit = q;
+            }
+            if (hit < 0) {
+                npts = batch(st, pts);
+                if (int rc = values(scale, pts, npts, val)) return rc;
+                hit = 0;   // the batch starts with the point asked for
+            }
+            nm_feed(st, val[hit]);
+        }
+        for (int c = 0; c < 6; ++c) popt[c] = st.sim[c];
+        return 0;
+    }
+
+    // The point asked for, then the others this step may ask for next.
+    static int batch(const NMState &st, double (*pts)[6])
+    {
+        const int n = st.n;
+        int k = 0;
+        for (int c = 0; c < n; ++c) pts[k][c] = st.x[c];
+        ++k;
+        if (st.phase == nm::kInit) {
+            // st.k is the vertex asked for; the rest of the initial simplex follows
+            for (int v = st.k + 1; v <= n && k < kBatch; ++v, ++k)
+                for (int c = 0; c < n; ++c) pts[k][c] = st.sim[v * n + c];
+        } else if (st.phase == nm::kReflect) {
+            NMState t = st;
+            nm::trial(t, 1.0 + 1.0 * 2.0, -(1.0 * 2.0), pts[k++]);
+            nm::trial(t, 1.0 + 0.5 * 1.0, -(0.5 * 1.0), pts[k++]);
+            nm::trial(t, 1.0 - 0.5, 0.5, pts[k++]);
+        } else if (st.phase == nm::kShrink) {
+            // st.k is the vertex asked for; later vertices move the same way from their old places
+            for (int v = st.k + 1; v <= n && k < kBatch; ++v, ++k)
+                for (int c = 0; c < n; ++c)
+                    pts[k][c] = nm::add(st.sim[c], nm::mul(0.5, nm::sub(st.sim[v * n + c], st.sim[c])));
+        }
+        return k;
+    }
+
+    // GaussAbs (FitGauss.py:165-195) of each point, one launch.
+    int values(int scale, const double (*pts)[6], int k, double *val)
+    {
+        GaussBatch b{};
+        b.k = k;
+        for (int q = 0; q < k; ++q) b.g[q] = gauss_of(pts[q]);
+        fg_overlap_kernel<<<kFgBlocks, kFgThreads, 0, s_>>>(sc_.ncomp, sc_.cx, sc_.cy, sc_.cf, scale, b, sc_.opart,
+                                                             sc_.ores, sc_.count);
+        note_launches(1);
+        double h[3 * kBatch];
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, sc_.ores, sizeof(double) * 3 * k, cudaMemcpyDeviceToHost, s_);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
+        if (e != cudaSuccess) return fail(2, std::string("overlap sums: ") + cudaGetErrorString(e));
+        for (int q = 0; q < k; ++q) {
+            const double c00 = h[3 * q] * h[3 * q] / h[3 * q + 2] / h[3 * q + 1];
+            val[q] = std::fabs(1 - std::fabs(c00));
+        }
         return 0;
     }
 
@@ -447,8 +610,6 @@ public:
         note_launches(1);
         return read(&pw, 1, "Gaussian power");
     }
-
-    long n() const { return n_; }
 
 private:
     int ncx_, ncy_;
@@ -548,10 +709,7 @@ int fit_gauss_abs_dev(int ncx, int ncy, const double *g7, const double *fr, cons
     if (p0_out)
         for (int q = 0; q < 6; ++q) p0_out[q] = p0[q];
 
-    const Objective obj = [&](const double *p, double *fx) { return F.misfit(p, scale, fx); };
-    auto fmin = [&](double *out) {
-        return fmin_nm(6, p0, 1e-4, 1e-4, 0, 0, obj, out, nullptr, nullptr, nullptr);
-    };
+    auto fmin = [&](double *out) { return F.fmin(p0, scale, out); };
     if (!use_ratio) return fmin(popt);
 
     // ratio rounds (FitGauss.py:126-161)

@@ -15,15 +15,16 @@ GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "golden_fitgauss.n
 # Device sums and numpy's pairwise sums differ in the last bits, and so do the
 # device's and numpy's exp and log10, so the simplex's path can part from the
 # reference's near convergence; in LIN the fitted shape (x0, y0, xs, ys,
-# theta) then still agrees far inside the simplex's own stopping tolerance
-# (1e-4 absolute; measured on a GB300: 2e-6 relative at most). amp (index 5)
+# theta) then agrees within the simplex's own stopping tolerance, xatol =
+# 1e-4 absolute (measured on a GB300: 5e-5 at most, theta of a nearly round
+# beam, whose orientation the misfit barely fixes). amp (index 5)
 # is never read by the misfit (generateGauss ignores it), so the simplex moves
 # it freely and its final value only records the path: not compared. In dB
 # the reference's misfit is flat along the beam's scale (see
 # test_fitgauss.py), so a dB fit is checked through its start point and
 # the misfit it reaches from there.
 SHAPE = slice(0, 5)
-RTOL, ATOL = 1e-5, 1e-7
+RTOL, ATOL = 1e-5, 1e-4
 
 
 def _golden():
