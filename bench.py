@@ -481,9 +481,9 @@ def run_ours(args):
                      "forward_against": f"plain FP64 GPU sum on {idx.size} random targets (all sources)",
                      "phase_on": "E components within 20 dB of the sampled peak",
                      "adjoint": adj_acc,
-                     "adjoint_against": f"plain FP64 GPU adjoint, all targets x every {fstep}th source ({nsf})"},
+                     "adjoint_against": f"plain FP64 GPU adjoint, all targets x one source in {fstep} ({nsf})"},
         "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (fwd+adjoint step)", "speedup": value / world / fp64_rate,
-                     "sample": f"all {nt} targets x every {fstep}th source ({nsf})"},
+                     "sample": f"all {nt} targets x one source in {fstep} ({nsf})"},
         "roofline": {"bound": "fp32", "kernel": dom["kernel"], "achieved": dom["achieved_tflops"], "peak": peak,
                      "unit": "TFLOP/s", "frac": dom["frac"], "traffic": traffic,
                      "flops_per_pair": dom["flops_per_pair"],
