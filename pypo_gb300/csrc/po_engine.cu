@@ -313,7 +313,7 @@ int run_device(const RunArgs &a)
     float4 *srcpk = nullptr, *tgtpk = nullptr;
     double *part = nullptr;
     const size_t src_f4 = (size_t)((std::max(ns, 1L) + 1) / 2) * (scalar ? kRec2Scalar : kRec2);
-    const long ntb = (nt + (long)kThreads * kTPT2 - 1) / ((long)kThreads * kTPT2);
+    const long ntb = (nt + (long)kThreads * pk_tpt(kind) - 1) / ((long)kThreads * pk_tpt(kind));
     const int occ = di->occ2[kind][ts > 0][has_m ? 1 : 0];
     const long nsplit = choose_split(ntb, ns, (long)di->sms * occ, nt, nacc);
     const long tiles = std::max(1L, (ns + kTile - 1) / kTile);

@@ -786,7 +786,7 @@ void *fp64_kernel(int kind)
 template <int KIND, int T, bool HAS_M>
 static void *pk_ptr()
 {
-    return reinterpret_cast<void *>(&po_pk_kernel<KIND, T, HAS_M, kTPT2>);
+    return reinterpret_cast<void *>(&po_pk_kernel<KIND, T, HAS_M, pk_tpt(KIND)>);
 }
 
 void *pk_kernel(int kind, int t_sign, bool has_m)

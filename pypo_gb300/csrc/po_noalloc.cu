@@ -173,7 +173,7 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
 
     const int ts = t_direction > 0 ? 1 : -1;
     const bool has_m = kind != po::kKindScalar && !(flags & 1);
-    const long ntb = (nt + (long)po::kThreads * po::kTPT2 - 1) / ((long)po::kThreads * po::kTPT2);
+    const long ntb = (nt + (long)po::kThreads * po::pk_tpt(kind) - 1) / ((long)po::kThreads * po::pk_tpt(kind));
     const size_t part_room = kStaticScratchBytes - (need_bytes(ns, nt, rec2, nacc, 0));
     const long max_chunks = std::max(1L, (long)(part_room / ((size_t)nacc * nt * sizeof(double))));
     const long nsplit = choose_chunks(ntb, ns, (long)st->sms * st->occ[kind][ts > 0][has_m ? 1 : 0], max_chunks);
