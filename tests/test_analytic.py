@@ -7,7 +7,8 @@ without the reference's code (the reference's own tests pin no PO numbers).
   currents, in both time directions;
 * the far field (FF) is the limit of the near field at large distance,
   E_FF(r_hat) = lim k R exp(j k R) E(R r_hat), and equals its closed form;
-* PEC currents (JM) are 2 n x H of the EH field.
+* PEC currents (JM) are 2 n x H of the EH field;
+* a scalar source gives the free-space Green's function.
 
 Run on the oracle (CPU) and through the C-ABI on the GPU, FP64 and mixed."""
 import numpy as np
@@ -140,3 +141,26 @@ def test_pec_currents_are_twice_n_cross_h(backend, oracle_lib):
     Jt, Mt = AN.to_complex(out)
     np.testing.assert_allclose(Jt, 2 * np.cross(nt, H), rtol=0, atol=1e-13 * np.max(np.abs(H)) * 10)
     assert np.all(Mt == 0)
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+@pytest.mark.parametrize("t_dir", [-1.0, 1.0])
+def test_single_scalar_source_is_the_greens_function(backend, t_dir, oracle_lib):
+    """Scalar mode: -k^2 S A exp(-t j k r) / (4 pi r), the free-space Helmholtz
+    Green's function; the sign of its phase is the reference's scalar
+    convention (opposite to the vector kernel's exp(+t j k R)), and scalar
+    mode has no illumination test (targets all round)."""
+    r0 = np.array([0.2, 0.1, -0.3])
+    rng = np.random.default_rng(5)
+    d = rng.standard_normal((8, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    kr = np.array([0.5, 1.0, 3.0, 10.0, 50.0, 300.0, 2000.0, 6000.0])
+    pts = r0 + d * (kr / K)[:, None]
+    S = 0.6 - 0.45j
+    out = run(backend, "scalar", AN.unit_cloud(r0, [0, 0, 1], 0.2), np.array([[S.real], [S.imag]]),
+              AN.unit_cloud(pts, [0, 0, 1], 1.0), t_dir)
+    got = out[0] + 1j * out[1]
+    r = kr / K
+    want = -K * K * S * np.exp(-t_dir * 1j * K * r) / (4 * AN.PI_F * r) * 0.2
+    for i in range(len(kr)):
+        assert abs(got[i] - want[i]) <= TOL[backend] * abs(want[i]), kr[i]
