@@ -1,5 +1,6 @@
 """GPU edge cases against the oracle: single source / target, ragged tiles,
-multi-chunk source splits, empty sources, M = 0 kernels, large phases
+far-field direction counts around the two-per-thread CTA width, multi-chunk
+source splits, empty sources and targets, M = 0 kernels, large phases
 (kR ~ 1e3-1e4 rad, the regime of the benchmark configurations), determinism
 and the device error word."""
 import numpy as np
@@ -66,6 +67,40 @@ def test_many_source_chunks(cuda, lib, oracle_mod):
     assert engine.last_launches() >= 5
     _check("EH", s7, cur, 1, 120, 171, t7, 4.0, oracle_mod)
     _check("EH", s7, cur, 1, 120, 171, t7, 4.0, oracle_mod, t=1.0)
+
+
+@pytest.mark.parametrize("ns_shape,nt", [((2, 2), 1), ((3, 4), 7), ((17, 23), 255), ((31, 33), 257),
+                                         ((64, 41), 513)])
+def test_far_field_sizes_against_oracle(cuda, lib, oracle_mod, ns_shape, nt):
+    """Far field, two directions per thread: counts below, at and just past
+    the 256 directions of a CTA."""
+    rng = np.random.default_rng(sum(ns_shape) * 100 + nt)
+    src, s7, _, cur = _random_case(rng, ns_shape, 1)
+    t7 = np.zeros((7, nt))
+    # directions around -z and (every other one) around +z: both sides of the sources
+    t7[0] = np.pi - rng.uniform(0.0, 0.6, nt)
+    t7[0][::2] = rng.uniform(0.0, 0.6, (nt + 1) // 2)
+    t7[1] = rng.uniform(0.0, 2 * np.pi, nt)
+    t7[5], t7[6] = 1.0, 1.0
+    for t in (-1.0, 1.0):
+        _check("FF", s7, cur, 1, *ns_shape, t7, 5.0, oracle_mod, t)
+
+
+def test_empty_targets_give_empty_outputs(cuda, lib):
+    import torch
+    from pypo_gb300 import engine
+    rng = np.random.default_rng(2)
+    src, s7, _, cur = _random_case(rng, (5, 6), 1)
+    for mode in ("EH", "JM", "JMEH", "EHP", "FF", "scalar"):
+        c = cur[:2] if mode == "scalar" else cur
+        for prec in ("mixed", "fp64"):
+            out = engine.propagate(mode, s7, c, 1, 5, 6, np.zeros((7, 0)), 5.0, precision=prec)
+            assert out.shape == (engine.n_out(mode), 0)
+    # and the device-pointer entry
+    d = lambda a: torch.tensor(a, device=cuda)
+    out = engine.propagate_dev("EH", d(s7), d(cur), 1, 5, 6, d(np.zeros((7, 0))), 5.0)
+    torch.cuda.synchronize()
+    assert tuple(out.shape) == (12, 0)
 
 
 def test_empty_source_gives_zero(cuda, lib):
