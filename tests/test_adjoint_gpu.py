@@ -199,3 +199,22 @@ def test_adjoint_many_chunks_and_determinism(cuda, lib):
     assert _rel(g1["cur"], gd["cur"]) <= 1e-5
     assert _rel(g1["ds"], gd["ds"]) <= 1e-4
     assert _rel(g1["dt"], gd["dt"]) <= 1e-4
+
+
+def test_adjoint_with_no_targets_or_no_sources(cuda, lib):
+    """No targets: every gradient is zero. No sources: the target gradient is
+    zero and the source gradients are empty."""
+    from pypo_gb300 import engine, surfaces as SF
+    rng = np.random.default_rng(4)
+    s7 = engine.generate_grid(SF.paraboloid(3.0, [5, 6], gmode=1, lims_a=[0.2, 2.0]))
+    cur = rng.standard_normal((12, s7.shape[1]))
+    t7 = engine.generate_grid(SF.translate(SF.plane([4, 3], gmode=0, lims_a=[-1, 1]), dz=3.0))
+    for mode in ("EH", "FF"):
+        for prec in ("mixed", "fp64"):
+            g = engine.adjoint(mode, s7, cur, 1, 5, 6, np.zeros((7, 0)), 3.0,
+                               np.zeros((engine.n_out(mode), 0)), precision=prec)
+            assert np.all(g["cur"] == 0) and np.all(g["ds"] == 0) and g["cur"].shape == (12, 30)
+            if mode != "FF":
+                g = engine.adjoint(mode, np.zeros((7, 0)), np.zeros((12, 0)), -1, 0, 0, t7, 3.0,
+                                   rng.standard_normal((12, t7.shape[1])), precision=prec)
+                assert g["cur"].shape == (12, 0) and g["ds"].shape == (0,) and np.all(g["dt"] == 0)
