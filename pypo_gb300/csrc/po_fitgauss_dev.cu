@@ -671,8 +671,8 @@ int fit_gauss_abs_dev(int ncx, int ncy, const double *g7, const double *fr, cons
     if (int rc = F.alloc()) return rc;
     auto thr_of = [&](double t) { return scale == kScaleDb ? t : std::pow(10.0, t / 20); };
 
-    double fit_max, nf2;
-    long imax;
+    double fit_max = 0.0, nf2 = 0.0;
+    long imax = 0;
     if (int rc = F.pattern(fr, fi, scale, fit_max, imax, nf2)) return rc;
     const long i0 = imax / ncy, j0 = imax % ncy;
 
