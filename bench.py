@@ -206,6 +206,35 @@ def chain_stage_workloads(c, stages):
     return out
 
 
+def dish_chain_fd(c, grad, cot, k, nodes=64, h_lam=1e-6):
+    """The perturbed-dish chain's displacement gradient against central finite
+    differences of the FP64 chain on 64 seeded dish nodes (h = 1e-6 lambda).
+    The loss sum(cot * far field) is a sum of per-node far-field terms, and a
+    node's displacement changes only its own (its induced current and its
+    position), so each difference needs that node alone: a one-target JM from
+    the feed and a one-source FF."""
+    from pypo_gb300 import engine
+    f7, fcur, d7, ff7 = c["feed7"], c["feed_cur"], c["dish7"], c["ff7"]
+    fg, (gm, ncx, ncy) = c["feed_grid"], c["dish_grid"]
+    h = h_lam * c["lam"]
+    pick = np.random.default_rng(2).choice(d7.shape[1], nodes, replace=False)
+
+    def term(i, delta):
+        p7 = d7[:, i:i + 1].copy()
+        p7[:3, 0] += delta * d7[3:6, i]
+        ji = engine.propagate("JM", f7, fcur, *fg, p7, k, precision="fp64")
+        xu, yv = i // ncy, i % ncy   # the dish grid's trapezoid weight of node i
+        w = (0.5 if xu in (0, ncx - 1) else 1.0) * (0.5 if gm != 1 and yv in (0, ncy - 1) else 1.0)
+        p7[6, 0] *= w
+        return float((engine.propagate("FF", p7, ji, -1, 0, 0, ff7, k, precision="fp64") * cot).sum())
+
+    fd = np.array([(term(i, c["delta"][i] + h) - term(i, c["delta"][i] - h)) / (2 * h) for i in pick])
+    g = grad[pick]
+    return {"rel_l2": float(np.linalg.norm(g - fd) / np.linalg.norm(fd)), "nodes": nodes,
+            "h": f"{h_lam:g} lambda", "gradient": "mixed-precision autograd of the timed step",
+            "against": "central differences of the FP64 chain, one node moved at a time"}
+
+
 def run_reference_chain(args, threads):
     """Reference arm of a chain: the FP64 CPU oracle's forward rate per stage on
     bounded target samples, combined by pairs."""
@@ -661,6 +690,10 @@ def run_chain(args):
     acc = {"ff_rel_l2": rel(outs["mixed"][0], outs["fp64"][0])}
     for r in refl:
         acc[f"grad_{r[:-1]}_rel_l2"] = rel(outs["mixed"][1][r], outs["fp64"][1][r])
+    # the perturbed-dish chain's gradient against finite differences, at full size
+    grad_fd = None
+    if args.workload == "dish_chain" and args.scale == 1.0:
+        grad_fd = dish_chain_fd(c, dvars["dish7"].grad.detach().cpu().numpy(), cot_np, k)
 
     if rank != 0:
         return
@@ -683,6 +716,7 @@ def run_chain(args):
                    "l2": "flushed before every step (256 MB write inside the timed loop)",
                    "parallelism": f"replica per GPU x{world}"},
         "accuracy": dict(acc, against="FP64 GPU chain, configuration at scale 0.2"),
+        **({"gradient_vs_finite_differences": grad_fd} if grad_fd else {}),
         "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (chain fwd+adjoint)", "speedup": value / world / fp64_rate,
                      "sample": "each stage timed on every s-th source x every t-th target (>= 65536 of each where "
                                "available), combined by pairs"},
