@@ -44,8 +44,8 @@
 //     an index, which selects grid row 1 (repeated; the repetition cancels
 //     in every ratio), so the fit then runs on row 1 (on an xy grid x is
 //     constant along a row and that fit is decided by rounding residue);
-//   * the ratio rounds use the plain mask in round 0 and the windowed one
-//     after; a pattern whose ratio never drops below the limit loops for
+//   * the first of the ratio rounds uses the plain mask, later ones the
+//     windowed one; a pattern whose ratio never drops below the limit loops for
 //     ever in the reference; here the call returns an error once a round
 //     would only repeat the previous one.
 #include <cuda_runtime.h>
