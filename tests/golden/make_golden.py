@@ -9,7 +9,7 @@ vector Gaussian feed (makeGaussBeam). Outputs go to golden_*.npz beside this
 script. Needs the reference sources (this container); the fixtures then
 travel without them.
 
-Usage: python tests/golden/make_golden.py [--only-calcjm | --only-eff | --only-fitgauss]
+Usage: python tests/golden/make_golden.py [--only-calcjm | --only-eff | --only-fitgauss | --only-converge]
 """
 import json
 import pathlib
@@ -208,6 +208,82 @@ def fitgauss(ref):
     print("wrote fitgauss", len(out), "entries")
 
 
+def converge(ref):
+    """The reference's own System.autoConverge and System.convergeOnTarget
+    (System.py:2779-3086) on a Gaussian feed (createGaussian on a 21 x 21
+    plane, lambda 2 mm) and a dish facing it (uv or xy grid), with a target
+    plane behind the feed (xy or uv). System is imported with its plotting
+    modules replaced by mocks (matplotlib is not installed here), and its
+    bindings load the reference's library compiled from its sources
+    (oracle/build_ref.sh) in place of the libpypocpu / libpyporefl /
+    libpypobeam it looks for beside itself. Stores the feed's fields, the
+    reflectors' internal dicts and the grid sizes found."""
+    import ctypes
+    import copy
+    import types
+    from unittest import mock
+    for m in ("matplotlib", "matplotlib.pyplot", "matplotlib.cm", "matplotlib.colors", "matplotlib.ticker",
+              "matplotlib.patches", "matplotlib.collections", "mpl_toolkits", "mpl_toolkits.axes_grid1",
+              "mpl_toolkits.mplot3d"):
+        sys.modules.setdefault(m, mock.MagicMock())
+    sys.path.insert(0, "/root/reference/src")
+    import PyPO.BindBeam as BBeam
+    import PyPO.BindCPU as BCPU
+    import PyPO.BindRefl as BRefl
+    shim = types.ModuleType("ctypes_for_reference")
+    shim.__dict__.update(ctypes.__dict__)
+
+    def cdll(path, *a, **k):
+        base = pathlib.Path(str(path)).name
+        if base.startswith(("libpypo", "pypo")):
+            if not base.endswith(".so"):
+                raise OSError(base)
+            return ctypes.CDLL(str(O.REF_PATH))
+        return ctypes.CDLL(path, *a, **k)
+
+    shim.CDLL = cdll
+    for mod in (BCPU, BRefl, BBeam):
+        mod.ctypes = shim
+    from PyPO.System import System
+
+    out = {}
+    for dish_mode in ("uv", "xy"):
+        for tgt_mode in ("xy", "uv"):
+            s = System(verbose=False)
+            s.addPlane({"name": "feed", "gmode": "xy", "lims_x": np.array([-15.0, 15.0]),
+                        "lims_y": np.array([-15.0, 15.0]), "gridsize": np.array([21, 21])})
+            lims = ({"lims_u": np.array([0, 60.0]), "lims_v": np.array([0, 360.0])} if dish_mode == "uv"
+                    else {"lims_x": np.array([-60.0, 60.0]), "lims_y": np.array([-60.0, 60.0])})
+            s.addParabola(dict(name="dish", pmode="focus", vertex=np.zeros(3), focus_1=np.array([0, 0, 60.0]),
+                               gmode=dish_mode, gridsize=np.array([11, 11]), **lims))
+            s.rotateGrids("dish", np.array([180.0, 0, 0]))
+            s.translateGrids("dish", np.array([0, 0, 60.0]))
+            tl = ({"lims_u": np.array([0, 20.0]), "lims_v": np.array([0, 360.0])} if tgt_mode == "uv"
+                  else {"lims_x": np.array([-20.0, 20.0]), "lims_y": np.array([-20.0, 20.0])})
+            s.addPlane(dict(name="tplane", gmode=tgt_mode, gridsize=np.array([5, 5]), **tl))
+            s.translateGrids("tplane", np.array([0, 0, -150.0]))
+            s.createGaussian({"name": "gfield", "lam": 2.0, "w0x": 6.0, "w0y": 6.0, "n": 1, "E0": 1.0,
+                              "dxyz": 0.0, "pol": np.array([1, 0, 0])}, "feed")
+            key = f"{dish_mode}_{tgt_mode}"
+            dish0, tpl0 = copy.deepcopy(s.system["dish"]), copy.deepcopy(s.system["tplane"])
+            f = s.fields["gfield"]
+            blk = np.zeros((12, 441))
+            for c, comp in enumerate(("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")):
+                v = np.asarray(getattr(f, comp)).ravel()
+                r = c if c < 3 else c + 3
+                blk[r], blk[r + 3] = v.real, v.imag
+            out[key + "__feed_json"] = dict_to_json(s.system["feed"])
+            out[key + "__dish_json"] = dict_to_json(dish0)
+            out[key + "__target_json"] = dict_to_json(tpl0)
+            out[key + "__fields"] = blk
+            out[key + "__k"] = f.k
+            out[key + "__auto"] = np.asarray(s.autoConverge("gfield", "dish"))
+            s.system["dish"] = copy.deepcopy(dish0)
+            out[key + "__on_target"] = np.asarray(s.convergeOnTarget("gfield", "dish", "tplane"))
+    np.savez_compressed(HERE / "golden_converge.npz", **out)
+    print("wrote converge", {k: v for k, v in out.items() if k.endswith(("__auto", "__on_target"))})
+
+
 def main():
     if not O.REF_PATH.exists():
         subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
@@ -221,9 +297,13 @@ def main():
     if "--only-fitgauss" in sys.argv:
         fitgauss(ref)
         return
+    if "--only-converge" in sys.argv:
+        converge(ref)
+        return
     calcjm(ref)
     efficiencies(ref)
     fitgauss(ref)
+    converge(ref)
     rng = np.random.default_rng(20261203)
     k = 2 * np.pi / 0.7
     for name, src, tgt, modes in cases():
