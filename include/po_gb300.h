@@ -214,6 +214,13 @@ int po_generate_gauss_dev(long n, const double *grid7, const double *popt, int s
 int po_fmin(int n, const double *x0, double xtol, double ftol, long maxiter, long maxfun, po_objective f, void *ctx,
             double *xopt, double *fopt, long *iterations, long *fcalls);
 
+/* Frame half-extent, in wavelengths, of this thread's last mixed-precision
+ * host-buffer call (po_run_d, po_adjoint_d); 0 after any other call. It sets
+ * the mixed path's hi/lo quantum, so its error grows with it (the path holds
+ * 1e-5 relative L2 up to about 5e4); the library computes it on the device
+ * and reads it back with the call's results. */
+double po_last_extent(void);
+
 /* ---- explicit-grid, double-precision entry (host buffers) ---------------
  * New; the reference has no equivalent (its C-ABI regenerates grids inside
  * every call, Kernelsf.cu:1643-1644, so it cannot take perturbed surfaces or

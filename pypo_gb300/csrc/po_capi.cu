@@ -15,6 +15,10 @@ using po::fail;
 std::mutex g_stream_mu;
 cudaStream_t g_streams[64] = {};
 
+// Frame half-extent (wavelengths) of this thread's last mixed-precision
+// host-buffer call; 0 after any other call.
+thread_local double t_extent = 0.0;
+
 // Private non-blocking stream of the host-buffer entry points, one per device.
 int lib_stream(cudaStream_t *s)
 {
@@ -31,11 +35,33 @@ int lib_stream(cudaStream_t *s)
     return 0;
 }
 
-bool m_is_zero(const double *cur, long ns)
+// *flag = 1 where any of the n values is non-zero (-0.0 counts as zero, NaN
+// as non-zero). Every writer stores the same value.
+__global__ void po_any_nonzero_kernel(const double *__restrict__ p, long n, int *__restrict__ flag)
 {
-    for (long i = 6 * ns; i < 12 * ns; ++i)
-        if (cur[i] != 0.0) return false;
-    return true;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        if (p[i] != 0.0) *flag = 1;
+}
+
+// Whether the magnetic currents (rows 6-11 of a device copy of 12 x ns
+// currents) are all zero, which selects the M = 0 kernels. Checked on the
+// device after the copy: a host scan of the rows would leave the GPU idle.
+int device_m_is_zero(const double *d_cur, long ns, cudaStream_t s, bool &zero)
+{
+    int *flag = nullptr, h = 0;
+    cudaError_t e = cudaMallocAsync(&flag, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+    if (e == cudaSuccess) {
+        po_any_nonzero_kernel<<<2 * 152, 256, 0, s>>>(d_cur + 6 * ns, 6 * ns, flag);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (flag) cudaFreeAsync(flag, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(2, std::string("checking the magnetic currents: ") + cudaGetErrorString(e));
+    po::note_launches(1);
+    zero = h == 0;
+    return 0;
 }
 
 #define CK(expr)                                                                          \
@@ -52,6 +78,7 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
              const double *tgt7, double k, double eps, double t, int precision, double *out)
 {
     po::clear_error();
+    t_extent = 0.0;
     {
         po::RunArgs v;
         v.mode = mode;
@@ -77,6 +104,7 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
     if (int rc = lib_stream(&s)) return rc;
     double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_out = nullptr;
     int rc = 0, code = 0;
+    double extent = 0.0;
     po::RunArgs a;
     CK(cudaMallocAsync(&d_src, sizeof(double) * 7 * std::max(ns, 1L), s));
     CK(cudaMallocAsync(&d_cur, sizeof(double) * ncur * std::max(ns, 1L), s));
@@ -100,13 +128,20 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
     a.epsilon = eps;
     a.t_dir = t;
     a.precision = precision;
-    a.m_zero = mode != po::kScalar && ns > 0 && m_is_zero(cur, ns);
+    a.m_zero = false;
+    if (mode != po::kScalar && ns > 0) {
+        bool mz = false;
+        if ((rc = device_m_is_zero(d_cur, ns, s, mz))) goto done;
+        a.m_zero = mz;
+    }
+    a.extent_host = &extent;
     a.out = d_out;
     a.stream = s;
     rc = po::run_device(a);
     if (rc) goto done;
     CK(cudaMemcpyAsync(out, d_out, sizeof(double) * nout * nt, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (precision == 0) t_extent = extent;
     rc = po::read_device_error(s, &code);
     if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
                                       std::to_string(code) + "); results are invalid");
@@ -308,11 +343,13 @@ int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int nc
     return po::run_device(a);
 }
 
-int po_adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
-                   const double *tgt7, double k, double epsilon, double t_direction, int precision, int flags,
-                   const double *cot, double *grad_cur, double *grad_ds, double *grad_dt, void *stream)
+namespace {
+
+int adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
+                const double *tgt7, double k, double epsilon, double t_direction, int precision, int flags,
+                const double *cot, double *grad_cur, double *grad_ds, double *grad_dt, cudaStream_t stream,
+                double *extent_host)
 {
-    po::clear_error();
     po::AdjArgs a;
     a.mode = mode;
     a.ns = ns;
@@ -333,16 +370,31 @@ int po_adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, in
     a.grad_cur = grad_cur;
     a.grad_ds = grad_ds;
     a.grad_dt = grad_dt;
-    a.stream = static_cast<cudaStream_t>(stream);
+    a.stream = stream;
+    a.extent_host = extent_host;
     if (!grad_cur && !grad_ds && !grad_dt) return fail(1, "no gradient requested");
     return po::run_adjoint(a);
 }
+
+}  // namespace
+
+int po_adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
+                   const double *tgt7, double k, double epsilon, double t_direction, int precision, int flags,
+                   const double *cot, double *grad_cur, double *grad_ds, double *grad_dt, void *stream)
+{
+    po::clear_error();
+    return adjoint_dev(mode, ns, src7, gmode, ncx, ncy, cur, nt, tgt7, k, epsilon, t_direction, precision, flags, cot,
+                       grad_cur, grad_ds, grad_dt, static_cast<cudaStream_t>(stream), nullptr);
+}
+
+double po_last_extent(void) { return t_extent; }
 
 int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
                  const double *tgt7, double k, double epsilon, double t_direction, int precision, const double *cot,
                  double *grad_cur, double *grad_ds, double *grad_dt)
 {
     po::clear_error();
+    t_extent = 0.0;
     if (mode < 0 || mode > 5) return fail(1, "mode must be 0..5");
     if (ns < 0 || nt < 0) return fail(1, "negative size");
     const int nout = po::n_out(mode);
@@ -351,6 +403,7 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_cot = nullptr;
     double *d_gc = nullptr, *d_gs = nullptr, *d_gt = nullptr;
     int rc = 0, code = 0;
+    double extent = 0.0;
     const size_t ns1 = std::max(ns, 1L), nt1 = std::max(nt, 1L);
     CK(cudaMallocAsync(&d_src, sizeof(double) * 7 * ns1, s));
     CK(cudaMallocAsync(&d_cur, sizeof(double) * 12 * ns1, s));
@@ -367,13 +420,18 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
         CK(cudaMemcpyAsync(d_tgt, tgt7, sizeof(double) * 7 * nt, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_cot, cot, sizeof(double) * nout * nt, cudaMemcpyHostToDevice, s));
     }
-    rc = po_adjoint_dev(mode, ns, d_src, gmode, ncx, ncy, d_cur, nt, d_tgt, k, epsilon, t_direction, precision,
-                        (ns > 0 && m_is_zero(cur, ns)) ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s);
+    {
+        bool mz = false;
+        if (ns > 0 && (rc = device_m_is_zero(d_cur, ns, s, mz))) goto done;
+        rc = adjoint_dev(mode, ns, d_src, gmode, ncx, ncy, d_cur, nt, d_tgt, k, epsilon, t_direction, precision,
+                         mz ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s, &extent);
+    }
     if (rc) goto done;
     if (grad_cur && ns > 0) CK(cudaMemcpyAsync(grad_cur, d_gc, sizeof(double) * 12 * ns, cudaMemcpyDeviceToHost, s));
     if (grad_ds && ns > 0) CK(cudaMemcpyAsync(grad_ds, d_gs, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
     if (grad_dt && nt > 0) CK(cudaMemcpyAsync(grad_dt, d_gt, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (precision == 0) t_extent = extent;
     rc = po::read_device_error(s, &code);
     if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
                                       std::to_string(code) + "); results are invalid");

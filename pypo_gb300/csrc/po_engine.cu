@@ -352,6 +352,8 @@ int run_device(const RunArgs &a)
     double zi = zeta_inv;
     void *eargs[] = {&mode, &nspl, &nt, &part, &tgt7, &t, &zi, &out};
     if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
+    if (!rc && a.extent_host) PO_CK_RC(cudaMemcpyAsync(a.extent_host, &frame->m, sizeof(double),
+                                                       cudaMemcpyDeviceToHost, s));
     sfree(owned, s);
     return rc;
 }
@@ -512,6 +514,8 @@ int run_adjoint(const AdjArgs &a)
         void *teargs[] = {&one, &nt, &gt, &dsct, &grad_dt};
         rc = launch(adj_tgt_epilogue_kernel(), dim3(nblk_t), dim3(256), teargs, 0, s);
     }
+    if (!rc && a.extent_host) PO_CK_RC(cudaMemcpyAsync(a.extent_host, &frame->m, sizeof(double),
+                                                       cudaMemcpyDeviceToHost, s));
     sfree(owned, s);
     return rc;
 }

@@ -24,6 +24,8 @@ struct RunArgs {
     bool m_zero = false;           // M == 0 on the source
     double *out = nullptr;         // n_out(mode) rows x nt
     cudaStream_t stream = nullptr;
+    double *extent_host = nullptr; // mixed path: host slot for the frame's half-extent (wavelengths),
+                                   // written by a copy queued on `stream`
 };
 
 // Adjoint of one propagation: cotangents of the outputs in, gradients with

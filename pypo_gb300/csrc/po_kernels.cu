@@ -374,6 +374,7 @@ __global__ void po_frame_kernel(const double *__restrict__ partial, int nblk, do
     fr->kappa = kappa;
     fr->q = q;
     fr->inv_q = 1.0 / q;
+    fr->m = m;
 }
 
 __device__ __forceinline__ double trap_weight(long i, int gmode, int ncx, int ncy)

@@ -90,6 +90,7 @@ struct Frame {
     double kappa;
     double q;
     double inv_q;
+    double m;   // half-extent in wavelengths (turns), which sets q and the precision
 };
 
 // Pair-packed main kernel: stages plus the compensation words.

@@ -45,6 +45,7 @@ inline size_t up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 constexpr size_t kOffStatus = 0;                       // int, cleared every call
 constexpr size_t kOffFrame = 256;                      // po::Frame
 constexpr size_t kOffBbox = 512;                       // kBboxBlocks * 6 doubles
+static_assert(sizeof(po::Frame) <= kOffBbox - kOffFrame, "the frame must fit its slot");
 constexpr size_t kFixed = kOffBbox + ((po::kBboxBlocks * 6 * sizeof(double) + kAlign - 1) / kAlign) * kAlign;
 
 struct StaticSetup {

@@ -78,7 +78,9 @@ def mixed_extent(mode, src7, tgt7, k):
     positions are split into hi parts on a quantum ~ extent / 1024 and the lo
     parts' rounding grows with it. Near field and scalar: half the largest side
     of the bounding box of sources and targets (the frame is centred); far
-    field: the largest source coordinate (the frame is the coordinate origin)."""
+    field: the largest source coordinate (the frame is the coordinate origin).
+    A host computation for planning; the library reports the same value for
+    each host-buffer call (last_extent)."""
     kappa = float(k) / (2 * np.pi)
     if src7.shape[1] == 0:
         return 0.0
@@ -88,10 +90,17 @@ def mixed_extent(mode, src7, tgt7, k):
     return float((pts.max(axis=1) - pts.min(axis=1)).max()) * 0.5 * kappa
 
 
-def _extent_warning(mode, src7, tgt7, k, precision):
+def last_extent():
+    """Frame half-extent (wavelengths) of this thread's last mixed-precision
+    host-buffer call, computed on the device (po_last_extent)."""
+    return float(load().po_last_extent())
+
+
+def _extent_warning(m, precision):
+    """Warn when a mixed-precision call's frame half-extent m is beyond the
+    measured range of the path."""
     if precision != "mixed":
         return
-    m = mixed_extent(mode, src7, tgt7, k)
     if m > MIXED_EXTENT_LIMIT:
         warnings.warn(f"scene half-extent {m:.3g} wavelengths exceeds {MIXED_EXTENT_LIMIT:.3g}: the mixed path's "
                       "error grows with it (about 1e-5 relative at 1e5); use precision='fp64' for this call",
@@ -106,7 +115,6 @@ def propagate(mode, src7, cur, gmode, ncx, ncy, tgt7, k, epsilon=1.0, t_dir=-1.0
     tgt7 = np.ascontiguousarray(tgt7, dtype=np.float64)
     cur = np.ascontiguousarray(cur, dtype=np.float64)
     _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy)
-    _extent_warning(mode, src7, tgt7, k, precision)
     nt = tgt7.shape[1]
     if out is None:
         out = np.empty((n_out(mode), nt), dtype=np.float64)
@@ -115,6 +123,7 @@ def propagate(mode, src7, cur, gmode, ncx, ncy, tgt7, k, epsilon=1.0, t_dir=-1.0
     check(lib.po_run_d(MODE_ID[mode], src7.shape[1], src7.ctypes.data, int(gmode), int(ncx), int(ncy),
                        cur.ctypes.data, nt, tgt7.ctypes.data, float(k), float(epsilon), float(t_dir),
                        PRECISION[precision], out.ctypes.data))
+    _extent_warning(last_extent(), precision)
     return out
 
 
@@ -181,7 +190,6 @@ def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-
     cur = np.ascontiguousarray(cur, dtype=np.float64)
     cot = np.ascontiguousarray(cot, dtype=np.float64)
     _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy)
-    _extent_warning(mode, src7, tgt7, k, precision)
     ns, nt = src7.shape[1], tgt7.shape[1]
     if cot.shape != (n_out(mode), nt):
         raise POError(f"cot must have shape {(n_out(mode), nt)}")
@@ -193,6 +201,7 @@ def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-
     check(lib.po_adjoint_d(MODE_ID[mode], ns, src7.ctypes.data, int(gmode), int(ncx), int(ncy), cur.ctypes.data,
                            nt, tgt7.ctypes.data, float(k), float(epsilon), float(t_dir), PRECISION[precision],
                            cot.ctypes.data, ptr(gc), ptr(gs), ptr(gt)))
+    _extent_warning(last_extent(), precision)
     if gc is not None:
         out["cur"] = gc
     if gs is not None:

@@ -179,6 +179,8 @@ def test_large_scene_nearfield_within_limit(cuda, lib, oracle_mod):
     assert engine.mixed_extent("EH", s7, t7, k) <= engine.MIXED_EXTENT_LIMIT
     for mode in ("EH", "JM"):
         _check(mode, s7, cur, 1, 41, 40, t7, k, oracle_mod)
+        # the library's frame (computed on the device) has the host planner's extent
+        assert engine.last_extent() == pytest.approx(engine.mixed_extent(mode, s7, t7, k), rel=1e-12)
     cot = rng.standard_normal((12, t7.shape[1]))
     gm = engine.adjoint("EH", s7, cur, 1, 41, 40, t7, k, cot, precision="mixed")
     gd = engine.adjoint("EH", s7, cur, 1, 41, 40, t7, k, cot, precision="fp64")
@@ -211,3 +213,26 @@ def test_deterministic_and_clean_error_word(cuda, lib):
     b = engine.propagate("JMEH", s7, cur, 1, 40, 50, t7, 3.0)
     np.testing.assert_array_equal(a, b)
     assert engine.device_error(torch.cuda.current_stream()) == 0
+
+
+def test_scene_beyond_the_mixed_range_warns(cuda, lib):
+    """The host-buffer entries warn after a mixed-precision call whose frame
+    half-extent (read back from the device) is beyond the measured range;
+    the FP64 path does not."""
+    import warnings
+    from pypo_gb300 import engine, surfaces as SF
+    s7 = engine.generate_grid(SF.paraboloid(50.0, [5, 6], gmode=1, lims_a=[0, 20]))
+    t7 = engine.generate_grid(SF.translate(SF.plane([3, 3], gmode=0, lims_a=[-10, 10]), dz=2.0e5))   # 1e5 wavelengths
+    t7[3:6] *= -1.0
+    cur = np.random.default_rng(1).standard_normal((12, s7.shape[1]))
+    k = 2 * np.pi / 1.0
+    with pytest.warns(RuntimeWarning, match="fp64"):
+        engine.propagate("EH", s7, cur, 1, 5, 6, t7, k)
+    assert engine.last_extent() == pytest.approx(engine.mixed_extent("EH", s7, t7, k), rel=1e-12)
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        engine.propagate("EH", s7, cur, 1, 5, 6, t7, k, precision="fp64")
+    assert engine.last_extent() == 0.0
+    ff = engine.generate_grid(SF.farfield([3, 3], [-1, 1], [-1, 1]))
+    engine.propagate("FF", s7, cur, 1, 5, 6, ff, k)
+    assert engine.last_extent() == pytest.approx(engine.mixed_extent("FF", s7, ff, k), rel=1e-12)

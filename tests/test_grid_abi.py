@@ -126,11 +126,12 @@ def test_mixed_extent_and_warning():
     assert engine.mixed_extent("FF", s7, t7, k) == 2.0      # largest source coordinate only
     with warnings.catch_warnings():
         warnings.simplefilter("error")
-        engine._extent_warning("EH", s7, t7, k, "mixed")   # 1e3 wavelengths: no warning
+        engine._extent_warning(1.0e3, "mixed")             # 1e3 wavelengths: no warning
     far = t7.copy()
     far[2] = 1.0e5
+    m = engine.mixed_extent("EH", s7, far, k)
     with pytest.warns(RuntimeWarning, match="fp64"):
-        engine._extent_warning("EH", s7, far, k, "mixed")
+        engine._extent_warning(m, "mixed")
     with warnings.catch_warnings():
         warnings.simplefilter("error")
-        engine._extent_warning("EH", s7, far, k, "fp64")
+        engine._extent_warning(m, "fp64")
