@@ -333,7 +333,7 @@ int run_device(const RunArgs &a)
     double kap = kappa;
     int centred = far ? 0 : 1;
     void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
-    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
+    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(32), frargs, 0, s);
     float *srcf = reinterpret_cast<float *>(srcpk);
     void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcf};
     const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
@@ -455,7 +455,7 @@ int run_adjoint(const AdjArgs &a)
     double kap = kappa;
     int centred = far ? 0 : 1;
     void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
-    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
+    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(32), frargs, 0, s);
     void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&zero_scalar, &srcpk};
     if (!rc) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
     // Pair-packed adjoint: sources in registers, pairs of targets streamed.

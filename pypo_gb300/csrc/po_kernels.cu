@@ -347,18 +347,25 @@ __global__ void po_bbox_kernel(const double *__restrict__ a, long na, const doub
         for (int c = 0; c < 6; ++c) partial[blockIdx.x * 6 + c] = sm[c][0];
 }
 
-// One thread: reduce the block partials and fix origin, scale and quantum.
+// One warp: reduce the block partials (lane l takes blocks l, l + 32, ...;
+// min and max are exact in any order) and fix origin, scale and quantum.
 // centred: origin at the bbox centre (near field, scalar); otherwise origin 0
 // (far field: the phase reference is the coordinate origin).
 __global__ void po_frame_kernel(const double *__restrict__ partial, int nblk, double kappa, int centred,
                                 Frame *__restrict__ fr)
 {
     double lo[3] = {CUDART_INF, CUDART_INF, CUDART_INF}, hi[3] = {-CUDART_INF, -CUDART_INF, -CUDART_INF};
-    for (int b = 0; b < nblk; ++b)
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
         for (int c = 0; c < 3; ++c) {
             lo[c] = fmin(lo[c], partial[b * 6 + c]);
             hi[c] = fmax(hi[c], partial[b * 6 + 3 + c]);
         }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fmin(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+            hi[c] = fmax(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+    if (threadIdx.x != 0) return;
     double m = 0.0;
     for (int c = 0; c < 3; ++c) {
         double o = 0.0;

@@ -210,7 +210,7 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
     double kap = kappa;
     int centred = far ? 0 : 1;
     void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
-    if (!rc) rc = launch(po::frame_kernel(), dim3(1), dim3(1), frargs, 0, s);
+    if (!rc) rc = launch(po::frame_kernel(), dim3(1), dim3(32), frargs, 0, s);
     float *srcf = reinterpret_cast<float *>(srcpk);
     void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcf};
     const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
