@@ -15,6 +15,8 @@ spherical mapping (engine.generate_grid_dev(refl, transform=False,
 spheric=False)), as the reference's fit regenerates them; fields are
 (12, n) float64 device blocks in c2Bundle row order, the component 0-5
 (Ex Ey Ez Hx Hy Hz), or a real (n,) amplitude with comp None.
+fitGaussAbs and generateGauss take the reference's own arguments (a numpy
+field and a reflector dict) and make the grid on the device.
 """
 import ctypes
 
@@ -142,3 +144,35 @@ def fmin(func, x0, args=(), xtol=1e-4, ftol=1e-4, maxiter=None, maxfun=None, ful
     if full_output:
         return xopt, fopt.value, nit.value, nfev.value
     return xopt
+
+
+# ------------------------------------------------- the reference's signatures
+#
+# FitGauss.fitGaussAbs and FitGauss.generateGauss with the reference's
+# arguments: a numpy field component shaped like the surface's grid and the
+# surface's reflector dict. The grid (restframe, no spherical mapping, as the
+# reference regenerates it) and the fit run on the device.
+
+def _surface(surfaceObject):
+    from .engine import generate_grid_dev
+    ncx, ncy = (int(v) for v in np.asarray(surfaceObject["gridsize"]).reshape(2))
+    return generate_grid_dev(surfaceObject, transform=False, spheric=False), ncx, ncy
+
+
+def fitGaussAbs(field, surfaceObject, thres, scale, ratio=1):
+    """Gaussian parameters (x0, y0, xs, ys, theta, amp) fitted to |field|
+    (FitGauss.fitGaussAbs, :71-163); ratio None fits once."""
+    import torch
+    g7, ncx, ncy = _surface(surfaceObject)
+    amp = np.abs(np.asarray(field)).reshape(-1)
+    if amp.size != ncx * ncy:
+        raise ValueError(f"the field holds {amp.size} values, the surface {ncx * ncy} points")
+    return fit_gauss_abs_dev(g7, ncx, ncy, torch.tensor(amp, dtype=torch.float64, device=g7.device), None,
+                             thres, scale, ratio)
+
+
+def generateGauss(p0, surfaceObject, scale):
+    """The Gaussian of parameters p0 on the surface's grid, a numpy array
+    shaped like the grid (FitGauss.generateGauss, :201-228); scale LIN or dB."""
+    g7, ncx, ncy = _surface(surfaceObject)
+    return generate_gauss_dev(g7, p0, scale).cpu().numpy().reshape(ncx, ncy)

@@ -1,6 +1,7 @@
 """Source producers (pypo_gb300.beams) against the reference's outputs
 (golden vectors): makeGaussBeam in full and PEC modes, calcCurrents in every
-mode."""
+mode; and the oracle's restatement of the efficiencies pinned to the
+reference's Efficiencies.py."""
 import numpy as np
 
 from tests.common import GOLDEN, from_json
@@ -34,7 +35,8 @@ def test_calc_jm_matches_reference(lib):
 def test_efficiencies_match_reference():
     """Spillover, taper, cross-polar and main-beam efficiencies against the
     reference's Efficiencies.py run on the same field (golden vectors)."""
-    from pypo_gb300 import efficiencies as E, engine
+    from oracle import efficiencies as E
+    from pypo_gb300 import engine
     g = np.load(GOLDEN / "golden_eff.npz")
     b = engine.generate_grid(from_json(str(g["surface_json"])), transform=False)
     x, y, a = b[0], b[1], b[6]

@@ -46,3 +46,28 @@ def test_device_efficiency_rejects_bad_arguments(cuda, lib):
     assert b"imaginary row without a real row" in lib.po_last_error()
     # a real second field (a fitted Gaussian) needs no imaginary row
     assert lib.po_efficiency_sums_dev(4, p(g7), p(g7), p(g7), p(g7), None, 0, None, p(sums), st) == 0
+
+
+def test_reference_signatures_match_reference(cuda, lib):
+    """calcSpillover / calcTaper / calcXpol / calcMainBeam with the
+    reference's own arguments (numpy components shaped like the grid, the
+    surface's reflector dict): the grid and the sums made on the device."""
+    from pypo_gb300 import efficiencies as E
+    g = np.load(GOLDEN / "golden_eff.npz")
+    surf = from_json(str(g["surface_json"]))
+    shape = tuple(int(v) for v in surf["gridsize"])
+    co, xp, fit = (g[k].reshape(shape) for k in ("co", "xp", "fit"))
+    e, r = g["ell"], g["rect"]
+    ell = {"shape": "ell", "center": e[0:2], "outer": e[2:4]}
+    rect = {"shape": "rect", "center": r[0:2], "outer_x": r[2:4], "outer_y": r[4:6]}
+    tol = 1e-12
+    assert abs(E.calcSpillover(co, surf, ell) - g["spill_ell"]) <= tol
+    assert abs(E.calcSpillover(co, surf, rect) - g["spill_rect"]) <= tol
+    assert abs(E.calcTaper(co, surf, ell) - g["taper_ell"]) <= tol
+    assert abs(E.calcTaper(co, surf, rect) - g["taper_rect"]) <= tol
+    assert abs(E.calcTaper(co, surf, None) - g["taper_all"]) <= tol
+    assert abs(E.calcTaper(co, surf, {}) - g["taper_all"]) <= tol
+    assert abs(E.calcXpol(co, xp) - g["xpol"]) <= tol
+    assert abs(E.calcMainBeam(co, surf, fit) - g["mainbeam"]) <= tol
+    with pytest.raises(ValueError, match="points"):
+        E.calcSpillover(co.ravel()[:-1], surf, ell)

@@ -130,6 +130,33 @@ def test_device_main_beam_matches_reference():
     assert eff == pytest.approx(float(_golden()["airy_ff__mainbeam_s0"]), rel=1e-5)
 
 
+@pytest.mark.parametrize("key", [k for k in _keys() if "__s0__" in k])
+def test_reference_signature_fit_matches_reference(key):
+    """FitGauss.fitGaussAbs with the reference's own arguments (the numpy
+    field and the surface's reflector dict; the grid made on the device)."""
+    from pypo_gb300 import fitgauss as FG
+    from tests.common import from_json
+    name, scale, thres, ratio = _parse(key)
+    g = _golden()
+    surf = from_json(str(g[name + "__surface_json"]))
+    popt = FG.fitGaussAbs(g[name + "__field"], surf, thres, scale, ratio)
+    np.testing.assert_allclose(popt[SHAPE], g[key][SHAPE], rtol=RTOL, atol=ATOL)
+
+
+@pytest.mark.parametrize("scale", [0, 2])
+def test_reference_signature_gaussian_matches_oracle(scale):
+    from pypo_gb300 import fitgauss as FG
+    from tests.common import from_json
+    g = _golden()
+    surf = from_json(str(g["airy_ff__surface_json"]))
+    x, y = g["airy_ff__x"], g["airy_ff__y"]
+    p = np.array([0.11, 0.08, 0.03, -0.02, 1.86, 1.0])
+    psi = FG.generateGauss(p, surf, scale)
+    ref = OF.gaussian(p, x, y, scale)
+    assert psi.shape == x.shape
+    np.testing.assert_allclose(psi, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
+
+
 @pytest.mark.parametrize("scale", [0, 2])
 def test_device_gaussian_matches_oracle(scale):
     from pypo_gb300 import fitgauss as FG
