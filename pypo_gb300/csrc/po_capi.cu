@@ -73,6 +73,25 @@ int device_m_is_zero(const double *d_cur, long ns, cudaStream_t s, bool &zero)
         }                                                                                 \
     } while (0)
 
+// Host slot for the frame's half-extent read back by a host-buffer call. It
+// is page-locked so that the copy stays asynchronous: a device-to-host copy
+// into pageable memory makes the host wait for all of the call's kernels
+// before it can queue the output copies. Pageable (the caller's slot) if
+// pinning fails. One small page-locked block per calling thread, kept.
+double *extent_slot(double *pageable)
+{
+    thread_local double *pinned = nullptr;
+    thread_local bool tried = false;
+    if (!tried) {
+        tried = true;
+        if (cudaMallocHost(&pinned, sizeof(double)) != cudaSuccess) {
+            pinned = nullptr;
+            (void)cudaGetLastError();
+        }
+    }
+    return pinned ? pinned : pageable;
+}
+
 // Host buffers in, host buffers out; synchronous.
 int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
              const double *tgt7, double k, double eps, double t, int precision, double *out)
@@ -134,15 +153,15 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
         if ((rc = device_m_is_zero(d_cur, ns, s, mz))) goto done;
         a.m_zero = mz;
     }
-    a.extent_host = &extent;
+    a.extent_host = extent_slot(&extent);
+    *a.extent_host = 0.0;
     a.out = d_out;
     a.stream = s;
     rc = po::run_device(a);
     if (rc) goto done;
     CK(cudaMemcpyAsync(out, d_out, sizeof(double) * nout * nt, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (precision == 0) t_extent = extent;
-    rc = po::read_device_error(s, &code);
+    rc = po::read_device_error(s, &code);   // the call's one synchronisation
+    if (!rc && precision == 0) t_extent = *a.extent_host;
     if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
                                       std::to_string(code) + "); results are invalid");
 done:
@@ -150,7 +169,7 @@ done:
     if (d_cur) cudaFreeAsync(d_cur, s);
     if (d_tgt) cudaFreeAsync(d_tgt, s);
     if (d_out) cudaFreeAsync(d_out, s);
-    if (s) cudaStreamSynchronize(s);
+    if (s && rc) cudaStreamSynchronize(s);   // copies from the caller's buffers may still be in flight
     return rc;
 }
 
@@ -404,6 +423,8 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     double *d_gc = nullptr, *d_gs = nullptr, *d_gt = nullptr;
     int rc = 0, code = 0;
     double extent = 0.0;
+    double *ext = extent_slot(&extent);
+    *ext = 0.0;
     const size_t ns1 = std::max(ns, 1L), nt1 = std::max(nt, 1L);
     CK(cudaMallocAsync(&d_src, sizeof(double) * 7 * ns1, s));
     CK(cudaMallocAsync(&d_cur, sizeof(double) * 12 * ns1, s));
@@ -424,21 +445,20 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
         bool mz = false;
         if (ns > 0 && (rc = device_m_is_zero(d_cur, ns, s, mz))) goto done;
         rc = adjoint_dev(mode, ns, d_src, gmode, ncx, ncy, d_cur, nt, d_tgt, k, epsilon, t_direction, precision,
-                         mz ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s, &extent);
+                         mz ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s, ext);
     }
     if (rc) goto done;
     if (grad_cur && ns > 0) CK(cudaMemcpyAsync(grad_cur, d_gc, sizeof(double) * 12 * ns, cudaMemcpyDeviceToHost, s));
     if (grad_ds && ns > 0) CK(cudaMemcpyAsync(grad_ds, d_gs, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
     if (grad_dt && nt > 0) CK(cudaMemcpyAsync(grad_dt, d_gt, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (precision == 0) t_extent = extent;
-    rc = po::read_device_error(s, &code);
+    rc = po::read_device_error(s, &code);   // the call's one synchronisation
+    if (!rc && precision == 0) t_extent = *ext;
     if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
                                       std::to_string(code) + "); results are invalid");
 done:
     for (double *p : {d_src, d_cur, d_tgt, d_cot, d_gc, d_gs, d_gt})
         if (p) cudaFreeAsync(p, s);
-    if (s) cudaStreamSynchronize(s);
+    if (s && rc) cudaStreamSynchronize(s);   // copies from the caller's buffers may still be in flight
     return rc;
 }
 

@@ -36,6 +36,7 @@ struct DeviceInfo {
 
 std::mutex g_mu;
 DeviceInfo g_dev[64];
+constexpr uint64_t kPoolKeep = 16ull << 30;   // freed scratch a device's pool keeps (bytes)
 
 // Timing ring: CUDA event pairs recorded around each main-kernel launch.
 struct Timing {
@@ -96,6 +97,15 @@ static int device_info(DeviceInfo *&out)
     DeviceInfo &di = g_dev[dev];
     if (!di.ready) {
         PO_CK(cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev));
+        // Scratch comes from the device's stream-ordered pool, which by
+        // default hands freed memory back to the driver at every
+        // synchronisation, so each host-buffer call (which synchronises)
+        // would map its scratch afresh. Keep up to kPoolKeep bytes of freed
+        // scratch in this process's pool instead.
+        cudaMemPool_t pool;
+        PO_CK(cudaDeviceGetMemPool(&pool, dev));
+        uint64_t keep = kPoolKeep;
+        PO_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
         for (int kind = 0; kind < 3; ++kind)
             for (int ts = 0; ts < 2; ++ts)
                 for (int hm = 0; hm < 2; ++hm) {
@@ -223,9 +233,9 @@ int read_device_error(cudaStream_t s, int *code)
 {
     int *w = error_word();
     if (!w) return fail(2, "no device error word");
+    PO_CK(cudaMemcpyAsync(code, w, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PO_CK(cudaMemsetAsync(w, 0, sizeof(int), s));
     PO_CK(cudaStreamSynchronize(s));
-    PO_CK(cudaMemcpy(code, w, sizeof(int), cudaMemcpyDeviceToHost));
-    PO_CK(cudaMemset(w, 0, sizeof(int)));
     return 0;
 }
 
@@ -368,7 +378,11 @@ int run_adjoint(const AdjArgs &a)
         return fail(1, "the adjoint covers modes JM, EH, JMEH and FF (EHP is nonlinear, scalar not built)");
     if (a.mode == kFF && a.grad_dt) return fail(1, "far-field targets are directions: no target displacement");
     if (a.nt > 0 && !a.cot) return fail(1, "null cotangent buffer");
-    if (a.ns == 0) return 0;
+    if (a.ns == 0) {
+        // no sources: the target gradient is zero (the source gradients are empty)
+        if (a.grad_dt && a.nt > 0) PO_CK(cudaMemsetAsync(a.grad_dt, 0, sizeof(double) * a.nt, a.stream));
+        return 0;
+    }
     if (a.nt == 0) {
         // no targets: every gradient is zero
         if (a.grad_cur) PO_CK(cudaMemsetAsync(a.grad_cur, 0, sizeof(double) * 12 * a.ns, a.stream));

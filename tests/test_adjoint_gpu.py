@@ -218,3 +218,29 @@ def test_adjoint_with_no_targets_or_no_sources(cuda, lib):
                 g = engine.adjoint(mode, np.zeros((7, 0)), np.zeros((12, 0)), -1, 0, 0, t7, 3.0,
                                    rng.standard_normal((12, t7.shape[1])), precision=prec)
                 assert g["cur"].shape == (12, 0) and g["ds"].shape == (0,) and np.all(g["dt"] == 0)
+
+
+def test_empty_adjoints_write_their_zeros(cuda, lib):
+    """Device buffers the caller hands in hold whatever was there before:
+    the empty cases must write their zero gradients, not leave the buffers
+    alone (a recycled allocation is not zero)."""
+    import torch
+    from pypo_gb300 import engine, surfaces as SF
+    rng = np.random.default_rng(5)
+    s7 = torch.tensor(engine.generate_grid(SF.paraboloid(3.0, [5, 6], gmode=1, lims_a=[0.2, 2.0])), device=cuda)
+    t7 = torch.tensor(engine.generate_grid(SF.translate(SF.plane([4, 3], gmode=0, lims_a=[-1, 1]), dz=3.0)),
+                      device=cuda)
+    nan = lambda *shape: torch.full(shape, float("nan"), dtype=torch.float64, device=cuda)
+    cur = torch.tensor(rng.standard_normal((12, 30)), device=cuda)
+    for prec in ("mixed", "fp64"):
+        # no targets: the source gradients are zero
+        gc, gs, _ = engine.adjoint_dev("EH", s7, cur, 1, 5, 6, t7[:, :0].contiguous(), 3.0,
+                                       nan(12, 0), precision=prec, grad_cur=nan(12, 30), grad_ds=nan(30))
+        torch.cuda.synchronize()
+        assert torch.all(gc == 0) and torch.all(gs == 0), prec
+        # no sources: the target gradient is zero
+        _, _, gt = engine.adjoint_dev("EH", s7[:, :0].contiguous(), cur[:, :0].contiguous(), -1, 0, 0, t7, 3.0,
+                                      torch.tensor(rng.standard_normal((12, 12)), device=cuda), precision=prec,
+                                      grad_dt=nan(12))
+        torch.cuda.synchronize()
+        assert torch.all(gt == 0), prec
