@@ -348,11 +348,16 @@ int run_device(const RunArgs &a)
     void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcf};
     const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
     if (!rc && ns > 0) rc = launch(pack_src2_kernel(), dim3(nblk_p), dim3(256), psargs, 0, s);
+    // tile boxes for the lit-tile proof (the scalar kind has no illumination test)
+    float2 *rec2 = reinterpret_cast<float2 *>(srcpk);
+    void *sbargs[] = {&rec2, &ns};
+    int boxes = !scalar && !has_m && ns > 0;   // the lit-tile proof serves the M = 0 kernels
+    if (!rc && boxes) rc = launch(src_box_kernel(), dim3((unsigned)tiles), dim3(32), sbargs, 0, s);
     int farflag = far ? 1 : 0;
     void *ptargs[] = {&nt, &tgt7, &frame, &farflag, &tgtpk};
     if (!rc) rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
     const float4 *srcc = srcpk, *tgtc = tgtpk;
-    void *margs[] = {&srcc, &ns, &chunk, &tgtc, &nt, &part, &err};
+    void *margs[] = {&srcc, &ns, &chunk, &tgtc, &nt, &part, &err, &boxes};
     timing_mark(s, true);
     if (!rc)
         rc = launch(pk_kernel(kind, ts, has_m), dim3((unsigned)ntb, (unsigned)nsplit), dim3(kThreads), margs,

@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "po_device.cuh"
 #include "po_kernels.cuh"
@@ -50,7 +51,9 @@ namespace po {
 // one of nf_pair; the sign (-1)^q of the half-turn sin/cos reduction is folded
 // into u, and the illumination test is a per-lane select of 1/R.
 
-template <int T, bool HAS_M>
+// LIT: the tile is proven lit (every pair passes the illumination test), so
+// the per-pair test is left out; the result is the same bits.
+template <int T, bool HAS_M, bool LIT>
 __device__ __forceinline__ void nf_pair2(float2 *acc, const float2 *th, const float2 *tl, const float2 *r)
 {
     const float2 dhx = sub2(th[0], r[0]), dhy = sub2(th[1], r[1]), dhz = sub2(th[2], r[2]);
@@ -64,8 +67,11 @@ __device__ __forceinline__ void nf_pair2(float2 *acc, const float2 *th, const fl
     float2 sn, cs, tq;
     phase_sincos2(S0, S1, Rh, rinv0, sn, cs, tq);
     const float2 dx = add2(dhx, dlx), dy = add2(dhy, dly), dz = add2(dhz, dlz);
-    const float2 w = fma2(dup2(kTangentTol32), Rh, fma2(r[8], dz, fma2(r[7], dy, mul2(r[6], dx))));
-    const float2 rinv = make_float2(w.x >= 0.0f ? rinv0.x : 0.0f, w.y >= 0.0f ? rinv0.y : 0.0f);
+    float2 rinv = rinv0;
+    if (!LIT) {
+        const float2 w = fma2(dup2(kTangentTol32), Rh, fma2(r[8], dz, fma2(r[7], dy, mul2(r[6], dx))));
+        rinv = make_float2(w.x >= 0.0f ? rinv0.x : 0.0f, w.y >= 0.0f ? rinv0.y : 0.0f);
+    }
     const float2 ex = mul2(dx, rinv), ey = mul2(dy, rinv), ez = mul2(dz, rinv);
     const float2 u = mul2(rinv, dup2(0.159154943091895336f));
     const float2 us = flip_parity(u, tq);
@@ -127,7 +133,7 @@ __device__ __forceinline__ void nf_pair2(float2 *acc, const float2 *th, const fl
 // Far field, pair-packed: tc = (rh xyz, rl xyz, r xyz) of the thread's
 // direction (r = rh + rl), r = the pair-packed record (slots 0-2 hi position,
 // 3-5 lo position, 6-8 normal, 9-14 J', 15-20 M').
-template <int T, bool HAS_M>
+template <int T, bool HAS_M, bool LIT>
 __device__ __forceinline__ void ff_pair2(float2 *acc, const float2 *tc, const float2 *r)
 {
     // r' . r_hat in turns: hi products are exact (hi parts have few bits)
@@ -136,12 +142,19 @@ __device__ __forceinline__ void ff_pair2(float2 *acc, const float2 *tc, const fl
                       fma2(r[1], tc[4], mul2(r[0], tc[3]))))));
     float2 sn, cs, tq;
     ff_phase_sincos2(Ph, Pl, sn, cs, tq);
-    const float2 ndr = fma2(r[8], tc[8], fma2(r[7], tc[7], mul2(r[6], tc[6])));
-    // G = e^{-t j theta}; (-1)^q and the illumination mask in one per-lane factor
-    const float2 one = flip_parity(dup2(1.0f), tq);
-    const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
-    const float2 gc = mul2(cs, m);
-    const float2 gs = mul2(T > 0 ? neg2(sn) : sn, m);
+    // G = e^{-t j theta}; (-1)^q and the illumination mask in one per-lane
+    // factor, or (lit tile) the sign (-1)^q alone, set on the bits
+    float2 gc, gs;
+    if (LIT) {
+        gc = flip_parity(cs, tq);
+        gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
+    } else {
+        const float2 ndr = fma2(r[8], tc[8], fma2(r[7], tc[7], mul2(r[6], tc[6])));
+        const float2 one = flip_parity(dup2(1.0f), tq);
+        const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
+        gc = mul2(cs, m);
+        gs = mul2(T > 0 ? neg2(sn) : sn, m);
+    }
     acc[0] = fma2(neg2(gs), r[10], fma2(gc, r[9], acc[0]));
     acc[3] = fma2(gs, r[9], fma2(gc, r[10], acc[3]));
     acc[1] = fma2(neg2(gs), r[12], fma2(gc, r[11], acc[1]));
@@ -180,16 +193,45 @@ __device__ __forceinline__ void sc_pair2(float2 *acc, const float2 *tc, const fl
     acc[1] = fma2(gi, r[6], fma2(gr, r[7], acc[1]));
 }
 
+// Whether every (source, target) pair of a tile passes the illumination
+// test, proven from the tile's box and the CTA's target box tb (lo xyz,
+// hi xyz, a bound on |t|_1). The tile's box (po_src_box_kernel: lowest and
+// highest normal xyz, largest n.s, largest |s|_1) travels with the tile in
+// the unused slot 21 of its first four pair records, so it arrives in
+// shared memory with the tile's copy. Near field: n.(t - s) >= min over the
+// boxes of n.t - max n.s, required above a margin of 1e-5 (|t|_1 + |s|_1)
+// for the FP32 rounding of both sides (the test is n.d + 5e-7 R >= 0). Far
+// field: n.r_hat >= 1e-5 (the test is n.r_hat >= -5e-7). The least of n t
+// over n in [a, b], t in [c, d] is the least of the four corner products.
+template <int KIND, int REC>
+__device__ __forceinline__ bool tile_lit(const float4 *tile, const float *tb)
+{
+    const float *f = reinterpret_cast<const float *>(tile);
+    float bx[kBoxF];
+#pragma unroll
+    for (int q = 0; q < kBoxF; ++q) bx[q] = f[(q >> 1) * REC * 4 + 42 + (q & 1)];
+    float L = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float a = bx[c], b = bx[3 + c];
+        L += fminf(fminf(a * tb[c], a * tb[3 + c]), fminf(b * tb[c], b * tb[3 + c]));
+    }
+    if (KIND == kKindFF) return L >= 1e-5f;
+    return L - bx[6] >= 1e-5f * (tb[6] + bx[7]);
+}
+
 // Pair-packed main kernel of all three kinds. Grid = (target blocks, source
 // chunks): blockIdx.y picks a chunk of sources (a multiple of kTile, so
 // chunks start on a pair boundary), whose tiles of kTile/2 pair records
 // stream through kStages TMA stages. The thread's target is duplicated into
 // both lanes once: near field and scalar (hi xyz, lo xyz), far field
-// (r_hat hi xyz, lo xyz, full xyz).
+// (r_hat hi xyz, lo xyz, full xyz). With `boxes` (po_src_box_kernel has run
+// on the records), a tile proven lit for the CTA skips the per-pair
+// illumination test (M = 0 kernels).
 template <int KIND, int T, bool HAS_M, int TP>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
 po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt, long nt,
-             double *__restrict__ part, int *__restrict__ err)
+             double *__restrict__ part, int *__restrict__ err, int boxes)
 {
     constexpr int PT = kTile / 2;                                       // pairs per tile
     constexpr int REC = KIND == kKindScalar ? kRec2Scalar : kRec2;      // float4 per pair record
@@ -218,6 +260,50 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
         tc[j][6] = dup2(a.x + a.w);
         tc[j][7] = dup2(a.y + c.x);
         tc[j][8] = dup2(a.z + c.y);
+    }
+
+    // The CTA's target box for the lit-tile proof: positions (hi + lo, turns)
+    // or directions, and a bound on |t|_1, over its real targets. The proof
+    // and its second copy of the pair loop are built for M = 0 only: with the
+    // magnetic terms the two-copy kernel measured slower in both copies
+    // (feed 101^2 -> dish 101^2, JM: 0.566 ms with one copy, 0.592 lit and
+    // 0.631 unlit with two).
+    constexpr bool kLitPath = KIND != kKindScalar && !HAS_M;
+    __shared__ float tbox_w[kThreads / 32][6];
+    __shared__ float tbox[7];
+    if (kLitPath) {
+        float v[6] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F};
+#pragma unroll
+        for (int j = 0; j < TP; ++j) {
+            if (tbase + (long)j * kThreads >= nt) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float x = KIND == kKindFF ? tc[j][6 + c].x : tc[j][c].x + tc[j][3 + c].x;
+                v[c] = fminf(v[c], x);
+                v[3 + c] = fmaxf(v[3 + c], x);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float u = __shfl_xor_sync(0xffffffffu, v[q], o);
+                v[q] = q < 3 ? fminf(v[q], u) : fmaxf(v[q], u);
+            }
+        if ((threadIdx.x & 31) == 0)
+#pragma unroll
+            for (int q = 0; q < 6; ++q) tbox_w[threadIdx.x >> 5][q] = v[q];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float a = 0.0f;   // sum of max(|lo|, |hi|): bounds |t|_1 of every target in the box
+            for (int q = 0; q < 6; ++q) {
+                float r = tbox_w[0][q];
+                for (int w = 1; w < kThreads / 32; ++w) r = q < 3 ? fminf(r, tbox_w[w][q]) : fmaxf(r, tbox_w[w][q]);
+                tbox[q] = r;
+            }
+            for (int c = 0; c < 3; ++c) a += fmaxf(fabsf(tbox[c]), fabsf(tbox[3 + c]));
+            tbox[6] = a;
+        }
     }
 
     float hi[TP][NACC];
@@ -269,21 +355,34 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
 #pragma unroll
             for (int a = 0; a < NACC; ++a) acc[j][a] = make_float2(0.f, 0.f);
 
+        auto pairs = [&](auto lit_c) {
+            constexpr bool LIT = decltype(lit_c)::value;
 #pragma unroll kUnrollF
-        for (int s = 0; s < cnt; ++s) {
-            float2 rec[2 * NLD];
+            for (int s = 0; s < cnt; ++s) {
+                float2 rec[2 * NLD];
 #pragma unroll
-            for (int q = 0; q < NLD; ++q) {
-                const float4 v = tile[s * REC + q];
-                rec[2 * q] = make_float2(v.x, v.y);
-                rec[2 * q + 1] = make_float2(v.z, v.w);
-            }
+                for (int q = 0; q < NLD; ++q) {
+                    const float4 v = tile[s * REC + q];
+                    rec[2 * q] = make_float2(v.x, v.y);
+                    rec[2 * q + 1] = make_float2(v.z, v.w);
+                }
 #pragma unroll
-            for (int j = 0; j < TP; ++j) {
-                if (KIND == kKindNF) nf_pair2<T, HAS_M>(acc[j], tc[j], tc[j] + 3, rec);
-                else if (KIND == kKindFF) ff_pair2<T, HAS_M>(acc[j], tc[j], rec);
-                else sc_pair2<T>(acc[j], tc[j], rec);
+                for (int j = 0; j < TP; ++j) {
+                    if (KIND == kKindNF) nf_pair2<T, HAS_M, LIT>(acc[j], tc[j], tc[j] + 3, rec);
+                    else if (KIND == kKindFF) ff_pair2<T, HAS_M, LIT>(acc[j], tc[j], rec);
+                    else sc_pair2<T>(acc[j], tc[j], rec);
+                }
             }
+        };
+        // block-uniform: every thread reads the same tile box and target box
+        // (a tile of fewer than 4 pair records carries no box)
+        if constexpr (kLitPath) {
+            if (boxes && cnt >= 4 && tile_lit<KIND, REC>(tile, tbox))
+                pairs(std::true_type{});
+            else
+                pairs(std::false_type{});
+        } else {
+            pairs(std::false_type{});
         }
 #pragma unroll
         for (int j = 0; j < TP; ++j)
@@ -479,6 +578,51 @@ __global__ void po_pack_src2_kernel(long ns, const double *__restrict__ src7, co
     }
     float *o = out + (i >> 1) * (rec4 * 4) + (i & 1);
     for (int q = 0; q < 2 * rec4; ++q) o[2 * q] = v[q];
+}
+
+// Box of each source tile (kTile sources = kTile / 2 pair records) for the
+// lit-tile proof of po_pk_kernel: lowest normal xyz, highest normal xyz,
+// largest n.s and largest |s|_1 (s = hi + lo, turns), kBoxF floats written
+// into the unused slot 21 of the tile's first four pair records. One warp
+// per tile; the padding source of an odd count repeats the last source, so
+// it changes nothing.
+__global__ void po_src_box_kernel(float2 *__restrict__ rec, long ns)
+{
+    constexpr int PT = kTile / 2;
+    constexpr int R2 = 2 * kRec2;   // float2 slots per pair record
+    float v[kBoxF] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F,
+                      -CUDART_INF_F, 0.0f};
+    const long np = (ns + 1) / 2;
+    for (int p = threadIdx.x; p < PT; p += 32) {
+        const long pair = (long)blockIdx.x * PT + p;
+        if (pair >= np) break;
+        const float2 *r = rec + pair * R2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float sv[3], nv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                sv[c] = (h ? r[c].y : r[c].x) + (h ? r[3 + c].y : r[3 + c].x);
+                nv[c] = h ? r[6 + c].y : r[6 + c].x;
+                v[c] = fminf(v[c], nv[c]);
+                v[3 + c] = fmaxf(v[3 + c], nv[c]);
+            }
+            v[6] = fmaxf(v[6], fmaf(nv[2], sv[2], fmaf(nv[1], sv[1], nv[0] * sv[0])));
+            v[7] = fmaxf(v[7], fabsf(sv[0]) + fabsf(sv[1]) + fabsf(sv[2]));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < kBoxF; ++q) {
+            const float u = __shfl_xor_sync(0xffffffffu, v[q], o);
+            v[q] = q < 3 ? fminf(v[q], u) : fmaxf(v[q], u);
+        }
+    if (threadIdx.x < kBoxF) {
+        const long pair = (long)blockIdx.x * PT + (threadIdx.x >> 1);
+        float *slot = reinterpret_cast<float *>(rec + pair * R2 + 21);
+        if (pair < np) slot[threadIdx.x & 1] = v[threadIdx.x];
+    }
 }
 
 // Near-field / scalar targets: hi/lo split positions in the same frame.
@@ -811,6 +955,7 @@ void *pk_kernel(int kind, int t_sign, bool has_m)
 }
 
 void *pack_src2_kernel() { return reinterpret_cast<void *>(&po_pack_src2_kernel); }
+void *src_box_kernel() { return reinterpret_cast<void *>(&po_src_box_kernel); }
 void *bbox_kernel() { return reinterpret_cast<void *>(&po_bbox_kernel); }
 void *frame_kernel() { return reinterpret_cast<void *>(&po_frame_kernel); }
 void *pack_src_kernel() { return reinterpret_cast<void *>(&po_pack_src_kernel); }

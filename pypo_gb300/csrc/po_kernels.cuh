@@ -36,6 +36,7 @@ constexpr int kRecScalar = 2;   // float4 per packed scalar record (32 B)
 constexpr int kAcc = 12;        // accumulators per target (E, H re/im x y z)
 constexpr int kRec2 = 11;       // float4 per pair-packed record (two sources), near and far field
 constexpr int kRec2Scalar = 4;  // float4 per pair-packed scalar record
+constexpr int kBoxF = 8;        // floats per source-tile box (lit-tile proof)
 #ifndef PO_MUFU_SINCOS
 #define PO_MUFU_SINCOS 1         // 0: the polynomial sin/cos (accuracy comparisons)
 #endif
@@ -102,6 +103,7 @@ inline int pk_smem_bytes(int kind)
 
 void *pk_kernel(int kind, int t_sign, bool has_m);
 void *pack_src2_kernel();
+void *src_box_kernel();
 void *fp64_kernel(int kind);
 void *bbox_kernel();
 void *frame_kernel();

@@ -121,6 +121,73 @@ def test_m_zero_kernel_matches_general_kernel(cuda, lib, oracle_mod):
     assert np.abs(got[6:]).max() > 0   # H from J alone is not zero
 
 
+def _plane_sources(rng, n, facing):
+    """n explicit source points on z = 0 in [-1, 1]^2, unit normal +z or -z
+    per point (facing: bool array), random weights and currents."""
+    s7 = np.zeros((7, n))
+    s7[0:2] = rng.uniform(-1, 1, (2, n))
+    s7[5] = np.where(facing, 1.0, -1.0)
+    s7[6] = rng.uniform(0.5, 1.5, n) * 1e-3
+    return s7, rng.standard_normal((12, n))
+
+
+def test_lit_tiles_give_the_bits_of_the_per_pair_test(cuda, lib):
+    """A source tile proven lit for a CTA's targets skips the per-pair
+    illumination test. One more target in the same CTA, lit by every source
+    but too close to the source plane for the proof's margin, turns the proof
+    off for the whole CTA (the grid frame is unchanged: the target is inside
+    the scene's box). The other targets' fields are the same bits."""
+    from pypo_gb300 import engine
+    rng = np.random.default_rng(21)
+    s7, cur = _plane_sources(rng, 1000, np.ones(1000, bool))
+    cur[6:] = 0.0                                    # the proof serves the M = 0 kernels
+    t7 = np.zeros((7, 100))
+    t7[0:2] = rng.uniform(-0.9, 0.9, (2, 100))
+    t7[2] = rng.uniform(0.5, 2.0, 100)
+    t7[5] = -1.0
+    near = t7[:, :1].copy()
+    near[2] = 1e-9                                   # n.d = 1e-9 mm > 0: lit, but inside the margin
+    k = 2 * np.pi / 0.05
+    for mode in ("EH", "JM"):
+        a = engine.propagate(mode, s7, cur, -1, 0, 0, t7, k)
+        b = engine.propagate(mode, s7, cur, -1, 0, 0, np.concatenate([t7, near], axis=1), k)
+        assert np.array_equal(a, b[:, :100]), mode
+    # far field: directions within 30 deg of +z, and one 1e-7 rad inside the horizon
+    d = np.zeros((7, 300))
+    d[0] = rng.uniform(0, np.radians(30), 300)
+    d[1] = rng.uniform(0, 2 * np.pi, 300)
+    edge = d[:, :1].copy()
+    edge[0] = np.pi / 2 - 1e-7
+    a = engine.propagate("FF", s7, cur, -1, 0, 0, d, k)
+    b = engine.propagate("FF", s7, cur, -1, 0, 0, np.concatenate([d, edge], axis=1), k)
+    assert np.array_equal(a, b[:, :300])
+
+
+def test_tiles_facing_both_ways_against_oracle(cuda, lib, oracle_mod):
+    """Sources that face the targets, sources that face away, and a tile that
+    holds both: lit tiles take the proven path, the others the per-pair
+    test; near and far field against the oracle."""
+    rng = np.random.default_rng(22)
+    facing = np.arange(700) < 300                     # tiles 0-1 face +z, tile 2 mixed, 3-5 face -z
+    s7, cur = _plane_sources(rng, 700, facing)
+    t7 = np.zeros((7, 150))
+    t7[0:2] = rng.uniform(-1, 1, (2, 150))
+    t7[2] = rng.uniform(0.3, 1.5, 150)
+    t7[5] = -1.0
+    k = 2 * np.pi / 0.1
+    d = np.zeros((7, 260))
+    d[0] = rng.uniform(0, np.radians(60), 260)
+    d[1] = rng.uniform(0, 2 * np.pi, 260)
+    for m_zero in (True, False):                      # with and without the proof
+        c = cur.copy()
+        if m_zero:
+            c[6:] = 0.0
+        for mode in ("EH", "JM"):
+            got = _check(mode, s7, c, -1, 0, 0, t7, k, oracle_mod)
+            assert np.abs(got).max() > 0
+        _check("FF", s7, c, -1, 0, 0, d, k, oracle_mod)
+
+
 def test_far_field_far_off_origin(cuda, lib, oracle_mod):
     """FF keeps the coordinate origin as phase reference; a displaced dish."""
     from pypo_gb300 import engine, surfaces as SF
