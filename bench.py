@@ -57,12 +57,13 @@ METRIC = "Gpairs/s fwd+adjoint, mixed-prec vs FP64 sum, 1 GB300 at ≤1e-5 rel e
 #: algorithmic FP32 flops per pair (FMA = 2; split-precision overhead not counted)
 FWD_FLOPS = {("EH", True): 234, ("EH", False): 140, ("FF", True): 61, ("FF", False): 37}
 # Adjoint. Near field: the fused kernel (currents 12 rows, source displacement
-# 416 flops/pair, plus 62 for the target displacement sharing the pair's
-# geometry, phase, coefficients and S); sources with M add 134 (source side:
-# alpha 24, M.R_hat 10, beta 8, M x R_hat 18, W.R_hat 24, W.n_s 24, b.n_s 10,
-# grad(beta).n_s 16) and 50 (target side: M.n_t 10, grad(beta).n_t 16,
-# W.n_t 24). Far field: currents + source displacement, 99; with M, +24.
-ADJ_FLOPS = {("EH", False): 478, ("EH", True): 662, ("FF", False): 99, ("FF", True): 123}
+# 416 flops/pair, plus 50 for the target displacement sharing the pair's
+# geometry, phase, coefficients, S and Z = b x J - a x M, from which
+# W.v = -v.Z for v = R_hat, n_s, n_t); sources with M add 116 (source side:
+# alpha 24, M.R_hat 10, beta 8, a x M into Z 48, b.n_s 10, grad(beta).n_s 16)
+# and 26 (target side: M.n_t 10, grad(beta).n_t 16). Far field: currents +
+# source displacement, 99; with M, +24.
+ADJ_FLOPS = {("EH", False): 466, ("EH", True): 608, ("FF", False): 99, ("FF", True): 123}
 
 
 def dist_env():

@@ -29,14 +29,14 @@ namespace po {
 
 // Pair-packed cotangent record, float2 slots (target 2p, target 2p + 1):
 //   0-2 hi position, 3-5 lo position (turns), 6-11 gE (re, im) x y z, 12-17 gH;
-//   with the target displacement: 18-20 n_t, 21-22 a.n_t, 23-28 n_t x b
-//   (re, im) x y z; with M as well: 29-30 b.n_t, 31-36 n_t x a
-//   (a = conj(gE), b = conj(gH)). A padding target has zero cotangent.
+//   with the target displacement: 18-20 n_t, 21-22 a.n_t; with M as well:
+//   23-24 b.n_t (a = conj(gE), b = conj(gH)). A padding target has zero
+//   cotangent.
 // Far field: 0-2 r_hat hi (on 2^-11), 3-5 r_hat lo, 6-11 gS_J, 12-17 gS_M,
 //   18-20 r_hat = hi + lo (11 float4).
 __host__ __device__ constexpr int adj2_rec(int kind, bool has_m, bool want_t)
 {
-    return kind == kKindFF ? 11 : (want_t ? (has_m ? 19 : 15) : 9);
+    return kind == kKindFF ? 11 : (want_t ? (has_m ? 13 : 12) : 9);
 }
 
 constexpr int kPairsA2 = PO_PAIRS_A;   // target pairs per shared-memory stage
@@ -52,7 +52,7 @@ __global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7
     const long k = i < nt ? i : nt - 1;
     const bool real = i < nt;
     const Frame fr = *frp;
-    float v[38];
+    float v[26];
     if (far) {
         const double th = tgt7[k], ph = tgt7[nt + k];
         const double rd[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
@@ -81,24 +81,17 @@ __global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7
         v[6 + q] = (float)ge[q];
         v[12 + q] = (float)gh[q];
     }
-    // a = conj(gE), b = conj(gH): a.n, n x b, b.n, n x a
+    // a = conj(gE), b = conj(gH): a.n and b.n
     for (int w = 0; w < 2; ++w) {
         const double *g = w == 0 ? ge : gh;
-        const double ar[3] = {g[0], g[2], g[4]}, ai[3] = {-g[1], -g[3], -g[5]};
-        const double dr = ar[0] * n[0] + ar[1] * n[1] + ar[2] * n[2];
-        const double di = ai[0] * n[0] + ai[1] * n[1] + ai[2] * n[2];
-        const double cr[3] = {n[1] * ar[2] - n[2] * ar[1], n[2] * ar[0] - n[0] * ar[2], n[0] * ar[1] - n[1] * ar[0]};
-        const double ci[3] = {n[1] * ai[2] - n[2] * ai[1], n[2] * ai[0] - n[0] * ai[2], n[0] * ai[1] - n[1] * ai[0]};
-        const int dot_at = w == 0 ? 21 : 29, cross_at = w == 0 ? 31 : 23;   // a.n, n x a | b.n, n x b
+        const double dr = g[0] * n[0] + g[2] * n[1] + g[4] * n[2];
+        const double di = -(g[1] * n[0] + g[3] * n[1] + g[5] * n[2]);
+        const int dot_at = w == 0 ? 21 : 23;   // a.n | b.n
         v[dot_at] = (float)dr;
         v[dot_at + 1] = (float)di;
-        for (int c = 0; c < 3; ++c) {
-            v[cross_at + 2 * c] = (float)cr[c];
-            v[cross_at + 2 * c + 1] = (float)ci[c];
-        }
     }
     for (int c = 0; c < 3; ++c) v[18 + c] = far ? v[c] + v[3 + c] : (float)n[c];
-    v[37] = 0.f;
+    v[25] = 0.f;
     float *o = out + (i >> 1) * (long)(rec4 * 4) + (i & 1);
     for (int q = 0; q < 2 * rec4; ++q) o[2 * q] = v[q];
 }
@@ -108,7 +101,6 @@ struct SrcC {
     float sh[3], sl[3], n[3];
     float J[6], M[6];            // (re, im) x y z
     float Jn[2], Mn[2];          // J.n_s, M.n_s
-    float Jxn[6], Mxn[6];        // J x n_s, M x n_s
 };
 
 // One pair of targets against the thread's source. acc: 12 current
@@ -186,12 +178,14 @@ __device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const floa
                       mul2(neg2(Exi), Jxr))))));
     const float2 jer = fma2(Jzr, ez, fma2(Jyr, ey, mul2(Jxr, ex))), jei = fma2(Jzi, ez, fma2(Jyi, ey, mul2(Jxi, ex)));
     float2 ber = fma2(jer, ger, mul2(jei, gei)), bei = fma2(jei, ger, mul2(neg2(jer), gei));
-    const float2 xxr = fma2(Jyr, ez, mul2(neg2(Jzr), ey)), xxi = fma2(Jyi, ez, mul2(neg2(Jzi), ey));
-    const float2 xyr = fma2(Jzr, ex, mul2(neg2(Jxr), ez)), xyi = fma2(Jzi, ex, mul2(neg2(Jxi), ez));
-    const float2 xzr = fma2(Jxr, ey, mul2(neg2(Jyr), ex)), xzi = fma2(Jxi, ey, mul2(neg2(Jyi), ex));
-    float2 wr = neg2(fma2(Hzr, xzr, fma2(Hzi, xzi, fma2(Hyr, xyr, fma2(Hyi, xyi, fma2(Hxr, xxr, mul2(Hxi, xxi)))))));
-    float2 wi = neg2(fma2(Hzr, xzi, fma2(neg2(Hzi), xzr, fma2(Hyr, xyi, fma2(neg2(Hyi), xyr, fma2(Hxr, xxi,
-                     mul2(neg2(Hxi), xxr)))))));
+    // Z = b x J (- a x M): by the scalar triple product, W.v = -b.(J x v)
+    // (+ a.(M x v)) = -v.Z for each of v = R_hat, n_s and n_t.
+    float2 zxr = fma2(Hyr, Jzr, fma2(Hyi, Jzi, fma2(neg2(Hzr), Jyr, mul2(neg2(Hzi), Jyi))));
+    float2 zxi = fma2(Hyr, Jzi, fma2(neg2(Hyi), Jzr, fma2(neg2(Hzr), Jyi, mul2(Hzi, Jyr))));
+    float2 zyr = fma2(Hzr, Jxr, fma2(Hzi, Jxi, fma2(neg2(Hxr), Jzr, mul2(neg2(Hxi), Jzi))));
+    float2 zyi = fma2(Hzr, Jxi, fma2(neg2(Hzi), Jxr, fma2(neg2(Hxr), Jzi, mul2(Hxi, Jzr))));
+    float2 zzr = fma2(Hxr, Jyr, fma2(Hxi, Jyi, fma2(neg2(Hyr), Jxr, mul2(neg2(Hyi), Jxi))));
+    float2 zzi = fma2(Hxr, Jyi, fma2(neg2(Hxi), Jyr, fma2(neg2(Hyr), Jxi, mul2(Hyi, Jxr))));
     float2 mer = dup2(0.f), mei = dup2(0.f);
     if (HAS_M) {
         const float2 Mxr = dup2(s.M[0]), Mxi = dup2(s.M[1]), Myr = dup2(s.M[2]), Myi = dup2(s.M[3]);
@@ -203,13 +197,16 @@ __device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const floa
         mei = fma2(Mzi, ez, fma2(Myi, ey, mul2(Mxi, ex)));
         ber = fma2(mer, ghr, fma2(mei, ghi, ber));
         bei = fma2(mei, ghr, fma2(neg2(mer), ghi, bei));
-        const float2 yxr = fma2(Myr, ez, mul2(neg2(Mzr), ey)), yxi = fma2(Myi, ez, mul2(neg2(Mzi), ey));
-        const float2 yyr = fma2(Mzr, ex, mul2(neg2(Mxr), ez)), yyi = fma2(Mzi, ex, mul2(neg2(Mxi), ez));
-        const float2 yzr = fma2(Mxr, ey, mul2(neg2(Myr), ex)), yzi = fma2(Mxi, ey, mul2(neg2(Myi), ex));
-        wr = fma2(Ezr, yzr, fma2(Ezi, yzi, fma2(Eyr, yyr, fma2(Eyi, yyi, fma2(Exr, yxr, fma2(Exi, yxi, wr))))));
-        wi = fma2(Ezr, yzi, fma2(neg2(Ezi), yzr, fma2(Eyr, yyi, fma2(neg2(Eyi), yyr, fma2(Exr, yxi,
-                  fma2(neg2(Exi), yxr, wi))))));
+        // Z -= a x M
+        zxr = fma2(neg2(Eyr), Mzr, fma2(neg2(Eyi), Mzi, fma2(Ezr, Myr, fma2(Ezi, Myi, zxr))));
+        zxi = fma2(neg2(Eyr), Mzi, fma2(Eyi, Mzr, fma2(Ezr, Myi, fma2(neg2(Ezi), Myr, zxi))));
+        zyr = fma2(neg2(Ezr), Mxr, fma2(neg2(Ezi), Mxi, fma2(Exr, Mzr, fma2(Exi, Mzi, zyr))));
+        zyi = fma2(neg2(Ezr), Mxi, fma2(Ezi, Mxr, fma2(Exr, Mzi, fma2(neg2(Exi), Mzr, zyi))));
+        zzr = fma2(neg2(Exr), Myr, fma2(neg2(Exi), Myi, fma2(Eyr, Mxr, fma2(Eyi, Mxi, zzr))));
+        zzi = fma2(neg2(Exr), Myi, fma2(Exi, Myr, fma2(Eyr, Mxi, fma2(neg2(Eyi), Mxr, zzi))));
     }
+    const float2 wr = neg2(fma2(ez, zzr, fma2(ey, zyr, mul2(ex, zxr))));
+    const float2 wi = neg2(fma2(ez, zzi, fma2(ey, zyi, mul2(ex, zxi))));
     // Re S, S = G (D1 alpha + D2 beta + D3 w), G = (cs, t sn)
     const float2 u2 = mul2(u, u);
     const float2 p1 = fma2(dup2(-3.0f), u2, dup2(1.0f));
@@ -224,24 +221,17 @@ __device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const floa
     const float2 Sr = fma2(cs, xr, mul2(neg2(gi), xi));
 
     if (WANT_D) {
-        // W.n_s = -b.(J x n_s) (+ a.(M x n_s)); grad(beta).n_s = (a.R_hat)(J.n_s) + (J.R_hat)(a.n_s) (+ M terms)
-        const float *Jxn = s.Jxn;
-        float2 wnr = neg2(fma2(Hzr, dup2(Jxn[4]), fma2(Hzi, dup2(Jxn[5]), fma2(Hyr, dup2(Jxn[2]),
-                          fma2(Hyi, dup2(Jxn[3]), fma2(Hxr, dup2(Jxn[0]), mul2(Hxi, dup2(Jxn[1]))))))));
-        float2 wni = neg2(fma2(Hzr, dup2(Jxn[5]), fma2(neg2(Hzi), dup2(Jxn[4]), fma2(Hyr, dup2(Jxn[3]),
-                          fma2(neg2(Hyi), dup2(Jxn[2]), fma2(Hxr, dup2(Jxn[1]), mul2(neg2(Hxi), dup2(Jxn[0]))))))));
-        const float2 anr = fma2(Ezr, dup2(s.n[2]), fma2(Eyr, dup2(s.n[1]), mul2(Exr, dup2(s.n[0]))));
-        const float2 ani = neg2(fma2(Ezi, dup2(s.n[2]), fma2(Eyi, dup2(s.n[1]), mul2(Exi, dup2(s.n[0])))));
+        // W.n_s = -n_s.Z; grad(beta).n_s = (a.R_hat)(J.n_s) + (J.R_hat)(a.n_s) (+ M terms)
+        const float2 nsx = dup2(s.n[0]), nsy = dup2(s.n[1]), nsz = dup2(s.n[2]);
+        const float2 wnr = neg2(fma2(nsz, zzr, fma2(nsy, zyr, mul2(nsx, zxr))));
+        const float2 wni = neg2(fma2(nsz, zzi, fma2(nsy, zyi, mul2(nsx, zxi))));
+        const float2 anr = fma2(Ezr, nsz, fma2(Eyr, nsy, mul2(Exr, nsx)));
+        const float2 ani = neg2(fma2(Ezi, nsz, fma2(Eyi, nsy, mul2(Exi, nsx))));
         float2 gbr = fma2(ger, dup2(s.Jn[0]), fma2(gei, dup2(s.Jn[1]), fma2(jer, anr, mul2(neg2(jei), ani))));
         float2 gbi = fma2(ger, dup2(s.Jn[1]), fma2(neg2(gei), dup2(s.Jn[0]), fma2(jer, ani, mul2(jei, anr))));
         if (HAS_M) {
-            const float *Mxn = s.Mxn;
-            wnr = fma2(Ezr, dup2(Mxn[4]), fma2(Ezi, dup2(Mxn[5]), fma2(Eyr, dup2(Mxn[2]), fma2(Eyi, dup2(Mxn[3]),
-                       fma2(Exr, dup2(Mxn[0]), fma2(Exi, dup2(Mxn[1]), wnr))))));
-            wni = fma2(Ezr, dup2(Mxn[5]), fma2(neg2(Ezi), dup2(Mxn[4]), fma2(Eyr, dup2(Mxn[3]),
-                       fma2(neg2(Eyi), dup2(Mxn[2]), fma2(Exr, dup2(Mxn[1]), fma2(neg2(Exi), dup2(Mxn[0]), wni))))));
-            const float2 bnr = fma2(Hzr, dup2(s.n[2]), fma2(Hyr, dup2(s.n[1]), mul2(Hxr, dup2(s.n[0]))));
-            const float2 bni = neg2(fma2(Hzi, dup2(s.n[2]), fma2(Hyi, dup2(s.n[1]), mul2(Hxi, dup2(s.n[0])))));
+            const float2 bnr = fma2(Hzr, nsz, fma2(Hyr, nsy, mul2(Hxr, nsx)));
+            const float2 bni = neg2(fma2(Hzi, nsz, fma2(Hyi, nsy, mul2(Hxi, nsx))));
             gbr = fma2(ghr, dup2(s.Mn[0]), fma2(ghi, dup2(s.Mn[1]), fma2(mer, bnr, fma2(neg2(mei), bni, gbr))));
             gbi = fma2(ghr, dup2(s.Mn[1]), fma2(neg2(ghi), dup2(s.Mn[0]), fma2(mer, bni, fma2(mei, bnr, gbi))));
         }
@@ -251,28 +241,22 @@ __device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const floa
         acc[12] = fma2(rinv, inner, acc[12]);
     }
     if (WANT_T) {
-        // W.n_t = -J.(n_t x b) (+ M.(n_t x a)); grad(beta).n_t = (a.R_hat)(J.n_t) + (J.R_hat)(a.n_t) (+ M terms)
+        // W.n_t = -n_t.Z; grad(beta).n_t = (a.R_hat)(J.n_t) + (J.R_hat)(a.n_t) (+ M terms)
         const float2 ntx = r[18], nty = r[19], ntz = r[20];
         const float2 ent = fma2(ez, ntz, fma2(ey, nty, mul2(ex, ntx)));
         const float2 jnr = fma2(Jzr, ntz, fma2(Jyr, nty, mul2(Jxr, ntx)));
         const float2 jni = fma2(Jzi, ntz, fma2(Jyi, nty, mul2(Jxi, ntx)));
         float2 gbr = fma2(ger, jnr, fma2(gei, jni, fma2(jer, r[21], mul2(neg2(jei), r[22]))));
         float2 gbi = fma2(ger, jni, fma2(neg2(gei), jnr, fma2(jer, r[22], mul2(jei, r[21]))));
-        float2 wnr = neg2(fma2(Jzr, r[27], fma2(neg2(Jzi), r[28], fma2(Jyr, r[25], fma2(neg2(Jyi), r[26],
-                          fma2(Jxr, r[23], mul2(neg2(Jxi), r[24])))))));
-        float2 wni = neg2(fma2(Jzr, r[28], fma2(Jzi, r[27], fma2(Jyr, r[26], fma2(Jyi, r[25],
-                          fma2(Jxr, r[24], mul2(Jxi, r[23])))))));
+        const float2 wnr = neg2(fma2(ntz, zzr, fma2(nty, zyr, mul2(ntx, zxr))));
+        const float2 wni = neg2(fma2(ntz, zzi, fma2(nty, zyi, mul2(ntx, zxi))));
         if (HAS_M) {
             const float2 Mxr = dup2(s.M[0]), Mxi = dup2(s.M[1]), Myr = dup2(s.M[2]), Myi = dup2(s.M[3]);
             const float2 Mzr = dup2(s.M[4]), Mzi = dup2(s.M[5]);
             const float2 mnr = fma2(Mzr, ntz, fma2(Myr, nty, mul2(Mxr, ntx)));
             const float2 mni = fma2(Mzi, ntz, fma2(Myi, nty, mul2(Mxi, ntx)));
-            gbr = fma2(ghr, mnr, fma2(ghi, mni, fma2(mer, r[29], fma2(neg2(mei), r[30], gbr))));
-            gbi = fma2(ghr, mni, fma2(neg2(ghi), mnr, fma2(mer, r[30], fma2(mei, r[29], gbi))));
-            wnr = fma2(Mzr, r[35], fma2(neg2(Mzi), r[36], fma2(Myr, r[33], fma2(neg2(Myi), r[34],
-                       fma2(Mxr, r[31], fma2(neg2(Mxi), r[32], wnr))))));
-            wni = fma2(Mzr, r[36], fma2(Mzi, r[35], fma2(Myr, r[34], fma2(Myi, r[33], fma2(Mxr, r[32],
-                       fma2(Mxi, r[31], wni))))));
+            gbr = fma2(ghr, mnr, fma2(ghi, mni, fma2(mer, r[23], fma2(neg2(mei), r[24], gbr))));
+            gbi = fma2(ghr, mni, fma2(neg2(ghi), mnr, fma2(mer, r[24], fma2(mei, r[23], gbi))));
         }
         const float2 inner = fma2(ent, Sr, fma2(C2r, gbr, fma2(neg2(C2i), gbi, fma2(C3r, wnr,
                                   mul2(neg2(C3i), wni)))));
@@ -356,14 +340,8 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
     for (int w = 0; w < 2; ++w) {
         const float *v = w == 0 ? s.J : s.M;
         float *dn = w == 0 ? s.Jn : s.Mn;
-        float *o = w == 0 ? s.Jxn : s.Mxn;
 #pragma unroll
-        for (int ri = 0; ri < 2; ++ri) {
-            dn[ri] = fmaf(v[4 + ri], s.n[2], fmaf(v[2 + ri], s.n[1], v[ri] * s.n[0]));
-            o[0 + ri] = fmaf(v[2 + ri], s.n[2], -v[4 + ri] * s.n[1]);
-            o[2 + ri] = fmaf(v[4 + ri], s.n[0], -v[0 + ri] * s.n[2]);
-            o[4 + ri] = fmaf(v[0 + ri], s.n[1], -v[2 + ri] * s.n[0]);
-        }
+        for (int ri = 0; ri < 2; ++ri) dn[ri] = fmaf(v[4 + ri], s.n[2], fmaf(v[2 + ri], s.n[1], v[ri] * s.n[0]));
     }
 
     float hi[kAccAdj];
@@ -477,6 +455,8 @@ int adj_pk_smem_bytes(int kind, bool has_m, bool want_t)
 }
 
 int adj_pk_pairs_per_tile() { return kPairsA2; }
+
+int adj_pk_rec4(int kind, bool has_m, bool want_t) { return adj2_rec(kind, has_m, want_t); }
 
 template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
 static void *adj_pk_ptr()

@@ -480,7 +480,7 @@ int run_adjoint(const AdjArgs &a)
     // Pair-packed adjoint: sources in registers, pairs of targets streamed.
     // Near field fused (currents, source and target displacement in one pass).
     const bool want_t = grad_dt != nullptr;
-    const int rec4 = far ? 11 : (want_t ? (has_m ? 19 : 15) : 9);
+    const int rec4 = adj_pk_rec4(kind, has_m, want_t);
     const long npair = (nt + 1) / 2;
     float *trec2 = nullptr;
     double *gt = nullptr;
