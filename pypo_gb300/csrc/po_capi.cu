@@ -1,6 +1,7 @@
 // po_capi.cu -- the extern "C" entry points of libpo_gb300 (include/po_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -62,6 +63,24 @@ int device_m_is_zero(const double *d_cur, long ns, cudaStream_t s, bool &zero)
     po::note_launches(1);
     zero = h == 0;
     return 0;
+}
+
+// Whether the magnetic currents of a host-buffer call are all zero. A
+// non-zero among the first kMPrefix values of the caller's host rows settles
+// it at once (no device round trip: currents with M, the common case of a
+// feed); otherwise the device checks all of them (device_m_is_zero), which
+// keeps the host from scanning a large M = 0 block.
+constexpr long kMPrefix = 4096;
+int m_is_zero(const double *h_cur, const double *d_cur, long ns, cudaStream_t s, bool &zero)
+{
+    const double *m = h_cur + 6 * ns;
+    const long n = std::min(6 * ns, kMPrefix);
+    for (long i = 0; i < n; ++i)
+        if (m[i] != 0.0) {   // -0.0 counts as zero, NaN as non-zero, as on the device
+            zero = false;
+            return 0;
+        }
+    return device_m_is_zero(d_cur, ns, s, zero);
 }
 
 #define CK(expr)                                                                          \
@@ -150,7 +169,7 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
     a.m_zero = false;
     if (mode != po::kScalar && ns > 0) {
         bool mz = false;
-        if ((rc = device_m_is_zero(d_cur, ns, s, mz))) goto done;
+        if ((rc = m_is_zero(cur, d_cur, ns, s, mz))) goto done;
         a.m_zero = mz;
     }
     a.extent_host = extent_slot(&extent);
@@ -443,7 +462,7 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     }
     {
         bool mz = false;
-        if (ns > 0 && (rc = device_m_is_zero(d_cur, ns, s, mz))) goto done;
+        if (ns > 0 && (rc = m_is_zero(cur, d_cur, ns, s, mz))) goto done;
         rc = adjoint_dev(mode, ns, d_src, gmode, ncx, ncy, d_cur, nt, d_tgt, k, epsilon, t_direction, precision,
                          mz ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s, ext);
     }

@@ -188,6 +188,22 @@ def test_tiles_facing_both_ways_against_oracle(cuda, lib, oracle_mod):
         _check("FF", s7, c, -1, 0, 0, d, k, oracle_mod)
 
 
+def test_magnetic_current_found_past_the_host_prefix(cuda, lib, oracle_mod):
+    """The host-buffer entries settle M = 0 from the first 4096 magnetic
+    values on the host, and the device checks the rest: a single non-zero M
+    at the last source must still select the kernel with magnetic terms."""
+    rng = np.random.default_rng(31)
+    src, s7, t7, cur = _random_case(rng, (64, 80), 120)
+    cur[6:] = 0.0
+    cur[11, -1] = 0.7                                  # Mz (im) of the last source only
+    _check("EH", s7, cur, 1, 64, 80, t7, 6.0, oracle_mod)
+    from pypo_gb300 import engine
+    cot = rng.standard_normal((12, t7.shape[1]))
+    g = engine.adjoint("EH", s7, cur, 1, 64, 80, t7, 6.0, cot)
+    g0 = engine.adjoint("EH", s7, np.where(np.arange(12)[:, None] >= 6, 0.0, cur), 1, 64, 80, t7, 6.0, cot)
+    assert not np.allclose(g["ds"], g0["ds"], rtol=0, atol=0)   # the last source's M term is in
+
+
 def test_far_field_far_off_origin(cuda, lib, oracle_mod):
     """FF keeps the coordinate origin as phase reference; a displaced dish."""
     from pypo_gb300 import engine, surfaces as SF
