@@ -20,7 +20,9 @@
 // Far field: the same kernel with the far-field pair (currents and source
 // displacement; far-field targets are directions and do not move).
 #include <cuda_runtime.h>
+#include <math_constants.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "po_device.cuh"
 #include "po_kernels.cuh"
@@ -268,7 +270,10 @@ __device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const floa
 //   Jbar' += conj(G) gS_J, Mbar' += conj(G) gS_M (G = e^{-t j k r'.r_hat}),
 //   source displacement: Re[-t j k G (conj(gS_J).J' + conj(gS_M).M')] (n_s . r_hat),
 // k in turns is 2 pi.
-template <int T, bool HAS_M, bool WANT_D>
+// LIT: the tile is proven lit for the CTA's sources (every pair passes the
+// illumination test), so the sign (-1)^q is set on the bits and the mask is
+// left out; the result is the same bits.
+template <int T, bool HAS_M, bool WANT_D, bool LIT>
 __device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const SrcC &s)
 {
     const float2 Ph = fma2(dup2(s.sh[2]), r[2], fma2(dup2(s.sh[1]), r[1], mul2(dup2(s.sh[0]), r[0])));
@@ -277,10 +282,16 @@ __device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const
     float2 sn, cs, tq;
     ff_phase_sincos2(Ph, Pl, sn, cs, tq);
     const float2 ndr = fma2(dup2(s.n[2]), r[20], fma2(dup2(s.n[1]), r[19], mul2(dup2(s.n[0]), r[18])));
-    const float2 one = flip_parity(dup2(1.0f), tq);
-    const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
-    const float2 gc = mul2(cs, m);                          // G = (gc, gs)
-    const float2 gs = mul2(T > 0 ? neg2(sn) : sn, m);
+    float2 gc, gs;                                          // G = (gc, gs)
+    if (LIT) {
+        gc = flip_parity(cs, tq);
+        gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
+    } else {
+        const float2 one = flip_parity(dup2(1.0f), tq);
+        const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
+        gc = mul2(cs, m);
+        gs = mul2(T > 0 ? neg2(sn) : sn, m);
+    }
     // conj(G) g = (gc g.re + gs g.im, gc g.im - gs g.re)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -308,10 +319,44 @@ __device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const
     }
 }
 
+// Direction box of each far-field cotangent tile (kPairsA2 pair records) for
+// the lit-tile proof of the far-field adjoint: lowest and highest r_hat per
+// axis, written into the unused slot 21 of the tile's first three pair
+// records. One warp per tile; the padding target of an odd count repeats
+// the last target, so it changes nothing.
+__global__ void po_adj_tgt_box_kernel(float2 *__restrict__ rec, long nt)
+{
+    constexpr int R2 = 2 * adj2_rec(kKindFF, false, false);   // float2 slots per pair record
+    float v[6] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F};
+    const long np = (nt + 1) / 2;
+    for (int p = threadIdx.x; p < kPairsA2; p += 32) {
+        const long pair = (long)blockIdx.x * kPairsA2 + p;
+        if (pair >= np) break;
+        const float2 *r = rec + pair * R2;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = fminf(v[c], fminf(r[18 + c].x, r[18 + c].y));
+            v[3 + c] = fmaxf(v[3 + c], fmaxf(r[18 + c].x, r[18 + c].y));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float u = __shfl_xor_sync(0xffffffffu, v[q], o);
+            v[q] = q < 3 ? fminf(v[q], u) : fmaxf(v[q], u);
+        }
+    if (threadIdx.x < 6) {
+        const long pair = (long)blockIdx.x * kPairsA2 + (threadIdx.x >> 1);
+        float *slot = reinterpret_cast<float *>(rec + pair * R2 + 21);
+        if (pair < np) slot[threadIdx.x & 1] = v[threadIdx.x];
+    }
+}
+
 template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
 __global__ void __launch_bounds__(kThreadsA, kMinBlocksA2)
 po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
-                 double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err)
+                 double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err, int boxes)
 {
     static_assert(KIND == kKindNF || !WANT_T, "far-field targets do not move");
     constexpr int RT = adj2_rec(KIND, HAS_M, WANT_T);
@@ -351,6 +396,41 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
         lo[a * kThreadsA + threadIdx.x] = 0.f;
     }
 
+    // Far field, M = 0: the CTA's box of source normals for the lit-tile
+    // proof (a tile's directions r_hat against it: min n.r_hat >= 1e-5, the
+    // least of n.r over the two boxes being the sum of the least corner
+    // products per axis; the test is n.r_hat >= -5e-7). Only there: the
+    // near-field adjoint needs n_s.R for its displacement gradient anyway,
+    // and a second copy of the loop is not worth its cost with M.
+    constexpr bool kLitA = KIND == kKindFF && !HAS_M;
+    __shared__ float nbox_w[kThreadsA / 32][6];
+    __shared__ float nbox[6];
+    if (kLitA) {
+        float v[6];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = si < ns ? s.n[c] : CUDART_INF_F;
+            v[3 + c] = si < ns ? s.n[c] : -CUDART_INF_F;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float u = __shfl_xor_sync(0xffffffffu, v[q], o);
+                v[q] = q < 3 ? fminf(v[q], u) : fmaxf(v[q], u);
+            }
+        if ((threadIdx.x & 31) == 0)
+#pragma unroll
+            for (int q = 0; q < 6; ++q) nbox_w[threadIdx.x >> 5][q] = v[q];
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            const int q = threadIdx.x;
+            float r = nbox_w[0][q];
+            for (int w = 1; w < kThreadsA / 32; ++w) r = q < 3 ? fminf(r, nbox_w[w][q]) : fmaxf(r, nbox_w[w][q]);
+            nbox[q] = r;
+        }
+    }
+
     const long t0 = (long)blockIdx.y * chunk;     // chunk: a multiple of 2 * kPairsA2 targets
     const long t1 = min(nt, t0 + chunk);
     const long p0 = t0 / 2, p1 = (t1 + 1) / 2;
@@ -387,21 +467,59 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
         float2 acc[kAccAdj];
 #pragma unroll
         for (int a = 0; a < kAccAdj; ++a) acc[a] = make_float2(0.f, 0.f);
+        // block-uniform: the tile's direction box (in the first three pair
+        // records, as po_adj_tgt_box_kernel wrote it) against the CTA's normals
+        [[maybe_unused]] bool lit = false;
+        if constexpr (kLitA) {
+            if (boxes && cnt >= 3) {
+                const float *f = reinterpret_cast<const float *>(tile);
+                float L = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float tl = f[(c >> 1) * RT * 4 + 42 + (c & 1)];
+                    const float th = f[((3 + c) >> 1) * RT * 4 + 42 + ((3 + c) & 1)];
+                    L += fminf(fminf(nbox[c] * tl, nbox[c] * th), fminf(nbox[3 + c] * tl, nbox[3 + c] * th));
+                }
+                lit = L >= 1e-5f;
+            }
+        }
         for (int fb = 0; fb < cnt; fb += kFlush) {
             const int fend = min(cnt, fb + kFlush);
+            if constexpr (kLitA) {
+                // far field, M = 0: two copies of the pair loop, with and without the test
+                auto pairs = [&](auto lit_c) {
+                    constexpr bool LIT = decltype(lit_c)::value;
 #pragma unroll kUnrollA
-            for (int p = fb; p < fend; ++p) {
-                float2 rec[NL];
+                    for (int p = fb; p < fend; ++p) {
+                        float2 rec[NL];
 #pragma unroll
-                for (int c = 0; c < RT; ++c) {
-                    const float4 v = tile[p * RT + c];
-                    rec[2 * c] = make_float2(v.x, v.y);
-                    rec[2 * c + 1] = make_float2(v.z, v.w);
+                        for (int c = 0; c < RT; ++c) {
+                            const float4 v = tile[p * RT + c];
+                            rec[2 * c] = make_float2(v.x, v.y);
+                            rec[2 * c + 1] = make_float2(v.z, v.w);
+                        }
+                        adj_ff_pair2<T, HAS_M, WANT_D, LIT>(acc, rec, s);
+                    }
+                };
+                if (lit)
+                    pairs(std::true_type{});
+                else
+                    pairs(std::false_type{});
+            } else {
+#pragma unroll kUnrollA
+                for (int p = fb; p < fend; ++p) {
+                    float2 rec[NL];
+#pragma unroll
+                    for (int c = 0; c < RT; ++c) {
+                        const float4 v = tile[p * RT + c];
+                        rec[2 * c] = make_float2(v.x, v.y);
+                        rec[2 * c + 1] = make_float2(v.z, v.w);
+                    }
+                    float2 vt = make_float2(0.f, 0.f);
+                    if (KIND == kKindNF) adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s);
+                    else adj_ff_pair2<T, HAS_M, WANT_D, false>(acc, rec, s);
+                    if (WANT_T) vbuf[(p - fb) * kThreadsA + threadIdx.x] = vt;
                 }
-                float2 vt = make_float2(0.f, 0.f);
-                if (KIND == kKindNF) adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s);
-                else adj_ff_pair2<T, HAS_M, WANT_D>(acc, rec, s);
-                if (WANT_T) vbuf[(p - fb) * kThreadsA + threadIdx.x] = vt;
             }
             if (WANT_T) {
                 // Sum the CTA's sources for each target pair of this flush: thread
@@ -457,6 +575,8 @@ int adj_pk_smem_bytes(int kind, bool has_m, bool want_t)
 int adj_pk_pairs_per_tile() { return kPairsA2; }
 
 int adj_pk_rec4(int kind, bool has_m, bool want_t) { return adj2_rec(kind, has_m, want_t); }
+
+void *adj_tgt_box_kernel() { return reinterpret_cast<void *>(&po_adj_tgt_box_kernel); }
 
 template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
 static void *adj_pk_ptr()

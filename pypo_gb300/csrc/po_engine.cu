@@ -493,6 +493,11 @@ int run_adjoint(const AdjArgs &a)
     void *p2args[] = {&nt, &tgt7, &gam, &frame, &farflag, (void *)&rec4, &trec2};
     const unsigned nblk_p = (unsigned)((2 * npair + 255) / 256);
     if (!rc) rc = launch(adj_pack_tgt2_kernel(), dim3(nblk_p), dim3(256), p2args, 0, s);
+    // direction boxes of the far-field tiles for the lit-tile proof (M = 0 kernels)
+    int boxes = far && !has_m && nt > 0;
+    void *tbargs[] = {&trec2, &nt};
+    const unsigned ntile_a = (unsigned)((npair + adj_pk_pairs_per_tile() - 1) / adj_pk_pairs_per_tile());
+    if (!rc && boxes) rc = launch(adj_tgt_box_kernel(), dim3(ntile_a), dim3(32), tbargs, 0, s);
     if (want_t) PO_CK_RC(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
     void *fk = adj_pk_kernel(kind, ts, has_m, want_d, want_t);
     const int smem2 = adj_pk_smem_bytes(kind, has_m, want_t);
@@ -518,7 +523,7 @@ int run_adjoint(const AdjArgs &a)
     double *part = nullptr;
     if (!rc && (rc = salloc(&part, (size_t)split * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
     const float4 *srcc = srcpk, *trc2 = reinterpret_cast<const float4 *>(trec2);
-    void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err};
+    void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err, &boxes};
     timing_mark(s, true);
     if (!rc) rc = launch(fk, dim3((unsigned)nsb, (unsigned)split), dim3(kThreadsA), fargs, smem2, s);
     timing_mark(s, false);

@@ -123,6 +123,7 @@ void *adj_pack_tgt2_kernel();
 int adj_pk_smem_bytes(int kind, bool has_m, bool want_t);
 int adj_pk_pairs_per_tile();
 int adj_pk_rec4(int kind, bool has_m, bool want_t);   // float4 per pair-packed cotangent record
+void *adj_tgt_box_kernel();   // far-field cotangent tiles: direction boxes for the lit-tile proof
 void *adj_tgt_epilogue_kernel();
 
 }  // namespace po

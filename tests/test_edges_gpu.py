@@ -163,6 +163,27 @@ def test_lit_tiles_give_the_bits_of_the_per_pair_test(cuda, lib):
     assert np.array_equal(a, b[:, :300])
 
 
+def test_lit_far_field_adjoint_tiles_give_the_bits_of_the_per_pair_test(cuda, lib):
+    """The far-field adjoint's lit-tile proof: one more direction in the last
+    tile, 1e-7 rad inside the horizon and with a zero cotangent, turns the
+    proof off for that tile; the gradients are the same bits."""
+    from pypo_gb300 import engine
+    rng = np.random.default_rng(23)
+    s7, cur = _plane_sources(rng, 1000, np.ones(1000, bool))
+    cur[6:] = 0.0
+    d = np.zeros((7, 300))
+    d[0] = rng.uniform(0, np.radians(30), 300)
+    d[1] = rng.uniform(0, 2 * np.pi, 300)
+    edge = d[:, :1].copy()
+    edge[0] = np.pi / 2 - 1e-7
+    cot = rng.standard_normal((12, 300))
+    k = 2 * np.pi / 0.05
+    a = engine.adjoint("FF", s7, cur, -1, 0, 0, d, k, cot, want=("cur", "ds"))
+    b = engine.adjoint("FF", s7, cur, -1, 0, 0, np.concatenate([d, edge], axis=1), k,
+                       np.concatenate([cot, np.zeros((12, 1))], axis=1), want=("cur", "ds"))
+    assert np.array_equal(a["cur"], b["cur"]) and np.array_equal(a["ds"], b["ds"])
+
+
 def test_tiles_facing_both_ways_against_oracle(cuda, lib, oracle_mod):
     """Sources that face the targets, sources that face away, and a tile that
     holds both: lit tiles take the proven path, the others the per-pair
@@ -178,6 +199,8 @@ def test_tiles_facing_both_ways_against_oracle(cuda, lib, oracle_mod):
     d = np.zeros((7, 260))
     d[0] = rng.uniform(0, np.radians(60), 260)
     d[1] = rng.uniform(0, 2 * np.pi, 260)
+    from pypo_gb300 import engine
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
     for m_zero in (True, False):                      # with and without the proof
         c = cur.copy()
         if m_zero:
@@ -186,6 +209,11 @@ def test_tiles_facing_both_ways_against_oracle(cuda, lib, oracle_mod):
             got = _check(mode, s7, c, -1, 0, 0, t7, k, oracle_mod)
             assert np.abs(got).max() > 0
         _check("FF", s7, c, -1, 0, 0, d, k, oracle_mod)
+        # far-field adjoint: mixed (lit tiles proven or not) against the FP64 adjoint
+        cot = rng.standard_normal((12, 260))
+        gm = engine.adjoint("FF", s7, c, -1, 0, 0, d, k, cot, want=("cur", "ds"))
+        gd = engine.adjoint("FF", s7, c, -1, 0, 0, d, k, cot, precision="fp64", want=("cur", "ds"))
+        assert rel(gm["cur"], gd["cur"]) <= 1e-5 and rel(gm["ds"], gd["ds"]) <= 1e-4, m_zero
 
 
 def test_magnetic_current_found_past_the_host_prefix(cuda, lib, oracle_mod):
