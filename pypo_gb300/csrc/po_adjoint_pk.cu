@@ -17,8 +17,13 @@
 // an FP64 accumulator per target with atomicAdd (the order of those adds
 // varies from run to run: grad_dt is reproducible to ~1e-16, not bitwise).
 //
+// The three projections of W (on R_hat, n_s, n_t) come from one complex
+// vector per pair, Z = b x J - a x M: W.v = -v.Z (scalar triple product).
+//
 // Far field: the same kernel with the far-field pair (currents and source
-// displacement; far-field targets are directions and do not move).
+// displacement; far-field targets are directions and do not move). With
+// M = 0, a cotangent tile whose direction box proves every pair lit for the
+// CTA's source normals skips the illumination mask.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <cstdint>

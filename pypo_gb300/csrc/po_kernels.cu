@@ -20,6 +20,9 @@
 //     reduction, sin/cos of the reduced angle only, everything else in FP32;
 //   * each tile's FP32 partial is folded into a float-float total (two-sum),
 //     so long oscillatory sums stay compensated;
+//   * (M = 0) a tile whose box of normals and positions proves every pair
+//     lit for the CTA's targets runs without the per-pair illumination test
+//     (tile_lit; the boxes travel in the records' spare slot 21);
 //   * a source chunk (blockIdx.y) writes its totals as doubles; the epilogue
 //     kernel adds the chunks in a fixed order and applies the mode's physics
 //     (PEC current, EHP reflection, far-field projection) in FP64.
