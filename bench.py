@@ -611,27 +611,35 @@ def run_chain(args):
     value = world * pairs * args.steps / (ms * 1e-3) / 1e9
     g_auto = {r: v.grad.cpu().numpy() for r, v in dvars.items()}
 
-    # ---- e2e: host buffers through the C-ABI, chain rule stage by stage
-    host = {key: np.ascontiguousarray(c[key]) for key in keys}
+    # ---- e2e: host buffers through the C-ABI, chain rule stage by stage; every
+    # host buffer (inputs, each stage's output, each stage's gradients) is
+    # page-locked and allocated once, as a user of the C-ABI would
+    pinned = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    pinned_empty = lambda *shape: torch.empty(shape, dtype=torch.float64).pin_memory().numpy()
+    host = {key: pinned(c[key]) for key in keys}
     for r in refl:                                   # displaced reflector points (normals, areas frozen)
-        host[r] = host[r].copy()
         host[r][:3] += disp0[r][None, :] * host[r][3:6]
+    feed_cur = pinned(c["feed_cur"])
+    cot_h = pinned(cot_np)
+    stage_out = [pinned_empty(engine.n_out(mode), n[tk]) for mode, _, _, tk in stages]
+    stage_grad = [{"cur": pinned_empty(12, n[sk]), "ds": pinned_empty(n[sk]), "dt": pinned_empty(n[tk])}
+                  for _, sk, _, tk in stages]
     io_bytes = []
 
     def host_step():
-        curs = [np.ascontiguousarray(c["feed_cur"])]
-        for mode, sk, gk, tk in stages[:-1]:
-            curs.append(engine.propagate(mode, host[sk], curs[-1], *c[gk], host[tk], k))
+        curs = [feed_cur]
+        for j, (mode, sk, gk, tk) in enumerate(stages[:-1]):
+            curs.append(engine.propagate(mode, host[sk], curs[-1], *c[gk], host[tk], k, out=stage_out[j]))
         mode, sk, gk, tk = stages[-1]
-        engine.propagate(mode, host[sk], curs[-1], *c[gk], host[tk], k)
+        engine.propagate(mode, host[sk], curs[-1], *c[gk], host[tk], k, out=stage_out[-1])
         grads = {r: np.zeros(n[r]) for r in refl}
-        ct = cot_np
+        ct = cot_h
         b_in = b_out = 0
         for i in range(len(stages) - 1, -1, -1):
             mode, sk, gk, tk = stages[i]
             want = (("cur",) if i > 0 else ()) + (("ds",) if sk in refl else ()) + \
                 (("dt",) if tk in refl and mode != "FF" else ())
-            g = engine.adjoint(mode, host[sk], curs[i], *c[gk], host[tk], k, ct, want=want)
+            g = engine.adjoint(mode, host[sk], curs[i], *c[gk], host[tk], k, ct, want=want, out=stage_grad[i])
             if sk in refl:
                 grads[sk] += g["ds"]
             if tk in refl and mode != "FF":
@@ -722,7 +730,7 @@ def run_chain(args):
                      "sample": "each stage timed on every s-th source x every t-th target (>= 65536 of each where "
                                "available), combined by pairs"},
         "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": io_bytes[0], "d2h_bytes_per_step": io_bytes[1],
-                "path": "po_run_d / po_adjoint_d per stage from host arrays, chain rule on the host",
+                "path": "po_run_d / po_adjoint_d per stage from page-locked host arrays, chain rule on the host",
                 "host_vs_autograd_grad_rel": host_vs_autograd},
         "cpu_baseline": {"value": cpu_pairs / cpu_s / 1e9, "unit": "Gpairs/s (forward chain)", "cores": threads,
                          "kind": "port", "sample": "per stage " + "; ".join(cpu_parts) + ", FP64 oracle, combined by pairs"},

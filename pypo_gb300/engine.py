@@ -178,11 +178,13 @@ def timing_collect(max_n=4096):
 
 
 def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-1.0, precision="mixed",
-            want=("cur", "ds", "dt")):
+            want=("cur", "ds", "dt"), out=None):
     """Host-buffer adjoint (po_adjoint_d).
 
     cot: (n_out(mode), nt) float64, dL/d(output rows). Returns a dict with the
-    requested gradients: "cur" (12, ns), "ds" (ns,) and "dt" (nt,) (near field).
+    requested gradients: "cur" (12, ns), "ds" (ns,) and "dt" (nt,) (near field),
+    written into the arrays of `out` (a dict of C-contiguous float64 arrays of
+    those shapes, e.g. page-locked ones) where it has them.
     """
     lib = load()
     src7 = np.ascontiguousarray(src7, dtype=np.float64)
@@ -193,10 +195,20 @@ def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-
     ns, nt = src7.shape[1], tgt7.shape[1]
     if cot.shape != (n_out(mode), nt):
         raise POError(f"cot must have shape {(n_out(mode), nt)}")
+    given = out or {}
+
+    def buf(name, shape):
+        a = given.get(name)
+        if a is None:
+            return np.zeros(shape)
+        if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise POError(f"out[{name!r}] must be a C-contiguous float64 array of shape {shape}")
+        return a
+
     out = {}
-    gc = np.zeros((12, ns)) if "cur" in want else None
-    gs = np.zeros(ns) if "ds" in want else None
-    gt = np.zeros(nt) if ("dt" in want and mode != "FF") else None
+    gc = buf("cur", (12, ns)) if "cur" in want else None
+    gs = buf("ds", (ns,)) if "ds" in want else None
+    gt = buf("dt", (nt,)) if ("dt" in want and mode != "FF") else None
     ptr = lambda a: a.ctypes.data if a is not None else None
     check(lib.po_adjoint_d(MODE_ID[mode], ns, src7.ctypes.data, int(gmode), int(ncx), int(ncy), cur.ctypes.data,
                            nt, tgt7.ctypes.data, float(k), float(epsilon), float(t_dir), PRECISION[precision],
