@@ -135,3 +135,18 @@ def test_mixed_extent_and_warning():
     with warnings.catch_warnings():
         warnings.simplefilter("error")
         engine._extent_warning(m, "fp64")
+
+
+def test_adjoint_output_buffers_are_checked_before_any_device_work(lib):
+    """engine.adjoint writes into caller-provided arrays (page-locked ones, for
+    instance) only when their shape and layout fit."""
+    from pypo_gb300 import engine
+    from pypo_gb300._lib import POError
+    s7 = np.zeros((7, 4))
+    t7 = np.zeros((7, 3))
+    cur = np.zeros((12, 4))
+    cot = np.zeros((12, 3))
+    for bad in ({"cur": np.zeros((12, 5))}, {"ds": np.zeros(4, dtype=np.float32)},
+                {"dt": np.zeros((3, 1))}, {"cur": np.zeros((4, 12)).T}):
+        with pytest.raises(POError, match="out\\["):
+            engine.adjoint("EH", s7, cur, -1, 0, 0, t7, 1.0, cot, out=bad)
