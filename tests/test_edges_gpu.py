@@ -148,7 +148,7 @@ def test_lit_tiles_give_the_bits_of_the_per_pair_test(cuda, lib):
     near = t7[:, :1].copy()
     near[2] = 1e-9                                   # n.d = 1e-9 mm > 0: lit, but inside the margin
     k = 2 * np.pi / 0.05
-    for mode in ("EH", "JM"):
+    for mode in ("EH", "JM", "JMEH", "EHP"):
         a = engine.propagate(mode, s7, cur, -1, 0, 0, t7, k)
         b = engine.propagate(mode, s7, cur, -1, 0, 0, np.concatenate([t7, near], axis=1), k)
         assert np.array_equal(a, b[:, :100]), mode
