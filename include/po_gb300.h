@@ -233,6 +233,11 @@ double po_last_extent(void);
  *         angle and y the azimuth (radians), as the reference's AoE grid
  *   out   po_n_out(mode)*nt doubles in bundle row order
  *   precision  0 mixed (FP32 bulk + split hi/lo phase), 1 plain FP64
+ *
+ * Whether M == 0 (which selects the kernels without magnetic terms) is
+ * settled from the first 4096 magnetic values on the host when one of them
+ * is non-zero, else by a device check of all of them. The call synchronises
+ * once, on a private stream; page-locked buffers make its copies fastest.
  */
 int po_n_out(int mode);
 int po_run_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
