@@ -239,7 +239,7 @@ def dish_chain_fd(c, grad, cot, k, nodes=64, h_lam=1e-6):
 def run_reference_chain(args, threads):
     """Reference arm of a chain: the FP64 CPU oracle's forward rate per stage on
     bounded target samples, combined by pairs."""
-    c, stages, _, _ = chain_config(args.workload)
+    c, stages, _, _ = chain_config(args.workload, args.scale)
     per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup)) / len(stages)
     rates = []
     for i in range(args.warmup + args.steps):
@@ -276,7 +276,7 @@ def run_reference(args):
                 "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
-    w = configs.WORKLOADS[args.workload]()
+    w = configs.WORKLOADS[args.workload](scale=args.scale)   # the same workload as the other arm
     per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
     kind = "port"
     try:
