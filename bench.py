@@ -31,9 +31,15 @@ stage by stage (e2e). The FP64 GPU chain is timed per stage on source
 subsamples and combined by pairs; the accuracy is the mixed chain against
 the FP64 chain at scale 0.2.
 
-`--impl reference` times the reference's CPU path (its compiled library when
-it loads here, else the oracle's C restatement of it) on the same workload.
-The reference has no adjoint, so that arm times the forward pass.
+`--impl reference` times the reference's CPU path on the host cores, on the
+same workload and the same step: the FP64 C restatement of the reference's
+forward (oracle/po_oracle.c, pinned to the reference's own outputs) plus the
+FP64 C adjoint (the reference has none; po_oracle_adjoint states the same
+formulas), over every source and a random sample of targets sized to a few
+seconds a step. Its ms_per_step is that sampled step as timed; its value is
+pairs per second. The arm imports only oracle/ (inputs from
+oracle/workloads.py, equal to pypo_gb300/configs.py's): no product code
+runs on it.
 
 Multi-GPU: one process per GPU (torchrun); each rank runs its own replica of
 the workload (targets are independent, no collective on the data path);
@@ -130,49 +136,76 @@ def gpu_index(local):
     return local
 
 
-def cpu_oracle_rate(w, seconds, threads):
-    """Pairs/s of the FP64 CPU oracle (forward) on a random target sample sized to ~`seconds`."""
+#: the workloads as the JSON line names them (both arms print the same config)
+DESCS = {
+    "dish_eh": "paraboloid D1000 f500 uv 501x501 -> focal plane 301x301 +-50 mm, lambda 1.0 mm, EH, M=0",
+    "dish_ff": "paraboloid D2000 f800 uv 1001x1001 -> far field 401x401 +-0.5 deg, lambda 1.0 mm, FF, M=0",
+    "feed_dish_jm": "Gaussian feed 101x101 -> f300 D300 dish uv 101x101, lambda 3 mm, JM",
+    "cassegrain": "feed 201^2 -> hyperboloid 401^2 -> paraboloid 1001^2 -> FF 201^2, lambda 1 mm",
+    "dish_chain": "feed 101^2 -> dish 301^2 (+surface error) -> FF 101^2, lambda 2 mm",
+}
+STEP = "forward + adjoint (grad wrt currents, source and target normal displacement)"
+STEP_CHAIN = "forward chain + backward (currents' cotangents, displacement of every reflector)"
+L2 = ("GPU arm: flushed before every step (256 MB write inside the timed loop); CPU arm: "
+      "not applicable (host caches, inputs larger than them)")
+
+
+def config_of(name, scale, pairs, **extra):
+    """The `config` object, identical for both arms of one workload."""
+    c = {"workload": name + ("" if scale == 1.0 else f" (scale {scale})"), "desc": DESCS[name],
+         "pairs_per_step": pairs, **extra}
+    c["step"] = STEP_CHAIN if name in CHAINS else STEP
+    c["l2"] = L2
+    return c
+
+
+def field_errors(got, ref, mode):
+    """Relative L2 over every row, and the largest phase error over the complex
+    components within 20 dB and 40 dB of the sample's largest component."""
+    got, ref = np.asarray(got), np.asarray(ref)
+    out = {"rel_l2": float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300))}
+    nc = {"scalar": 1, "JMEH": 4}.get(mode, 2)
+    rc = np.concatenate([ref[6 * b:6 * b + 3] + 1j * ref[6 * b + 3:6 * b + 6] for b in range(nc)]) \
+        if mode != "scalar" else ref[0:1] + 1j * ref[1:2]
+    gc = np.concatenate([got[6 * b:6 * b + 3] + 1j * got[6 * b + 3:6 * b + 6] for b in range(nc)]) \
+        if mode != "scalar" else got[0:1] + 1j * got[1:2]
+    mag = np.abs(rc)
+    for db in (20, 40):
+        sel = mag >= mag.max() * 10 ** (-db / 20)
+        out[f"max_phase_rad_{db}db"] = float(np.abs(np.angle(gc[sel] / rc[sel])).max()) if sel.any() else 0.0
+    return out
+
+
+def cot_for(mode, nt):
+    """The step's cotangent: seeded, the same in both arms."""
+    return np.random.default_rng(7).standard_normal((N_OUT[mode], nt))
+
+
+N_OUT = {"JM": 12, "EH": 12, "JMEH": 24, "EHP": 15, "FF": 12, "scalar": 2}
+
+
+def cpu_step(w, cot, idx, threads):
+    """One step of the FP64 CPU path over every source and the targets `idx`:
+    the oracle's forward (the reference's algorithm) and its adjoint. Returns
+    (forward rows, gradients, forward seconds, adjoint seconds)."""
     from oracle import oracle as O
-    rng = np.random.default_rng(123)
+    t7s = np.ascontiguousarray(w["t7"][:, idx])
+    cots = np.ascontiguousarray(cot[:, idx])
+    grid = (w["gmode"], w["ncx"], w["ncy"])
+    t0 = time.perf_counter()
+    out = O.run(w["mode"], w["s7"], w["cur"], *grid, t7s, w["k"], 1.0, -1.0, nthreads=threads)
+    t1 = time.perf_counter()
+    g = O.adjoint(w["mode"], w["s7"], w["cur"], *grid, t7s, w["k"], cots, 1.0, -1.0, nthreads=threads)
+    t2 = time.perf_counter()
+    return out, g, t1 - t0, t2 - t1
+
+
+def cpu_sample_size(w, cot, seconds, threads, rng):
+    """Number of sampled targets for which one CPU step takes about `seconds`."""
     nt = w["t7"].shape[1]
-    ns = w["s7"].shape[1]
-
-    def run(n):
-        idx = np.sort(rng.choice(nt, size=n, replace=False))
-        t0 = time.perf_counter()
-        O.run(w["mode"], w["s7"], w["cur"], w["gmode"], w["ncx"], w["ncy"], w["t7"], w["k"],
-              1.0, -1.0, nthreads=threads, tidx=idx)
-        return time.perf_counter() - t0
-
-    n0 = max(threads, 16)
-    dt = run(n0)
-    n = int(min(nt, max(n0, n0 * seconds / max(dt, 1e-3))))
-    dt = run(n)
-    return ns * n / dt, n, dt
-
-
-def reference_lib_rate(w, seconds, threads):
-    """Pairs/s of the reference's own compiled CPU library on leading target rows."""
-    from oracle import oracle as O
-    ref = O.Reference()
-    tgt = dict(w["tgt"])
-    ncy = int(tgt["gridsize"][1])
-    ncx = int(tgt["gridsize"][0])
-    lx = np.asarray(tgt["lims_x"], dtype=float)
-    dx = (lx[1] - lx[0]) / (ncx - 1)
-    ns = w["s7"].shape[1]
-
-    def run(rows):
-        sub = dict(tgt, gridsize=np.array([rows, ncy]), lims_x=np.array([lx[0], lx[0] + (rows - 1) * dx]))
-        t0 = time.perf_counter()
-        ref.propagate(w["mode"], w["src"], sub, w["cur"], w["k"], 1.0, -1.0, nthreads=threads)
-        return time.perf_counter() - t0
-
-    r0 = 2
-    dt = run(r0)
-    rows = int(min(ncx, max(r0, r0 * seconds / max(dt, 1e-3))))
-    dt = run(rows)
-    return ns * rows * ncy / dt, rows * ncy, dt
+    n0 = min(nt, max(threads, 16))
+    _, _, tf, ta = cpu_step(w, cot, np.sort(rng.choice(nt, size=n0, replace=False)), threads)
+    return int(min(nt, max(n0, n0 * seconds / max(tf + ta, 1e-3))))
 
 
 #: chain workloads: config builder, stages (mode, source, source grid, target),
@@ -186,6 +219,7 @@ CHAINS = {
 
 
 def chain_config(name, scale=1.0):
+    """The product's chain configuration (the GPU arm)."""
     from pypo_gb300 import configs
     builder, stages, refl = CHAINS[name]
     c = getattr(configs, builder)(scale=scale)
@@ -195,117 +229,134 @@ def chain_config(name, scale=1.0):
 
 
 def chain_stage_workloads(c, stages):
-    """The chain's stages as workload dicts (cpu_oracle_rate's inputs); the
-    source currents after the feed are seeded random rows (the forward rate
-    does not depend on their values)."""
+    """The chain's stages as workload dicts (cpu_step's inputs) with a seeded
+    cotangent each; the source currents after the feed are seeded random rows
+    (the step's cost does not depend on their values)."""
     rng = np.random.default_rng(11)
     out = []
     for mode, skey, gkey, tkey in stages:
         g = c[gkey]
         cur = c["feed_cur"] if skey == "feed7" else rng.standard_normal((12, c[skey].shape[1]))
-        out.append(dict(mode=mode, s7=c[skey], cur=cur, gmode=g[0], ncx=g[1], ncy=g[2], t7=c[tkey], k=c["k"]))
+        w = dict(mode=mode, s7=c[skey], cur=cur, gmode=g[0], ncx=g[1], ncy=g[2], t7=c[tkey], k=c["k"])
+        w["cot"] = rng.standard_normal((N_OUT[mode], c[tkey].shape[1]))
+        out.append(w)
     return out
+
+
+def cpu_chain_step(ws, frac, threads, rng):
+    """One sampled step of the FP64 CPU chain: in every stage, forward and
+    adjoint over all its sources and the same fraction `frac` of its targets,
+    so that the sampled pairs are in the stages' proportion. Returns (pairs,
+    seconds, per-stage descriptions)."""
+    pairs, secs, parts = 0, 0.0, []
+    for w in ws:
+        nt, ns = w["t7"].shape[1], w["s7"].shape[1]
+        n = int(min(nt, max(1, round(frac * nt))))
+        idx = np.sort(rng.choice(nt, size=n, replace=False))
+        _, _, tf, ta = cpu_step(w, w["cot"], idx, threads)
+        pairs += ns * n
+        secs += tf + ta
+        parts.append(f"{n} targets x {ns} sources")
+    return pairs, secs, parts
+
+
+def cpu_chain_fraction(ws, seconds, threads, rng):
+    total = sum(w["s7"].shape[1] * w["t7"].shape[1] for w in ws)
+    f0 = 2e6 / total
+    p, sec, _ = cpu_chain_step(ws, f0, threads, rng)
+    return min(1.0, f0 * seconds / max(sec, 1e-3))
 
 
 def dish_chain_fd(c, grad, cot, k, nodes=64, h_lam=1e-6):
     """The perturbed-dish chain's displacement gradient against central finite
-    differences of the FP64 chain on 64 seeded dish nodes (h = 1e-6 lambda).
-    The loss sum(cot * far field) is a sum of per-node far-field terms, and a
-    node's displacement changes only its own (its induced current and its
-    position), so each difference needs that node alone: a one-target JM from
-    the feed and a one-source FF."""
-    from pypo_gb300 import engine
+    differences of the FP64 oracle chain (the reference's CPU algorithm) on 64
+    seeded dish nodes (h = 1e-6 lambda). The loss sum(cot * far field) is a
+    sum of per-node far-field terms, and a node's displacement changes only its
+    own (its induced current and its position), so each difference needs that
+    node alone: a one-target JM from the feed and a one-source FF."""
+    from oracle import oracle as O
     f7, fcur, d7, ff7 = c["feed7"], c["feed_cur"], c["dish7"], c["ff7"]
     fg, (gm, ncx, ncy) = c["feed_grid"], c["dish_grid"]
     h = h_lam * c["lam"]
     pick = np.random.default_rng(2).choice(d7.shape[1], nodes, replace=False)
+    threads = os.cpu_count() or 1
 
     def term(i, delta):
         p7 = d7[:, i:i + 1].copy()
         p7[:3, 0] += delta * d7[3:6, i]
-        ji = engine.propagate("JM", f7, fcur, *fg, p7, k, precision="fp64")
+        ji = O.run("JM", f7, fcur, *fg, p7, k, nthreads=1)
         xu, yv = i // ncy, i % ncy   # the dish grid's trapezoid weight of node i
         w = (0.5 if xu in (0, ncx - 1) else 1.0) * (0.5 if gm != 1 and yv in (0, ncy - 1) else 1.0)
         p7[6, 0] *= w
-        return float((engine.propagate("FF", p7, ji, -1, 0, 0, ff7, k, precision="fp64") * cot).sum())
+        return float((O.run("FF", p7, ji, -1, 0, 0, ff7, k, nthreads=threads) * cot).sum())
 
     fd = np.array([(term(i, c["delta"][i] + h) - term(i, c["delta"][i] - h)) / (2 * h) for i in pick])
     g = grad[pick]
     return {"rel_l2": float(np.linalg.norm(g - fd) / np.linalg.norm(fd)), "nodes": nodes,
             "h": f"{h_lam:g} lambda", "gradient": "mixed-precision autograd of the timed step",
-            "against": "central differences of the FP64 chain, one node moved at a time"}
+            "against": "central differences of the FP64 CPU oracle chain (the reference's algorithm), "
+                       "one node moved at a time"}
 
 
-def run_reference_chain(args, threads):
-    """Reference arm of a chain: the FP64 CPU oracle's forward rate per stage on
-    bounded target samples, combined by pairs."""
-    c, stages, _, _ = chain_config(args.workload, args.scale)
-    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup)) / len(stages)
-    rates = []
-    for i in range(args.warmup + args.steps):
-        total_s, pairs, parts = 0.0, 0, []
-        for w in chain_stage_workloads(c, stages):
-            rate, n, dt = cpu_oracle_rate(w, per_step, threads)
-            sp = w["s7"].shape[1] * w["t7"].shape[1]
-            total_s += sp / rate
-            pairs += sp
-            parts.append(f"{n} targets x {w['s7'].shape[1]} sources")
-        if i >= args.warmup:
-            rates.append(pairs / total_s)
-    value = float(np.mean(rates)) / 1e9
-    sample = "per stage " + "; ".join(parts) + ", combined by pairs, forward only"
-    return value, pairs, sample, c["desc"]
+def reference_line(args, world, value, ms, timed_pairs, full_pairs, threads, sample, config):
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (the same inputs as the GPU arm)",
+            "config": config, "device": "cpu", "precision": "FP64",
+            "timed_pairs_per_step": timed_pairs,
+            "full_step_ms_extrapolated": full_pairs / (value * 1e9) * 1e3,
+            "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
 
 
 def run_reference(args):
+    """The CPU arm: the reference's algorithm (the oracle's C restatement,
+    pinned to the reference's outputs) timed on the host cores on the same
+    workload and step, each step a bounded sample of it. Imports only oracle/."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from pypo_gb300 import configs
+    from oracle import workloads as OW
     threads = os.cpu_count() or 1
+    per_step = max(0.2, args.cpu_seconds / max(1, args.steps + args.warmup))
+    rng = np.random.default_rng(123)
     if args.workload in CHAINS:
-        value, pairs, sample, desc = run_reference_chain(args, threads)
-        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs / (value * 1e9) * 1e3,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": args.workload, "desc": desc, "pairs_per_step": pairs,
-                                                "device": "cpu", "threads": threads,
-                                                "step": "forward chain (the reference has no adjoint)"},
-                "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": threads, "kind": "port",
-                                 "sample": sample},
-                "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        builder, stages, _ = CHAINS[args.workload]
+        c = OW.CHAINS[builder](scale=args.scale)
+        ws = chain_stage_workloads(c, stages)
+        full = sum(w["s7"].shape[1] * w["t7"].shape[1] for w in ws)
+        frac = cpu_chain_fraction(ws, per_step, threads, rng)
+        times, pairs, parts = [], 0, []
+        for i in range(args.warmup + args.steps):
+            pairs, sec, parts = cpu_chain_step(ws, frac, threads, rng)
+            if i >= args.warmup:
+                times.append(sec)
+        sec = float(np.mean(times))
+        value = pairs / sec / 1e9
+        sample = ("per stage " + "; ".join(parts) + f" (a fraction {frac:.2e} of every stage's targets), "
+                  "forward + adjoint, FP64 oracle")
+        line = reference_line(args, world, value, sec * 1e3, pairs, full, threads, sample,
+                              config_of(args.workload, args.scale, full,
+                                        stage_pairs=[w["s7"].shape[1] * w["t7"].shape[1] for w in ws]))
         print(json.dumps(line), flush=True)
         return
-    w = configs.WORKLOADS[args.workload](scale=args.scale)   # the same workload as the other arm
-    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
-    kind = "port"
-    try:
-        from oracle import oracle as O
-        if O.REF_PATH.exists():
-            O.Reference()
-            kind = "reference"
-    except OSError:
-        kind = "port"
-    rates, sample = [], ""
+    w = OW.WORKLOADS[args.workload](scale=args.scale)   # equal to the GPU arm's inputs
+    nt, ns = w["t7"].shape[1], w["s7"].shape[1]
+    cot = cot_for(w["mode"], nt)
+    n = cpu_sample_size(w, cot, per_step, threads, rng)
+    times = []
     for i in range(args.warmup + args.steps):
-        if kind == "reference":
-            rate, n, dt = reference_lib_rate(w, per_step, threads)
-            sample = f"{n} targets (leading grid rows) x {w['s7'].shape[1]} sources per step, forward only"
-        else:
-            rate, n, dt = cpu_oracle_rate(w, per_step, threads)
-            sample = f"{n} random targets x {w['s7'].shape[1]} sources per step, forward only"
+        idx = np.sort(rng.choice(nt, size=n, replace=False))
+        _, _, tf, ta = cpu_step(w, cot, idx, threads)
         if i >= args.warmup:
-            rates.append(rate)
-    value = float(np.mean(rates)) / 1e9
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": w["pairs"] / (value * 1e9) * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": w["name"], "desc": w["desc"], "pairs_per_step": w["pairs"],
-                                            "device": "cpu", "threads": threads,
-                                            "step": "forward propagation (the reference has no adjoint)"},
-            "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": threads, "kind": kind,
-                             "sample": sample},
-            "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            times.append(tf + ta)
+    sec = float(np.mean(times))
+    value = ns * n / sec / 1e9
+    sample = (f"{n} random targets x {ns} sources per step (a new sample every step), forward + adjoint, "
+              "FP64 oracle")
+    line = reference_line(args, world, value, sec * 1e3, ns * n, w["pairs"], threads, sample,
+                          config_of(args.workload, args.scale, w["pairs"], ns=ns, nt=nt))
     print(json.dumps(line), flush=True)
 
 
@@ -328,8 +379,8 @@ def run_ours(args):
     ns, nt = w["s7"].shape[1], w["t7"].shape[1]
     nout = engine.n_out(mode)
     far = mode == "FF"
-    rng = np.random.default_rng(7)
-    cot_np = rng.standard_normal((nout, nt))
+    cot_np = cot_for(mode, nt)
+    rng = np.random.default_rng(8)
     s7 = torch.tensor(np.ascontiguousarray(w["s7"]), device=dev)
     cur = torch.tensor(np.ascontiguousarray(w["cur"]), device=dev)
     t7 = torch.tensor(np.ascontiguousarray(w["t7"]), device=dev)
@@ -420,12 +471,31 @@ def run_ours(args):
     t7s = torch.tensor(np.ascontiguousarray(w["t7"][:, idx]), device=dev)
     ref = engine.propagate_dev(mode, s7, cur, *grid, t7s, k, 1.0, -1.0, "fp64")
     torch.cuda.synchronize()
-    ref_n, got_n = ref.cpu().numpy(), out[:, idx].cpu().numpy()
-    rel_l2 = float(np.linalg.norm(got_n - ref_n) / np.linalg.norm(ref_n))
-    rc = ref_n[0:3] + 1j * ref_n[3:6]
-    gcx = got_n[0:3] + 1j * got_n[3:6]
-    sel = np.abs(rc) >= np.abs(rc).max() * 0.1
-    max_phase = float(np.abs(np.angle(gcx[sel] / rc[sel])).max())
+    acc_gpu64 = field_errors(out[:, idx].cpu().numpy(), ref.cpu().numpy(), mode)
+
+    # ---- the reference's CPU path (the FP64 oracle) on a random target sample:
+    # its rate (cpu_baseline) and the GPU results against its outputs
+    threads = os.cpu_count() or 1
+    crng = np.random.default_rng(123)
+    ncpu = cpu_sample_size(w, cot_np, 10.0, threads, crng)
+    cidx = np.sort(crng.choice(nt, size=ncpu, replace=False))
+    ref_out, ref_g, cpu_tf, cpu_ta = cpu_step(w, cot_np, cidx, threads)
+    cpu_rate = ns * ncpu / (cpu_tf + cpu_ta)
+    acc_cpu = field_errors(out[:, cidx].cpu().numpy(), ref_out, mode)
+    # the mixed adjoint over every source and the sampled targets, against the CPU adjoint
+    t7c = torch.tensor(np.ascontiguousarray(w["t7"][:, cidx]), device=dev)
+    cotc = torch.tensor(np.ascontiguousarray(cot_np[:, cidx]), device=dev)
+    gcc = torch.empty((12, ns), dtype=torch.float64, device=dev)
+    gsc = torch.empty(ns, dtype=torch.float64, device=dev)
+    gtc = None if far else torch.empty(ncpu, dtype=torch.float64, device=dev)
+    engine.adjoint_dev(mode, s7, cur, *grid, t7c, k, cotc, 1.0, -1.0, "mixed", m_zero=m_zero, grad_cur=gcc,
+                       grad_ds=gsc, grad_dt=gtc)
+    torch.cuda.synchronize()
+    rel_np = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    adj_cpu = {"grad_cur_rel_l2": rel_np(gcc.cpu().numpy(), ref_g["cur"]),
+               "grad_ds_rel_l2": rel_np(gsc.cpu().numpy(), ref_g["ds"])}
+    if not far:
+        adj_cpu["grad_dt_rel_l2"] = rel_np(gtc.cpu().numpy(), ref_g["dt"])
 
     # ---- adjoint accuracy and FP64 step rate on a sub-problem: all targets and
     # every fstep-th source, with fstep chosen so that the FP64 kernels, one
@@ -490,28 +560,28 @@ def run_ours(args):
     step_flops = sum(f for f in flops[:kernels_per_step] if f)
     step_ms_kernels = float(launch_ms.sum(axis=1).mean())
 
-    # ---- FP64 CPU oracle (forward) on a bounded sample
-    threads = os.cpu_count() or 1
-    cpu_rate, cpu_n, cpu_dt = cpu_oracle_rate(w, 10.0, threads)
-
     line = {
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded currents with the configuration's taper and phase noise; random cotangent)",
-        "config": {"workload": w["name"] + ("" if args.scale == 1.0 else f" (scale {args.scale})"), "desc": w["desc"],
-                   "ns": ns, "nt": nt, "pairs_per_step": w["pairs"],
-                   "step": "forward + adjoint (grad wrt currents, source and target normal displacement)",
-                   "precision": "FP32 bulk in packed FP32x2; separation, R and phase in split hi/lo form",
-                   "l2": "flushed before every step (256 MB write inside the timed loop)",
-                   "parallelism": f"replica per GPU x{world}"},
+        "config": config_of(args.workload, args.scale, w["pairs"], ns=ns, nt=nt),
+        "device": "gpu", "parallelism": f"replica per GPU x{world}",
+        "precision": "FP32 bulk in packed FP32x2; separation, R and phase in split hi/lo form",
         "forward_gpairs_per_s": kernels[0]["gpairs_per_s"],
         "adjoint_gpairs_per_s": w["pairs"] / (sum(kk["launch_ms"] for kk in kernels[1:]) * 1e-3) / 1e9,
-        "accuracy": {"forward_rel_l2": rel_l2, "forward_max_phase_rad": max_phase,
-                     "forward_against": f"plain FP64 GPU sum on {idx.size} random targets (all sources)",
-                     "phase_on": "E components within 20 dB of the sampled peak",
-                     "adjoint": adj_acc,
-                     "adjoint_against": f"plain FP64 GPU adjoint, all targets x one source in {fstep} ({nsf})"},
+        "accuracy": {
+            "against_reference_cpu": {
+                "forward": acc_cpu, "adjoint": adj_cpu,
+                "against": f"the reference's CPU FP64 path (oracle restatement, pinned to the reference's "
+                           f"outputs) on {ncpu} random targets x all {ns} sources, the GPU step's own outputs "
+                           f"(forward) and the GPU mixed adjoint over the same targets"},
+            "against_fp64_gpu": {
+                "forward": acc_gpu64, "adjoint": adj_acc,
+                "against": f"plain FP64 GPU sum on {idx.size} random targets (all sources); plain FP64 GPU "
+                           f"adjoint, all targets x one source in {fstep} ({nsf})"},
+            "phase_on": "max |arg(got/ref)| over the E and H components whose magnitude is within 20 dB "
+                        "(and 40 dB) of the sample's largest component; rel_l2 over every output row"},
         "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (fwd+adjoint step)", "speedup": value / world / fp64_rate,
                      "sample": f"all {nt} targets x one source in {fstep} ({nsf})"},
         "roofline": {"bound": "fp32", "kernel": dom["kernel"], "achieved": dom["achieved_tflops"], "peak": peak,
@@ -520,8 +590,9 @@ def run_ours(args):
                      "step_frac": step_flops * w["pairs"] / (step_ms_kernels * 1e-3) / 1e12 / peak,
                      "kernels": kernels,
                      "peak_source": "measured: po_fp32_probe FFMA chains on this GPU, best of 3"},
-        "cpu_baseline": {"value": cpu_rate / 1e9, "unit": "Gpairs/s (forward)", "cores": threads, "kind": "port",
-                         "sample": f"{cpu_n} random targets x {ns} sources ({cpu_dt:.1f} s), FP64 oracle"},
+        "cpu_baseline": {"value": cpu_rate / 1e9, "unit": "Gpairs/s", "cores": threads, "kind": "port",
+                         "sample": f"{ncpu} random targets x {ns} sources, forward {cpu_tf:.1f} s + adjoint "
+                                   f"{cpu_ta:.1f} s, FP64 oracle (the reference's algorithm)"},
         "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
@@ -707,23 +778,17 @@ def run_chain(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    cpu_s, cpu_pairs, cpu_parts = 0.0, 0, []
-    for w in chain_stage_workloads(c, stages):
-        rate, nsmp, _ = cpu_oracle_rate(w, 3.0, threads)
-        sp = w["s7"].shape[1] * w["t7"].shape[1]
-        cpu_s += sp / rate
-        cpu_pairs += sp
-        cpu_parts.append(f"{nsmp} targets x {w['s7'].shape[1]} sources")
+    ws = chain_stage_workloads(c, stages)
+    crng = np.random.default_rng(123)
+    frac = cpu_chain_fraction(ws, 6.0, threads, crng)
+    cpu_pairs, cpu_s, cpu_parts = cpu_chain_step(ws, frac, threads, crng)
     line = {
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (Gaussian feed of the configuration; random cotangent on the far field)",
-        "config": {"workload": args.workload + ("" if args.scale == 1.0 else f" (scale {args.scale})"),
-                   "desc": c["desc"], "stage_pairs": stage_pairs, "pairs_per_step": pairs,
-                   "step": "forward chain + backward (currents' cotangents, displacement of every reflector)",
-                   "l2": "flushed before every step (256 MB write inside the timed loop)",
-                   "parallelism": f"replica per GPU x{world}"},
+        "config": config_of(args.workload, args.scale, pairs, stage_pairs=stage_pairs),
+        "device": "gpu", "parallelism": f"replica per GPU x{world}",
         "accuracy": dict(acc, against="FP64 GPU chain, configuration at scale 0.2"),
         **({"gradient_vs_finite_differences": grad_fd} if grad_fd else {}),
         "fp64_gpu": {"value": fp64_rate, "unit": "Gpairs/s (chain fwd+adjoint)", "speedup": value / world / fp64_rate,
@@ -732,8 +797,9 @@ def run_chain(args):
         "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": io_bytes[0], "d2h_bytes_per_step": io_bytes[1],
                 "path": "po_run_d / po_adjoint_d per stage from page-locked host arrays, chain rule on the host",
                 "host_vs_autograd_grad_rel": host_vs_autograd},
-        "cpu_baseline": {"value": cpu_pairs / cpu_s / 1e9, "unit": "Gpairs/s (forward chain)", "cores": threads,
-                         "kind": "port", "sample": "per stage " + "; ".join(cpu_parts) + ", FP64 oracle, combined by pairs"},
+        "cpu_baseline": {"value": cpu_pairs / cpu_s / 1e9, "unit": "Gpairs/s", "cores": threads,
+                         "kind": "port", "sample": "per stage " + "; ".join(cpu_parts) +
+                         f" (a fraction {frac:.2e} of every stage's targets), forward + adjoint, FP64 oracle"},
         "gpu_launches": launches[0] * args.steps, "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -748,6 +814,9 @@ def main():
                     choices=["dish_eh", "dish_ff", "feed_dish_jm", "cassegrain", "dish_chain"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink both grids (profiling runs only; the bench line is the full size)")
+    ap.add_argument("--cpu-seconds", type=float, default=90.0,
+                    help="reference arm: host time of the whole run (warm-up and timed steps), which sizes "
+                         "each step's target sample")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -50,6 +50,12 @@ def load():
             ctypes.c_int, ctypes.c_int, ctypes.c_int,
             ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long,
             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+        lib.po_oracle_adjoint.restype = ctypes.c_int
+        lib.po_oracle_adjoint.argtypes = [
+            ctypes.c_int, ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p,
+            ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p,
+            ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _lib = lib
     return _lib
 
@@ -83,6 +89,35 @@ def run(mode, src7, cur, gmode, ncx, ncy, tgt7, k, epsilon=1.0, t_dir=-1.0,
     if rc != 0:
         raise RuntimeError(f"po_oracle_run failed with status {rc}")
     return out
+
+
+def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-1.0,
+            nthreads=None, want=("cur", "ds", "dt")):
+    """FP64 vector-Jacobian product of `run` (po_oracle_adjoint): gradients of
+    L = sum(cot * run(...)) with respect to the currents ("cur", the shape of
+    cur), the normal displacement of every source ("ds", (ns,)) and, near
+    field and scalar, of every target ("dt", (nt,)). Modes JM, EH, JMEH, FF,
+    scalar."""
+    lib = load()
+    src7 = np.ascontiguousarray(src7, dtype=np.float64)
+    tgt7 = np.ascontiguousarray(tgt7, dtype=np.float64)
+    cur = np.ascontiguousarray(cur, dtype=np.float64)
+    cot = np.ascontiguousarray(cot, dtype=np.float64)
+    ns, nt = src7.shape[1], tgt7.shape[1]
+    if cot.shape != (N_OUT[mode], nt):
+        raise ValueError(f"cot must have shape {(N_OUT[mode], nt)}")
+    gc = np.zeros(cur.shape) if "cur" in want else None
+    gs = np.zeros(ns) if "ds" in want else None
+    gt = np.zeros(nt) if ("dt" in want and mode != "FF") else None
+    if nthreads is None:
+        nthreads = os.cpu_count() or 1
+    ptr = lambda a: a.ctypes.data if a is not None else None
+    rc = lib.po_oracle_adjoint(MODES[mode], ns, src7.ctypes.data, cur.ctypes.data, int(gmode), int(ncx), int(ncy),
+                               nt, tgt7.ctypes.data, cot.ctypes.data, float(k), float(epsilon), float(t_dir),
+                               int(nthreads), ptr(gc), ptr(gs), ptr(gt))
+    if rc != 0:
+        raise RuntimeError(f"po_oracle_adjoint failed with status {rc}")
+    return {name: a for name, a in (("cur", gc), ("ds", gs), ("dt", gt)) if a is not None}
 
 
 class Reference:

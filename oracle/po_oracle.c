@@ -392,3 +392,369 @@ int po_oracle_run(int mode, long ns, const double *src, const double *cur,
     free(th);
     return 0;
 }
+
+/* ------------------------------------------------------------------ adjoint
+ *
+ * FP64 vector-Jacobian product of po_oracle_run for modes JM, EH, JMEH, FF and
+ * scalar. The reference has no derivatives; this is the CPU statement of the
+ * engine's adjoint (the formulas of pypo_gb300/csrc/po_adjoint.cu, written
+ * here from the forward above), used as a checker and as the CPU baseline's
+ * adjoint leg. For a real loss L = sum(cot * out):
+ *   - the cotangent rows map onto (gE, gH) per target: EH, FF direct; JM
+ *     J = 2 n x H gives gH += 2 gJ x n; JMEH adds its E, H rows; FF then
+ *     becomes gS_J = P gE + t r x gH, gS_M = P gH - t r x gE (P = I - r r^T);
+ *   - currents: Jbar' = sum_t conj(c1) gE + conj(c2)(gE.d)d + conj(c3)(gH x d),
+ *     Mbar' = sum_t conj(c1) gH + conj(c2)(gH.d)d - conj(c3)(gE x d), with
+ *     c1 = G s1, c2 = G s2 / R^2, c3 = G s3 / R (s1..s3 and G = e^{t j k R} as
+ *     in or_field_at_point); far field Jbar' = sum_t conj(G) gS_J (and M);
+ *     the gradient with respect to the caller's currents is
+ *     conj(prefactor * weight * area) times these;
+ *   - displacement of a point along its frozen normal (areas frozen, the
+ *     reference's surface-error convention, InterfaceReflector.cpp:852-866):
+ *     phi(d) = Re[a.E + b.H] for one pair, a = conj gE, b = conj gH, d = r_t - r_s;
+ *     grad phi = Re[sigma d + c2 grad(beta) + c3 W] with alpha = a.J + b.M,
+ *     beta = (J.d)(a.d) + (M.d)(b.d), W = a x M - b x J,
+ *     sigma = d1 alpha + d2 beta + d3 (W.d) and the radial derivatives
+ *     d1 = G/R^2 [t(1-3u^2) + j(2u-3u^3)], d2 = G/R^4 [-t(1-15u^2) + j(-6u+15u^3)],
+ *     d3 = G/R^3 [-(1-3u^2) - 3jtu]; dL/d delta_s = -n_s . sum_t grad phi,
+ *     dL/d delta_t = n_t . sum_s grad phi; far field
+ *     dL/d delta_s = t k (n_s . r) Im[G (conj(gS_J).J' + conj(gS_M).M')];
+ *     scalar: out = sum c f with c = -k^2 e^{-t j k r} w A / (4 pi r),
+ *     dc/dr = c (-t j k - 1/r);
+ *   - the illumination mask is piecewise constant: its derivative is dropped.
+ */
+
+typedef struct {
+    int mode, side;          /* side 0: one source per item; 1: one target per item */
+    long ns, nt;
+    const double *src, *tgt;
+    const cplx *Jp, *Mp;     /* folded currents, 3 per source (scalar: Jp[0] = f') */
+    const cplx *gE, *gH;     /* mapped cotangents, 3 per target (scalar: gE[0]) */
+    const double *dir;       /* far field: r_hat, 3 per target */
+    double k, t;
+    double *acc;             /* side 0: 13 per source (Jbar' re/im 6, Mbar' 6, displacement) */
+    double *gdt;             /* side 1: one per target */
+    long begin, end;
+} oa_job;
+
+static cplx oa_dot_r(const cplx *v, const double *x) { return v[0] * x[0] + v[1] * x[1] + v[2] * x[2]; }
+static cplx oa_dot_c(const cplx *a, const cplx *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static void oa_cross_r(const cplx *v, const double *x, cplx *o)
+{
+    o[0] = v[1] * x[2] - v[2] * x[1];
+    o[1] = v[2] * x[0] - v[0] * x[2];
+    o[2] = v[0] * x[1] - v[1] * x[0];
+}
+
+/* Near-field pair: c2, c3 and the gradient of phi along `nv`, the caller's
+ * normal (n . grad phi). Lit test and rounding as or_field_at_point. */
+static int oa_nf_pair(const oa_job *jb, long s, long ti, double d[3], double *R_out, cplx *c1, cplx *c2, cplx *c3,
+                      cplx *d1, cplx *d2, cplx *d3)
+{
+    const double *sp = jb->src, *tp = jb->tgt;
+    const long ns = jb->ns, nt = jb->nt;
+    d[0] = tp[ti] - sp[s];
+    d[1] = tp[nt + ti] - sp[ns + s];
+    d[2] = tp[2 * nt + ti] - sp[2 * ns + s];
+    const double R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double rinv = 1.0 / R;
+    const double rh[3] = {d[0] * rinv, d[1] * rinv, d[2] * rinv};
+    const double ndr = sp[3 * ns + s] * rh[0] + sp[4 * ns + s] * rh[1] + sp[5 * ns + s] * rh[2];
+    if (ndr < 0) return 0;
+    const double t = jb->t, u = 1.0 / (jb->k * R), u2 = u * u, u3 = u2 * u;
+    const double rinv2 = rinv * rinv;
+    const cplx G = cexp(t * I * jb->k * R);
+    *c1 = G * (t * u2 + I * (u3 - u));
+    *c2 = (-3.0 * *c1 - 2.0 * I * u * G) * rinv2;
+    *c3 = G * (-u2 * rinv + I * t * u * rinv);
+    *d1 = G * (t * (1 - 3 * u2) + I * (2 * u - 3 * u3)) * rinv2;
+    *d2 = G * (-t * (1 - 15 * u2) + I * (-6 * u + 15 * u3)) * rinv2 * rinv2;
+    *d3 = G * (-(1 - 3 * u2) - 3 * I * t * u) * rinv2 * rinv;
+    *R_out = R;
+    return 1;
+}
+
+/* n . grad_d phi for one near-field pair (J, M the folded currents of the
+ * source; a, b the conjugated cotangents of the target). */
+static double oa_nf_grad(const double d[3], const double n[3], cplx c2, cplx c3, cplx d1, cplx d2, cplx d3,
+                         const cplx *J, const cplx *M, const cplx *a, const cplx *b)
+{
+    const cplx Jd = oa_dot_r(J, d), Md = oa_dot_r(M, d), ad = oa_dot_r(a, d), bd = oa_dot_r(b, d);
+    const cplx alpha = oa_dot_c(a, J) + oa_dot_c(b, M);
+    const cplx beta = Jd * ad + Md * bd;
+    cplx Mxd[3], Jxd[3], Mxn[3], Jxn[3];
+    oa_cross_r(M, d, Mxd);
+    oa_cross_r(J, d, Jxd);
+    oa_cross_r(M, n, Mxn);
+    oa_cross_r(J, n, Jxn);
+    const cplx Wd = oa_dot_c(a, Mxd) - oa_dot_c(b, Jxd);
+    const cplx Wn = oa_dot_c(a, Mxn) - oa_dot_c(b, Jxn);
+    const cplx gbn = ad * oa_dot_r(J, n) + Jd * oa_dot_r(a, n) + bd * oa_dot_r(M, n) + Md * oa_dot_r(b, n);
+    const cplx sig = d1 * alpha + d2 * beta + d3 * Wd;
+    const double ndd = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
+    return creal(sig) * ndd + creal(c2 * gbn) + creal(c3 * Wn);
+}
+
+static void *oa_worker(void *arg)
+{
+    const oa_job *jb = (const oa_job *)arg;
+    const long ns = jb->ns, nt = jb->nt;
+    const double *sp = jb->src, *tp = jb->tgt;
+    const double k = jb->k, t = jb->t;
+    for (long it = jb->begin; it < jb->end; ++it) {
+        if (jb->side == 1) {   /* target displacement (near field) */
+            const long ti = it;
+            const double n[3] = {tp[3 * nt + ti], tp[4 * nt + ti], tp[5 * nt + ti]};
+            cplx a[3], b[3];
+            for (int q = 0; q < 3; ++q) { a[q] = conj(jb->gE[3 * ti + q]); b[q] = conj(jb->gH[3 * ti + q]); }
+            double acc = 0;
+            for (long s = 0; s < ns; ++s) {
+                double d[3], R;
+                cplx c1, c2, c3, d1, d2, d3;
+                if (jb->mode == OR_SCALAR) {
+                    d[0] = tp[ti] - sp[s]; d[1] = tp[nt + ti] - sp[ns + s]; d[2] = tp[2 * nt + ti] - sp[2 * ns + s];
+                    R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                    const cplx c = cexp(-t * I * k * R) / R;
+                    const cplx dcdr = c * (-t * I * k - 1.0 / R);
+                    const double ndd = (n[0] * d[0] + n[1] * d[1] + n[2] * d[2]) / R;
+                    acc += creal(a[0] * jb->Jp[3 * s] * dcdr) * ndd;
+                    continue;
+                }
+                if (!oa_nf_pair(jb, s, ti, d, &R, &c1, &c2, &c3, &d1, &d2, &d3)) continue;
+                acc += oa_nf_grad(d, n, c2, c3, d1, d2, d3, jb->Jp + 3 * s, jb->Mp + 3 * s, a, b);
+            }
+            jb->gdt[ti] = acc;
+            continue;
+        }
+        const long s = it;
+        const double n[3] = {sp[3 * ns + s], sp[4 * ns + s], sp[5 * ns + s]};
+        const cplx *J = jb->Jp + 3 * s, *M = jb->Mp + 3 * s;
+        cplx jb_[3] = {0, 0, 0}, mb_[3] = {0, 0, 0};
+        double dsum = 0;
+        for (long ti = 0; ti < nt; ++ti) {
+            const cplx *gE = jb->gE + 3 * ti, *gH = jb->gH + 3 * ti;
+            if (jb->mode == OR_SCALAR) {
+                double d[3] = {tp[ti] - sp[s], tp[nt + ti] - sp[ns + s], tp[2 * nt + ti] - sp[2 * ns + s]};
+                const double R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                const cplx c = cexp(-t * I * k * R) / R;
+                jb_[0] += conj(c) * gE[0];
+                const cplx dcdr = c * (-t * I * k - 1.0 / R);
+                const double ndd = (n[0] * d[0] + n[1] * d[1] + n[2] * d[2]) / R;
+                dsum -= creal(conj(gE[0]) * J[0] * dcdr) * ndd;
+                continue;
+            }
+            if (jb->mode == OR_FF) {
+                const double *r = jb->dir + 3 * ti;
+                const double ndr = n[0] * r[0] + n[1] * r[1] + n[2] * r[2];
+                if (ndr < 0) continue;
+                const double rpr = sp[s] * r[0] + sp[ns + s] * r[1] + sp[2 * ns + s] * r[2];
+                const cplx G = cexp(-t * I * k * rpr);
+                cplx Z = 0;
+                for (int q = 0; q < 3; ++q) {
+                    jb_[q] += conj(G) * gE[q];
+                    mb_[q] += conj(G) * gH[q];
+                    Z += conj(gE[q]) * J[q] + conj(gH[q]) * M[q];
+                }
+                dsum += t * k * cimag(G * Z) * ndr;
+                continue;
+            }
+            double d[3], R;
+            cplx c1, c2, c3, d1, d2, d3;
+            if (!oa_nf_pair(jb, s, ti, d, &R, &c1, &c2, &c3, &d1, &d2, &d3)) continue;
+            const cplx ged = oa_dot_r(gE, d), ghd = oa_dot_r(gH, d);
+            cplx ghxd[3], gexd[3];
+            oa_cross_r(gH, d, ghxd);
+            oa_cross_r(gE, d, gexd);
+            for (int q = 0; q < 3; ++q) {
+                jb_[q] += conj(c1) * gE[q] + conj(c2) * ged * d[q] + conj(c3) * ghxd[q];
+                mb_[q] += conj(c1) * gH[q] + conj(c2) * ghd * d[q] - conj(c3) * gexd[q];
+            }
+            cplx a[3], b[3];
+            for (int q = 0; q < 3; ++q) { a[q] = conj(gE[q]); b[q] = conj(gH[q]); }
+            dsum -= oa_nf_grad(d, n, c2, c3, d1, d2, d3, J, M, a, b);
+        }
+        double *o = jb->acc + 13 * s;
+        for (int q = 0; q < 3; ++q) {
+            o[q] = creal(jb_[q]);
+            o[3 + q] = cimag(jb_[q]);
+            o[6 + q] = creal(mb_[q]);
+            o[9 + q] = cimag(mb_[q]);
+        }
+        o[12] = dsum;
+    }
+    return NULL;
+}
+
+static void oa_run(oa_job *base, long n, int nthreads)
+{
+    if (n <= 0) return;
+    if (nthreads > n) nthreads = (int)n;
+    if (nthreads < 1) nthreads = 1;
+    oa_job *jobs = (oa_job *)malloc(sizeof(oa_job) * nthreads);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    char *live = (char *)calloc(nthreads, 1);
+    if (!jobs || !th || !live) {   /* run serially */
+        base->begin = 0;
+        base->end = n;
+        oa_worker(base);
+        free(jobs); free(th); free(live);
+        return;
+    }
+    long step = (n + nthreads - 1) / nthreads;
+    for (int w = 0; w < nthreads; ++w) {
+        jobs[w] = *base;
+        jobs[w].begin = w * step;
+        jobs[w].end = (w + 1) * step < n ? (w + 1) * step : n;
+        if (jobs[w].begin >= jobs[w].end) continue;
+        if (nthreads == 1 || pthread_create(&th[w], NULL, oa_worker, &jobs[w]) != 0)
+            oa_worker(&jobs[w]);
+        else
+            live[w] = 1;
+    }
+    for (int w = 0; w < nthreads; ++w)
+        if (live[w]) pthread_join(th[w], NULL);
+    free(live);
+    free(jobs);
+    free(th);
+}
+
+/*
+ * Adjoint of po_oracle_run. cot: po_oracle_nout(mode) rows of nt. Outputs
+ * (each may be NULL): grad_cur (12, ns) rows in c2Bundle order (2 rows for
+ * scalar), grad_ds (ns), grad_dt (nt; near field and scalar). Returns 0 on
+ * success, 1 for a mode without an adjoint (EHP) or bad sizes, 2 on memory.
+ */
+int po_oracle_adjoint(int mode, long ns, const double *src, const double *cur,
+                      int gmode, int ncx, int ncy, long nt, const double *tgt,
+                      const double *cot, double k, double epsilon, double t_dir, int nthreads,
+                      double *grad_cur, double *grad_ds, double *grad_dt)
+{
+    (void)epsilon;
+    if (mode < 0 || mode > 5 || mode == OR_EHP || ns < 0 || nt < 0) return 1;
+    if (mode == OR_FF) grad_dt = NULL;
+    int unit_w = gmode < 0;
+    if (unit_w) { ncx = ns > 0 ? 1 : 0; ncy = (int)ns; }
+    else if ((long)ncx * ncy != ns) return 1;
+    const int sc = mode == OR_SCALAR;
+    const int ncur = sc ? 2 : 12;
+    if (ns == 0 || nt == 0) {
+        if (grad_cur) memset(grad_cur, 0, sizeof(double) * ncur * ns);
+        if (grad_ds) memset(grad_ds, 0, sizeof(double) * ns);
+        if (grad_dt) memset(grad_dt, 0, sizeof(double) * nt);
+        return 0;
+    }
+    const double pif = (double)3.14159265359f;
+    const double pref = k * k / (4. * pif);
+    /* folded prefactor: near field pref, far field -j pref, scalar -k^2/(4 pi) */
+    const cplx fac = sc ? -k * k / (4 * pif) : (mode == OR_FF ? -I * pref : pref);
+    cplx *Jp = (cplx *)malloc(sizeof(cplx) * 3 * ns), *Mp = (cplx *)malloc(sizeof(cplx) * 3 * ns);
+    cplx *fw = (cplx *)malloc(sizeof(cplx) * ns);
+    cplx *gE = (cplx *)calloc(3 * nt, sizeof(cplx)), *gH = (cplx *)calloc(3 * nt, sizeof(cplx));
+    double *dir = (double *)malloc(sizeof(double) * 3 * nt);
+    double *acc = (double *)calloc(13 * ns, sizeof(double));
+    if (!Jp || !Mp || !fw || !gE || !gH || !dir || !acc) {
+        free(Jp); free(Mp); free(fw); free(gE); free(gH); free(dir); free(acc);
+        return 2;
+    }
+    for (long s = 0; s < ns; ++s) {
+        const int xu = unit_w ? 0 : (int)(s / ncy), yv = unit_w ? 0 : (int)(s % ncy);
+        double w = 1.0;
+        if (!unit_w) {
+            int yhalf;
+            w = or_half_weight(gmode, ncx, ncy, xu, yv, &yhalf);
+            if (yhalf) w *= 0.5;
+        }
+        fw[s] = fac * w * src[6 * ns + s];
+        if (sc) {
+            Jp[3 * s] = fw[s] * (cur[s] + I * cur[ns + s]);
+            Jp[3 * s + 1] = Jp[3 * s + 2] = 0;
+            Mp[3 * s] = Mp[3 * s + 1] = Mp[3 * s + 2] = 0;
+            continue;
+        }
+        for (int q = 0; q < 3; ++q) {
+            Jp[3 * s + q] = fw[s] * (cur[q * ns + s] + I * cur[(3 + q) * ns + s]);
+            Mp[3 * s + q] = fw[s] * (cur[(6 + q) * ns + s] + I * cur[(9 + q) * ns + s]);
+        }
+    }
+    for (long i = 0; i < nt; ++i) {
+        cplx *e = gE + 3 * i, *h = gH + 3 * i;
+        if (sc) { e[0] = cot[i] + I * cot[nt + i]; continue; }
+        if (mode == OR_EH || mode == OR_FF)
+            for (int q = 0; q < 3; ++q) {
+                e[q] = cot[q * nt + i] + I * cot[(3 + q) * nt + i];
+                h[q] = cot[(6 + q) * nt + i] + I * cot[(9 + q) * nt + i];
+            }
+        if (mode == OR_JMEH)
+            for (int q = 0; q < 3; ++q) {
+                e[q] = cot[(12 + q) * nt + i] + I * cot[(15 + q) * nt + i];
+                h[q] = cot[(18 + q) * nt + i] + I * cot[(21 + q) * nt + i];
+            }
+        if (mode == OR_JM || mode == OR_JMEH) {   /* J = 2 n x H: gH += 2 gJ x n */
+            const double n[3] = {tgt[3 * nt + i], tgt[4 * nt + i], tgt[5 * nt + i]};
+            cplx g[3], gxn[3];
+            for (int q = 0; q < 3; ++q) g[q] = cot[q * nt + i] + I * cot[(3 + q) * nt + i];
+            oa_cross_r(g, n, gxn);
+            for (int q = 0; q < 3; ++q) h[q] += 2.0 * gxn[q];
+        }
+        if (mode == OR_FF) {
+            const double th = tgt[i], ph = tgt[nt + i];
+            double *r = dir + 3 * i;
+            r[0] = cos(ph) * sin(th); r[1] = sin(ph) * sin(th); r[2] = cos(th);
+            const cplx ed = oa_dot_r(e, r), hd = oa_dot_r(h, r);
+            cplx hxr[3], exr[3], sj[3], sm[3];
+            /* r x v = -(v x r) */
+            oa_cross_r(h, r, hxr);
+            oa_cross_r(e, r, exr);
+            for (int q = 0; q < 3; ++q) {
+                sj[q] = e[q] - ed * r[q] - t_dir * hxr[q];
+                sm[q] = h[q] - hd * r[q] + t_dir * exr[q];
+            }
+            for (int q = 0; q < 3; ++q) { e[q] = sj[q]; h[q] = sm[q]; }
+        }
+    }
+    oa_job base;
+    memset(&base, 0, sizeof(base));
+    base.mode = mode;
+    base.ns = ns;
+    base.nt = nt;
+    base.src = src;
+    base.tgt = tgt;
+    base.Jp = Jp;
+    base.Mp = Mp;
+    base.gE = gE;
+    base.gH = gH;
+    base.dir = dir;
+    base.k = k;
+    base.t = t_dir;
+    base.acc = acc;
+    base.gdt = grad_dt;
+    if (grad_cur || grad_ds) {
+        base.side = 0;
+        oa_run(&base, ns, nthreads);
+    }
+    if (grad_dt) {
+        base.side = 1;
+        oa_run(&base, nt, nthreads);
+    }
+    for (long s = 0; s < ns; ++s) {
+        const double *a = acc + 13 * s;
+        const cplx f = conj(fw[s]);
+        if (grad_cur) {
+            if (sc) {
+                const cplx g = f * (a[0] + I * a[3]);
+                grad_cur[s] = creal(g);
+                grad_cur[ns + s] = cimag(g);
+            } else {
+                for (int g = 0; g < 2; ++g)
+                    for (int q = 0; q < 3; ++q) {
+                        const cplx v = f * (a[6 * g + q] + I * a[6 * g + 3 + q]);
+                        grad_cur[(6 * g + q) * ns + s] = creal(v);
+                        grad_cur[(6 * g + 3 + q) * ns + s] = cimag(v);
+                    }
+            }
+        }
+        if (grad_ds) grad_ds[s] = a[12];
+    }
+    free(Jp); free(Mp); free(fw); free(gE); free(gH); free(dir); free(acc);
+    return 0;
+}
