@@ -95,6 +95,12 @@ typedef struct reflcontainerf {
     float *x, *y, *z, *nx, *ny, *nz, *area;
 } reflcontainerf;
 
+/* Ray-trace frame (reference Structs.h:352-362); only callRTKernel takes it. */
+typedef struct cframef {
+    int size;
+    float *x, *y, *z, *dx, *dy, *dz;
+} cframef;
+
 /* ---- errors ------------------------------------------------------------- */
 
 /* Message of the last failed call on this thread ("" when none). */
@@ -134,6 +140,16 @@ int callKernelf_scalar(arrC1f *res, reflparamsf source, reflparamsf target,
                        reflcontainerf *cs, reflcontainerf *ct, arrC1f *inp,
                        float k, float epsilon, float t_direction, int nBlocks, int nThreads);
     /* replaces Kernelsf.cu:2113-2175 */
+
+/* The reference's loadGPUlib (src/PyPO/BindGPU.py:18-81) also binds its GPU
+ * ray tracer, callRTKernel (InterfaceCUDA.h:66-68), so the library must
+ * export that name for the unmodified loader to bind. The ray tracer is not
+ * part of this library: the call writes nothing to fr_out, returns 6, sets
+ * po_last_error() and prints one line on stderr (the reference's binding
+ * ignores the status). Bind callRTKernel from libpypogpu to keep GPU ray
+ * tracing. */
+int callRTKernel(reflparamsf ctp, cframef *fr_in, cframef *fr_out, float epsilon, float t0,
+                 int nBlocks, int nThreads);
 
 /* ---- FP64 grid generation ------------------------------------------------
  * Same contract as the reference's generateGrid (src/common/InterfaceReflector.h:24-25,
@@ -263,7 +279,10 @@ int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int nc
  * latency-critical loop that cannot take the device-wide synchronisation of
  * cudaFree. Same arguments and results as po_run_dev in mixed precision, plus
  * `status`: an optional device int, cleared at the start of the call and set
- * to 101 if a kernel gave up a bounded wait (NULL: an internal word).
+ * to 101 if a kernel gave up a bounded wait. With status == NULL the 101 goes
+ * to an internal word inside the array instead, which stays set across calls
+ * until po_device_error reads and clears it (po_device_error allocates
+ * nothing).
  * The scratch is a fixed 64 MiB device array inside the library, held by
  * every GPU that loads it until the process exits; problems needing more
  * (about 88*ns + 128*nt bytes, plus 96*nt per extra source chunk) are
@@ -303,10 +322,27 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
 /* Number of kernel launches the last call on this thread queued. */
 int po_last_launches(void);
 
-/* Synchronises `stream`, then returns (and clears) the device error word in
+/* Synchronises `stream`, then returns (and clears) the device error words in
  * *code: 0 when every kernel finished normally, 101 when a kernel gave up a
- * bounded wait for a tile copy (its results are then invalid). */
+ * bounded wait for a tile copy (its results are then invalid). It reads the
+ * word of the allocating entries and the internal word of po_run_dev_static
+ * (calls made with status == NULL); it allocates nothing. */
 int po_device_error(void *stream, int *code);
+
+/* Self-test of the failure detection (no counterpart in the reference, whose
+ * CUDA error path calls exit(), src/include/MemUtils.h:27-34). One CTA waits
+ * on an mbarrier that nothing arrives on, with `limit` bounded polls (the
+ * kernels' own wait), gives up, and sets 101 in: `err` (a device int) when
+ * non-NULL, else the allocating entries' word (word == 0) or the internal
+ * word of po_run_dev_static (word == 1; 3 if that entry has not run on this
+ * device yet). No copy is in flight while it waits, so giving up is clean.
+ * Queued on `stream`. */
+int po_wait_selftest(unsigned limit, int *err, int word, void *stream);
+
+/* Bytes of the library's own scratch pool on the current device that are in
+ * use (allocated and not yet freed in stream order); 0 before the pool
+ * exists. The pool is private: the device's default pool is not changed. */
+int po_scratch_in_use(unsigned long long *bytes);
 
 /* ---- measurement support --------------------------------------------------
  * po_timing_enable(n) arms n CUDA event pairs, recorded on the launching

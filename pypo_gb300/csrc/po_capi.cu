@@ -1,6 +1,8 @@
 // po_capi.cu -- the extern "C" entry points of libpo_gb300 (include/po_gb300.h).
 #include <cuda_runtime.h>
 
+#include <cstdio>
+
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -50,8 +52,8 @@ __global__ void po_any_nonzero_kernel(const double *__restrict__ p, long n, int 
 int device_m_is_zero(const double *d_cur, long ns, cudaStream_t s, bool &zero)
 {
     int *flag = nullptr, h = 0;
-    cudaError_t e = cudaMallocAsync(&flag, sizeof(int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+    if (int rc = po::scratch_alloc(reinterpret_cast<void **>(&flag), sizeof(int), s)) return rc;
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
     if (e == cudaSuccess) {
         po_any_nonzero_kernel<<<2 * 152, 256, 0, s>>>(d_cur + 6 * ns, 6 * ns, flag);
         e = cudaGetLastError();
@@ -90,6 +92,12 @@ int m_is_zero(const double *h_cur, const double *d_cur, long ns, cudaStream_t s,
             rc = fail(2, std::string(#expr) + ": " + cudaGetErrorString(e_));             \
             goto done;                                                                    \
         }                                                                                 \
+    } while (0)
+
+// Stream-ordered scratch of a host-buffer call, from the library's own pool.
+#define PO_SCRATCH(ptr, bytes)                                                            \
+    do {                                                                                  \
+        if ((rc = po::scratch_alloc(reinterpret_cast<void **>(&ptr), (bytes), s))) goto done; \
     } while (0)
 
 // Host slot for the frame's half-extent read back by a host-buffer call. It
@@ -144,10 +152,10 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
     int rc = 0, code = 0;
     double extent = 0.0;
     po::RunArgs a;
-    CK(cudaMallocAsync(&d_src, sizeof(double) * 7 * std::max(ns, 1L), s));
-    CK(cudaMallocAsync(&d_cur, sizeof(double) * ncur * std::max(ns, 1L), s));
-    CK(cudaMallocAsync(&d_tgt, sizeof(double) * 7 * nt, s));
-    CK(cudaMallocAsync(&d_out, sizeof(double) * nout * nt, s));
+    PO_SCRATCH(d_src, sizeof(double) * 7 * std::max(ns, 1L));
+    PO_SCRATCH(d_cur, sizeof(double) * ncur * std::max(ns, 1L));
+    PO_SCRATCH(d_tgt, sizeof(double) * 7 * nt);
+    PO_SCRATCH(d_out, sizeof(double) * nout * nt);
     if (ns > 0) {
         CK(cudaMemcpyAsync(d_src, src7, sizeof(double) * 7 * ns, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_cur, cur, sizeof(double) * ncur * ns, cudaMemcpyHostToDevice, s));
@@ -445,13 +453,13 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     double *ext = extent_slot(&extent);
     *ext = 0.0;
     const size_t ns1 = std::max(ns, 1L), nt1 = std::max(nt, 1L);
-    CK(cudaMallocAsync(&d_src, sizeof(double) * 7 * ns1, s));
-    CK(cudaMallocAsync(&d_cur, sizeof(double) * 12 * ns1, s));
-    CK(cudaMallocAsync(&d_tgt, sizeof(double) * 7 * nt1, s));
-    CK(cudaMallocAsync(&d_cot, sizeof(double) * nout * nt1, s));
-    if (grad_cur) CK(cudaMallocAsync(&d_gc, sizeof(double) * 12 * ns1, s));
-    if (grad_ds) CK(cudaMallocAsync(&d_gs, sizeof(double) * ns1, s));
-    if (grad_dt) CK(cudaMallocAsync(&d_gt, sizeof(double) * nt1, s));
+    PO_SCRATCH(d_src, sizeof(double) * 7 * ns1);
+    PO_SCRATCH(d_cur, sizeof(double) * 12 * ns1);
+    PO_SCRATCH(d_tgt, sizeof(double) * 7 * nt1);
+    PO_SCRATCH(d_cot, sizeof(double) * nout * nt1);
+    if (grad_cur) PO_SCRATCH(d_gc, sizeof(double) * 12 * ns1);
+    if (grad_ds) PO_SCRATCH(d_gs, sizeof(double) * ns1);
+    if (grad_dt) PO_SCRATCH(d_gt, sizeof(double) * nt1);
     if (ns > 0) {
         CK(cudaMemcpyAsync(d_src, src7, sizeof(double) * 7 * ns, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_cur, cur, sizeof(double) * 12 * ns, cudaMemcpyHostToDevice, s));
@@ -506,7 +514,38 @@ int po_fp32_probe(int blocks, int iters, float *out, void *stream)
 int po_device_error(void *stream, int *code)
 {
     po::clear_error();
+    if (!code) return fail(1, "po_device_error: null code");
     return po::read_device_error(static_cast<cudaStream_t>(stream), code);
+}
+
+int po_wait_selftest(unsigned limit, int *err, int word, void *stream)
+{
+    po::clear_error();
+    int *w = err;
+    if (!w) {
+        if (word == 0) {
+            w = po::error_word();
+            if (!w) return fail(2, "po_wait_selftest: no device error word");
+        } else if (word == 1) {
+            w = po::static_status_word();
+            if (!w) return fail(3, "po_wait_selftest: po_run_dev_static has not run on this device");
+        } else {
+            return fail(1, "po_wait_selftest: word must be 0 (allocating entries) or 1 (po_run_dev_static)");
+        }
+    }
+    void *args[] = {&limit, &w};
+    cudaError_t e = cudaLaunchKernel(po::wait_selftest_kernel(), dim3(1), dim3(64), args, 0,
+                                     static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(2, std::string("po_wait_selftest: ") + cudaGetErrorString(e));
+    po::note_launches(1);
+    return 0;
+}
+
+int po_scratch_in_use(unsigned long long *bytes)
+{
+    po::clear_error();
+    if (!bytes) return fail(1, "po_scratch_in_use: null argument");
+    return po::scratch_used(bytes);
 }
 
 #define ROWS12(b) {b->r1x, b->r1y, b->r1z, b->i1x, b->i1y, b->i1z, b->r2x, b->r2y, b->r2z, b->i2x, b->i2y, b->i2z}
@@ -566,6 +605,14 @@ int callKernelf_scalar(arrC1f *res, reflparamsf source, reflparamsf target, refl
     float *r[2] = {res->x, res->y};
     float *c[2] = {inp->x, inp->y};
     return drop_in(po::kScalar, r, source, target, cs, ct, c, k, epsilon, t_direction);
+}
+
+int callRTKernel(reflparamsf, cframef *, cframef *, float, float, int, int)
+{
+    static const char msg[] =
+        "callRTKernel: the GPU ray tracer is not part of libpo_gb300; bind callRTKernel from libpypogpu";
+    std::fprintf(stderr, "libpo_gb300: %s\n", msg);
+    return fail(6, msg);
 }
 
 }  // extern "C"

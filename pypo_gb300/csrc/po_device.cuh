@@ -42,11 +42,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: gives up after kWaitLimit polls (each poll may itself block
-// for a bounded hardware time slice) and reports false.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+// Bounded wait: gives up after `limit` polls (kWaitLimit in the kernels; each
+// poll may itself block for a bounded hardware time slice) and reports false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t limit = kWaitLimit)
 {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
+    for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -113,10 +113,10 @@ int efficiency_sums_dev(long n, const double *g7, const double *fr, const double
         ap.rx[0] = aper[2]; ap.rx[1] = aper[3]; ap.ry[0] = aper[4]; ap.ry[1] = aper[5];
     }
     double *part = nullptr;
-    cudaError_t e = cudaMallocAsync(&part, sizeof(double) * kEffBlocks * kEffSums, s);
-    if (e != cudaSuccess) return fail(3, std::string("efficiency scratch: ") + cudaGetErrorString(e));
+    if (int rc = po::scratch_alloc(reinterpret_cast<void **>(&part), sizeof(double) * kEffBlocks * kEffSums, s))
+        return rc;
     po_eff_partial_kernel<<<kEffBlocks, kEffThreads, 0, s>>>(n, g7, fr, fi, gr, gi, ap, part);
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) {
         po_eff_final_kernel<<<1, 32, 0, s>>>(kEffBlocks, part, sums);
         e = cudaGetLastError();

@@ -5,8 +5,9 @@
 //   (target block, source chunk) grid -> FP64 epilogue summing the chunks.
 // Plain FP64 (precision 1):
 //   pack sources (double) -> one-thread-per-target FP64 direct sum -> epilogue.
-// Scratch is stream-ordered (cudaMallocAsync / cudaFreeAsync) on the caller's
-// stream; nothing here synchronises the device.
+// Scratch is stream-ordered on the caller's stream, from the library's own
+// memory pool (scratch_alloc / scratch_free); nothing here synchronises the
+// device.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,6 +31,7 @@ thread_local int t_launches = 0;
 struct DeviceInfo {
     bool ready = false;
     int sms = 0;
+    cudaMemPool_t pool = nullptr;   // the library's own scratch pool
     int occ2[3][2][2] = {};  // pair-packed kernels, [kind][t>0][has_m]
     std::map<void *, int> occ_adj;   // adjoint kernels: resident CTAs, attribute set
 };
@@ -97,15 +99,19 @@ static int device_info(DeviceInfo *&out)
     DeviceInfo &di = g_dev[dev];
     if (!di.ready) {
         PO_CK(cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev));
-        // Scratch comes from the device's stream-ordered pool, which by
-        // default hands freed memory back to the driver at every
-        // synchronisation, so each host-buffer call (which synchronises)
-        // would map its scratch afresh. Keep up to kPoolKeep bytes of freed
-        // scratch in this process's pool instead.
-        cudaMemPool_t pool;
-        PO_CK(cudaDeviceGetMemPool(&pool, dev));
+        // Scratch comes from a stream-ordered pool of the library's own, so
+        // the device's default pool (shared with every other user in the
+        // process) keeps its settings. A pool hands freed memory back to the
+        // driver at every synchronisation unless told otherwise, so each
+        // host-buffer call (which synchronises) would map its scratch afresh;
+        // this one keeps up to kPoolKeep bytes of freed scratch.
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        PO_CK(cudaMemPoolCreate(&di.pool, &props));
         uint64_t keep = kPoolKeep;
-        PO_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        PO_CK(cudaMemPoolSetAttribute(di.pool, cudaMemPoolAttrReleaseThreshold, &keep));
         for (int kind = 0; kind < 3; ++kind)
             for (int ts = 0; ts < 2; ++ts)
                 for (int hm = 0; hm < 2; ++hm) {
@@ -123,20 +129,16 @@ static int device_info(DeviceInfo *&out)
     return 0;
 }
 
-// Number of source chunks: minimise waves * chunk length, given `slots`
-// resident CTAs, with a small cost per extra chunk (partials, prologue) and
-// the partial buffer capped near 1 GiB.
-static long choose_split(long ntb, long ns, long slots, long nt, int nacc, long tile = kTile)
+long choose_split(long nb, long ns, long slots, long max_chunks, long tile)
 {
     const long tiles = std::max(1L, (ns + tile - 1) / tile);
-    const long cap = std::max(1L, (1L << 30) / std::max(1L, nt * nacc * 8));
     long best = 1;
     double best_cost = 1e300;
-    for (long s = 1; s <= std::min(tiles, std::min(cap, 1024L)); ++s) {
+    for (long s = 1; s <= std::min(tiles, std::min(std::max(1L, max_chunks), 1024L)); ++s) {
         const long chunk = (tiles + s - 1) / s;
         const long real = (tiles + chunk - 1) / chunk;
         if (real != s) continue;
-        const long waves = (ntb * real + slots - 1) / slots;
+        const long waves = (nb * real + slots - 1) / slots;
         const double cost = (double)waves * chunk + 0.05 * real;
         if (cost < best_cost - 1e-9) {
             best_cost = cost;
@@ -146,13 +148,46 @@ static long choose_split(long ntb, long ns, long slots, long nt, int nacc, long 
     return best;
 }
 
+// Partial buffers of the chunked kernels are capped near 1 GiB.
+static long partial_cap(long n, int nacc) { return std::max(1L, (1L << 30) / std::max(1L, n * nacc * 8)); }
+
+int scratch_alloc(void **p, size_t bytes, cudaStream_t s)
+{
+    DeviceInfo *di = nullptr;
+    if (int rc = device_info(di)) return rc;
+    cudaError_t e = cudaMallocFromPoolAsync(p, std::max<size_t>(bytes, 16), di->pool, s);
+    if (e != cudaSuccess) return fail(3, std::string("device scratch allocation failed: ") + err_str(e));
+    return 0;
+}
+
+void scratch_free(void *p, cudaStream_t s)
+{
+    if (p) cudaFreeAsync(p, s);
+}
+
+int scratch_used(unsigned long long *bytes)
+{
+    *bytes = 0;
+    int dev = 0;
+    PO_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(2, "device ordinal out of range");
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (g_dev[dev].ready) pool = g_dev[dev].pool;
+    }
+    if (!pool) return 0;
+    uint64_t used = 0;
+    PO_CK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+    *bytes = used;
+    return 0;
+}
+
 template <typename T>
 static int salloc(T **p, size_t count, cudaStream_t s, std::vector<void *> &owned)
 {
     void *q = nullptr;
-    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
-    cudaError_t e = cudaMallocAsync(&q, bytes, s);
-    if (e != cudaSuccess) return fail(3, std::string("device scratch allocation failed: ") + err_str(e));
+    if (int rc = scratch_alloc(&q, count * sizeof(T), s)) return rc;
     owned.push_back(q);
     *p = static_cast<T *>(q);
     return 0;
@@ -160,7 +195,7 @@ static int salloc(T **p, size_t count, cudaStream_t s, std::vector<void *> &owne
 
 static void sfree(std::vector<void *> &owned, cudaStream_t s)
 {
-    for (void *q : owned) cudaFreeAsync(q, s);
+    for (void *q : owned) scratch_free(q, s);
     owned.clear();
 }
 
@@ -216,26 +251,36 @@ int timing_collect(float *ms, int max)
 }
 
 // Persistent per-device error word, written by kernels that give up a wait.
-static int *error_word()
+static int *g_words[64] = {};
+
+static int *error_word_impl(bool create)
 {
-    static int *words[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!words[dev]) {
-        if (cudaMalloc(&words[dev], sizeof(int)) != cudaSuccess) return nullptr;
-        if (cudaMemset(words[dev], 0, sizeof(int)) != cudaSuccess) return nullptr;
+    if (!g_words[dev] && create) {
+        if (cudaMalloc(&g_words[dev], sizeof(int)) != cudaSuccess) return nullptr;
+        if (cudaMemset(g_words[dev], 0, sizeof(int)) != cudaSuccess) return nullptr;
     }
-    return words[dev];
+    return g_words[dev];
 }
+
+int *error_word() { return error_word_impl(true); }
 
 int read_device_error(cudaStream_t s, int *code)
 {
-    int *w = error_word();
-    if (!w) return fail(2, "no device error word");
-    PO_CK(cudaMemcpyAsync(code, w, sizeof(int), cudaMemcpyDeviceToHost, s));
-    PO_CK(cudaMemsetAsync(w, 0, sizeof(int), s));
+    // Both words: the allocating paths' (if it exists yet) and the
+    // allocation-free entry's (if it has set up on this device). Nothing is
+    // allocated here, so callers of the allocation-free entry can use it.
+    int *w[2] = {error_word_impl(false), static_status_word()};
+    int got[2] = {0, 0};
+    for (int i = 0; i < 2; ++i) {
+        if (!w[i]) continue;
+        PO_CK(cudaMemcpyAsync(&got[i], w[i], sizeof(int), cudaMemcpyDeviceToHost, s));
+        PO_CK(cudaMemsetAsync(w[i], 0, sizeof(int), s));
+    }
     PO_CK(cudaStreamSynchronize(s));
+    *code = got[0] ? got[0] : got[1];
     return 0;
 }
 
@@ -325,7 +370,7 @@ int run_device(const RunArgs &a)
     const size_t src_f4 = (size_t)((std::max(ns, 1L) + 1) / 2) * (scalar ? kRec2Scalar : kRec2);
     const long ntb = (nt + (long)kThreads * pk_tpt(kind) - 1) / ((long)kThreads * pk_tpt(kind));
     const int occ = di->occ2[kind][ts > 0][has_m ? 1 : 0];
-    const long nsplit = choose_split(ntb, ns, (long)di->sms * occ, nt, nacc);
+    const long nsplit = choose_split(ntb, ns, (long)di->sms * occ, partial_cap(nt, nacc), kTile);
     const long tiles = std::max(1L, (ns + kTile - 1) / kTile);
     long chunk = ((tiles + nsplit - 1) / nsplit) * kTile;
     if ((rc = salloc(&bbox, (size_t)kBboxBlocks * 6, s, owned)) || (rc = salloc(&frame, 1, s, owned)) ||
@@ -517,7 +562,7 @@ int run_adjoint(const AdjArgs &a)
     }
     const long tile_t = 2L * adj_pk_pairs_per_tile();
     const long nsb = (ns + kThreadsA - 1) / kThreadsA;
-    const long split = choose_split(nsb, nt, (long)di->sms * occ2, ns, kAccAdj, tile_t);
+    const long split = choose_split(nsb, nt, (long)di->sms * occ2, partial_cap(ns, kAccAdj), tile_t);
     const long tiles = std::max(1L, (nt + tile_t - 1) / tile_t);
     long chunk = ((tiles + split - 1) / split) * tile_t;
     double *part = nullptr;

@@ -433,8 +433,7 @@ public:
         const size_t parts = sizeof(double) * kFgBlocks * kFgMaxSums;
         const size_t bytes = 5 * (nd + 256) + parts + sizeof(double) * (kFgBlocks + 1) * 3 * kBatch + 8 * 256 +
                              2 * ((size_t)n_ + 256) + (size_t)ncx_ + ncy_ + 256;
-        cudaError_t e = cudaMallocAsync(&sc_.base, bytes, s_);
-        if (e != cudaSuccess) return fail(3, std::string("fit scratch: ") + cudaGetErrorString(e));
+        if (int rc = po::scratch_alloc(reinterpret_cast<void **>(&sc_.base), bytes, s_)) return rc;
         char *p = static_cast<char *>(sc_.base);
         auto take = [&](size_t b) {
             char *q = p;
@@ -454,7 +453,7 @@ public:
         sc_.ores = reinterpret_cast<double *>(take(sizeof(double) * 3 * kBatch));
         sc_.sel = reinterpret_cast<unsigned char *>(take((size_t)n_));
         sc_.lines = reinterpret_cast<unsigned char *>(take((size_t)ncx_ + ncy_));
-        e = cudaMemsetAsync(sc_.count, 0, sizeof(unsigned), s_);
+        const cudaError_t e = cudaMemsetAsync(sc_.count, 0, sizeof(unsigned), s_);
         if (e != cudaSuccess) return fail(2, std::string("fit scratch: ") + cudaGetErrorString(e));
         return 0;
     }

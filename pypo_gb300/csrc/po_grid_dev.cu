@@ -199,8 +199,7 @@ int generate_grid_dev(const reflparams &r, double *out7, bool transform, bool sp
             dev[i] = dist(gen);
         }
         double *d = nullptr;
-        e = cudaMallocAsync(&d, sizeof(double) * n, s);
-        if (e != cudaSuccess) return fail(3, std::string("surface-error scratch: ") + cudaGetErrorString(e));
+        if (int rc = po::scratch_alloc(reinterpret_cast<void **>(&d), sizeof(double) * n, s)) return rc;
         e = cudaMemcpyAsync(d, dev.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) {
             po_grid_error_kernel<<<nblk, 256, 0, s>>>(n, d, out7);

@@ -55,8 +55,28 @@ int last_launches();
 int timing_enable(int slots);
 int timing_collect(float *ms, int max);
 
-// Synchronises `s`, returns and clears the device error word (wait timeouts).
+// Synchronises `s`, returns and clears the device error words (wait
+// timeouts): the allocating paths' word and, once the allocation-free entry
+// has set up on this device, its static status word. Allocates nothing.
 int read_device_error(cudaStream_t s, int *code);
+// The allocating paths' error word of the current device (allocated once).
+int *error_word();
+// The allocation-free entry's status word on the current device, or null
+// before its first call there (po_noalloc.cu).
+int *static_status_word();
+
+// Stream-ordered scratch from the library's own memory pool (one per device,
+// created on first use; the device's default pool is left as it is).
+int scratch_alloc(void **p, size_t bytes, cudaStream_t s);
+void scratch_free(void *p, cudaStream_t s);
+// Bytes of the library's pool on the current device in use by scratch that
+// has not been freed (0 before the pool exists).
+int scratch_used(unsigned long long *bytes);
+
+// Number of chunks of a streamed axis (ns items in tiles of `tile`) for a
+// grid of `nb` owning blocks on `slots` resident CTAs: minimises waves times
+// chunk length, with a small cost per extra chunk; at most max_chunks.
+long choose_split(long nb, long ns, long slots, long max_chunks, long tile);
 
 // FP64 grid generation on the device into a 7-row layout (po_grid_dev.cu).
 int generate_grid_dev(const reflparams &r, double *out7, bool transform, bool spheric, cudaStream_t s);

@@ -418,6 +418,24 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
     }
 }
 
+// ------------------------------------------------ failure-detection self-test
+
+// One CTA waits, with the kernels' bounded wait and `limit` polls, on an
+// mbarrier that nothing arrives on and no copy completes on. The wait runs
+// out, and the CTA leaves as the main kernels do: a block-wide vote, then
+// the timeout code in the error word. Nothing is in flight when it leaves.
+__global__ void po_wait_selftest_kernel(uint32_t limit, int *__restrict__ err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0u, limit);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(err, kErrWaitTimeout);
+}
+
 // ----------------------------------------------------------- frame & packing
 
 __global__ void po_bbox_kernel(const double *__restrict__ a, long na, const double *__restrict__ b, long nb,
@@ -966,5 +984,6 @@ void *pack_tgt_kernel() { return reinterpret_cast<void *>(&po_pack_tgt_kernel); 
 void *pack_src_d_kernel() { return reinterpret_cast<void *>(&po_pack_src_d_kernel); }
 void *epilogue_kernel() { return reinterpret_cast<void *>(&po_epilogue_kernel); }
 void *fp32_probe_kernel() { return reinterpret_cast<void *>(&po_fp32_probe_kernel); }
+void *wait_selftest_kernel() { return reinterpret_cast<void *>(&po_wait_selftest_kernel); }
 
 }  // namespace po

@@ -112,6 +112,7 @@ void *pack_tgt_kernel();
 void *pack_src_d_kernel();
 void *epilogue_kernel();
 void *fp32_probe_kernel();
+void *wait_selftest_kernel();
 void *adj_src_fp64_kernel(int kind, int t_sign);
 void *adj_tgt_fp64_kernel(int t_sign);
 void *adj_cot_kernel();

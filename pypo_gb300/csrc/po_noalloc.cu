@@ -14,6 +14,9 @@
 //   * the first call on a device looks up the array's device address and the
 //     kernels' occupancy (the set-up below); make that first call before any
 //     stream capture;
+//   * a kernel that gives up a bounded wait sets the caller's status word,
+//     or (status == NULL) the array's own word, which po_device_error reads
+//     and clears;
 //   * every call shares the one array per device and leaves its contents for
 //     the next; calls that overlap on the GPU (different streams, or threads)
 //     race on it and must be serialised by the caller;
@@ -42,7 +45,7 @@ constexpr size_t kAlign = 256;
 inline size_t up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 // Offsets inside the array.
-constexpr size_t kOffStatus = 0;                       // int, cleared every call
+constexpr size_t kOffStatus = 0;                       // int: timeouts of calls with status == NULL
 constexpr size_t kOffFrame = 256;                      // po::Frame
 constexpr size_t kOffBbox = 512;                       // kBboxBlocks * 6 doubles
 static_assert(sizeof(po::Frame) <= kOffBbox - kOffFrame, "the frame must fit its slot");
@@ -102,27 +105,6 @@ size_t need_bytes(long ns, long nt, int rec2, int nacc, long chunks)
            up((size_t)chunks * nacc * nt * sizeof(double));
 }
 
-// Chunk count as the allocating path chooses it, but also capped so that the
-// partials fit in the static array.
-long choose_chunks(long ntb, long ns, long slots, long max_chunks)
-{
-    const long tiles = std::max(1L, (ns + po::kTile - 1) / po::kTile);
-    long best = 1;
-    double best_cost = 1e300;
-    for (long s = 1; s <= std::min(tiles, std::min(max_chunks, 1024L)); ++s) {
-        const long chunk = (tiles + s - 1) / s;
-        const long real = (tiles + chunk - 1) / chunk;
-        if (real != s) continue;
-        const long waves = (ntb * real + slots - 1) / slots;
-        const double cost = (double)waves * chunk + 0.05 * real;
-        if (cost < best_cost - 1e-9) {
-            best_cost = cost;
-            best = real;
-        }
-    }
-    return best;
-}
-
 int launch(void *fn, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t s)
 {
     if (grid.x == 0 || grid.y == 0) return 0;
@@ -133,6 +115,16 @@ int launch(void *fn, dim3 grid, dim3 block, void **args, size_t smem, cudaStream
 }
 
 }  // namespace
+
+// The internal status word of the current device, or null before the entry's
+// first call there. Read and cleared by po::read_device_error.
+int *po::static_status_word()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_setup[dev].ready ? reinterpret_cast<int *>(g_setup[dev].base + kOffStatus) : nullptr;
+}
 
 extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
                                  const double *cur, long nt, const double *tgt7, double k, double epsilon,
@@ -167,9 +159,14 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
     StaticSetup *st = nullptr;
     if (int rc = setup(st)) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // The caller's status word starts every call at zero. The internal word
+    // (status == NULL) keeps a timeout until po_device_error reads and clears
+    // it, so a later call cannot hide it.
     int *err = status ? status : reinterpret_cast<int *>(st->base + kOffStatus);
-    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
-    if (e != cudaSuccess) return fail(2, std::string("clearing the status word: ") + cudaGetErrorString(e));
+    if (status) {
+        cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
+        if (e != cudaSuccess) return fail(2, std::string("clearing the status word: ") + cudaGetErrorString(e));
+    }
     if (nt == 0) return 0;
 
     const int ts = t_direction > 0 ? 1 : -1;
@@ -177,7 +174,9 @@ extern "C" int po_run_dev_static(int mode, long ns, const double *src7, int gmod
     const long ntb = (nt + (long)po::kThreads * po::pk_tpt(kind) - 1) / ((long)po::kThreads * po::pk_tpt(kind));
     const size_t part_room = kStaticScratchBytes - (need_bytes(ns, nt, rec2, nacc, 0));
     const long max_chunks = std::max(1L, (long)(part_room / ((size_t)nacc * nt * sizeof(double))));
-    const long nsplit = choose_chunks(ntb, ns, (long)st->sms * st->occ[kind][ts > 0][has_m ? 1 : 0], max_chunks);
+    // the allocating path's chunk choice, capped so that the partials fit the array
+    const long nsplit = po::choose_split(ntb, ns, (long)st->sms * st->occ[kind][ts > 0][has_m ? 1 : 0], max_chunks,
+                                         po::kTile);
     const long tiles = std::max(1L, (ns + po::kTile - 1) / po::kTile);
     long chunk = ((tiles + nsplit - 1) / nsplit) * po::kTile;
 

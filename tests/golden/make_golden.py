@@ -10,13 +10,17 @@ script. Needs the reference sources (this container); the fixtures then
 travel without them.
 
 Usage: python tests/golden/make_golden.py [--only-calcjm | --only-eff | --only-fitgauss | --only-converge]
+The reference checkout is read from $PYPO_REFERENCE (default /root/reference).
 """
 import json
+import os
 import pathlib
 import subprocess
 import sys
 
 import numpy as np
+
+REFERENCE = pathlib.Path(os.environ.get("PYPO_REFERENCE", "/root/reference"))
 
 HERE = pathlib.Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
@@ -68,7 +72,7 @@ def efficiencies(ref):
     """The reference's own Efficiencies.py (calcSpillover, calcTaper,
     calcXpol, calcMainBeam) on a seeded aperture field, with its grid binding
     served by the reference's compiled generateGrid."""
-    sys.path.insert(0, "/root/reference/src")
+    sys.path.insert(0, str(REFERENCE / "src"))
     import PyPO.Efficiencies as E
     from PyPO.Enums import AperShapes
 
@@ -117,7 +121,7 @@ def fitgauss(ref):
     with a ratio (the reference's ratio loop never ends)."""
     import signal
     from scipy.special import j1
-    sys.path.insert(0, "/root/reference/src")
+    sys.path.insert(0, str(REFERENCE / "src"))
     import PyPO.Efficiencies as E
     import PyPO.FitGauss as FG
     from PyPO.Enums import Scales
@@ -226,7 +230,7 @@ def converge(ref):
               "matplotlib.patches", "matplotlib.collections", "mpl_toolkits", "mpl_toolkits.axes_grid1",
               "mpl_toolkits.mplot3d"):
         sys.modules.setdefault(m, mock.MagicMock())
-    sys.path.insert(0, "/root/reference/src")
+    sys.path.insert(0, str(REFERENCE / "src"))
     import PyPO.BindBeam as BBeam
     import PyPO.BindCPU as BCPU
     import PyPO.BindRefl as BRefl
