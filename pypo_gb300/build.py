@@ -15,7 +15,7 @@ INCLUDE = HERE.parent / "include"
 LIB = HERE / "libpo_gb300.so"
 BUILD = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["po_kernels.cu", "po_adjoint.cu", "po_adjoint_pk.cu", "po_engine.cu", "po_capi.cu", "po_grid.cpp", "po_grid_dev.cu", "po_sources_dev.cu", "po_eff_dev.cu", "po_noalloc.cu", "po_fmin.cpp", "po_fitgauss_dev.cu"]
+SOURCES = ["po_kernels.cu", "po_farfield.cu", "po_adjoint.cu", "po_adjoint_pk.cu", "po_engine.cu", "po_capi.cu", "po_grid.cpp", "po_grid_dev.cu", "po_sources_dev.cu", "po_eff_dev.cu", "po_noalloc.cu", "po_fmin.cpp", "po_fitgauss_dev.cu"]
 
 
 def nvcc():

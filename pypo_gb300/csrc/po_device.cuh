@@ -180,4 +180,26 @@ __device__ __forceinline__ void phase_sincos2(float2 S0, float2 S1, float2 Rh, f
     sincos_reduced2(fma2(res, rinv0, fma2(Rh, two, neg2(sub2(t, magic)))), sn, cs);
 }
 
+// Trapezoid weight of grid point i (row-major over x/u, y/v): 1/2 on the
+// x/u end rows, and on the y/v end columns unless the grid is uv (periodic in
+// v); 1 for a point cloud (gmode < 0). Reference src/CPU/Propagation.h:
+// the x/u end rows always, the y/v end columns for gmode != 1.
+__device__ __forceinline__ double trap_weight(long i, int gmode, int ncx, int ncy)
+{
+    if (gmode < 0) return 1.0;
+    const long xu = i / ncy, yv = i - xu * ncy;
+    double w = (xu == 0 || xu == ncx - 1) ? 0.5 : 1.0;
+    if (gmode != 1 && (yv == 0 || yv == ncy - 1)) w *= 0.5;
+    return w;
+}
+
+// A coordinate x (turns, relative to the frame origin) as hi + lo: hi on the
+// frame's quantum q (at most 11 significant bits), lo the small rest.
+__device__ __forceinline__ void split_hi_lo(double x, const Frame &fr, float &h, float &l)
+{
+    const double hd = rint(x * fr.inv_q) * fr.q;
+    h = (float)hd;
+    l = (float)(x - hd);
+}
+
 }  // namespace po

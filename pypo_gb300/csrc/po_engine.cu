@@ -33,6 +33,7 @@ struct DeviceInfo {
     int sms = 0;
     cudaMemPool_t pool = nullptr;   // the library's own scratch pool
     int occ2[3][2][2] = {};  // pair-packed kernels, [kind][t>0][has_m]
+    int occ_ff[2][2] = {};   // far-field tile kernels, [t>0][has_m]
     std::map<void *, int> occ_adj;   // adjoint kernels: resident CTAs, attribute set
 };
 
@@ -99,23 +100,10 @@ static int device_info(DeviceInfo *&out)
     DeviceInfo &di = g_dev[dev];
     if (!di.ready) {
         PO_CK(cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev));
-        // Scratch comes from a stream-ordered pool of the library's own, so
-        // the device's default pool (shared with every other user in the
-        // process) keeps its settings. A pool hands freed memory back to the
-        // driver at every synchronisation unless told otherwise, so each
-        // host-buffer call (which synchronises) would map its scratch afresh;
-        // this one keeps up to kPoolKeep bytes of freed scratch.
-        cudaMemPoolProps props = {};
-        props.allocType = cudaMemAllocationTypePinned;
-        props.location.type = cudaMemLocationTypeDevice;
-        props.location.id = dev;
-        PO_CK(cudaMemPoolCreate(&di.pool, &props));
-        uint64_t keep = kPoolKeep;
-        PO_CK(cudaMemPoolSetAttribute(di.pool, cudaMemPoolAttrReleaseThreshold, &keep));
         for (int kind = 0; kind < 3; ++kind)
             for (int ts = 0; ts < 2; ++ts)
                 for (int hm = 0; hm < 2; ++hm) {
-                    if (kind == kKindScalar && hm) continue;
+                    if (kind == kKindFF || (kind == kKindScalar && hm)) continue;   // FF: occ_ff below
                     void *fn = pk_kernel(kind, ts ? 1 : -1, hm != 0);
                     const int smem = pk_smem_bytes(kind);
                     PO_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -123,6 +111,15 @@ static int device_info(DeviceInfo *&out)
                     PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
                     di.occ2[kind][ts][hm] = std::max(nb, 1);
                 }
+        for (int ts = 0; ts < 2; ++ts)
+            for (int hm = 0; hm < 2; ++hm) {
+                void *fn = ff_kernel(ts ? 1 : -1, hm != 0);
+                const int smem = ff_smem_bytes(hm != 0);
+                PO_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+                int nb = 0;
+                PO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
+                di.occ_ff[ts][hm] = std::max(nb, 1);
+            }
         di.ready = true;
     }
     out = &di;
@@ -155,7 +152,32 @@ int scratch_alloc(void **p, size_t bytes, cudaStream_t s)
 {
     DeviceInfo *di = nullptr;
     if (int rc = device_info(di)) return rc;
-    cudaError_t e = cudaMallocFromPoolAsync(p, std::max<size_t>(bytes, 16), di->pool, s);
+    cudaMemPool_t pool = nullptr;
+    {
+        // Scratch comes from a stream-ordered pool of the library's own, made
+        // on first use, so the device's default pool (shared with every
+        // other user in the process) keeps its settings. A pool hands freed
+        // memory back to the driver at every synchronisation unless told
+        // otherwise, so each host-buffer call (which synchronises) would map
+        // its scratch afresh; this one keeps up to kPoolKeep bytes of freed
+        // scratch.
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!di->pool) {
+            int dev = 0;
+            PO_CK(cudaGetDevice(&dev));
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t np = nullptr;
+            PO_CK(cudaMemPoolCreate(&np, &props));
+            uint64_t keep = kPoolKeep;
+            PO_CK(cudaMemPoolSetAttribute(np, cudaMemPoolAttrReleaseThreshold, &keep));
+            di->pool = np;
+        }
+        pool = di->pool;
+    }
+    cudaError_t e = cudaMallocFromPoolAsync(p, std::max<size_t>(bytes, 16), pool, s);
     if (e != cudaSuccess) return fail(3, std::string("device scratch allocation failed: ") + err_str(e));
     return 0;
 }
@@ -174,7 +196,7 @@ int scratch_used(unsigned long long *bytes)
     cudaMemPool_t pool = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (g_dev[dev].ready) pool = g_dev[dev].pool;
+        pool = g_dev[dev].pool;
     }
     if (!pool) return 0;
     uint64_t used = 0;
@@ -198,6 +220,25 @@ static void sfree(std::vector<void *> &owned, cudaStream_t s)
     for (void *q : owned) scratch_free(q, s);
     owned.clear();
 }
+
+// Stream-ordered scratch from the library's pool, freed (in stream order)
+// when the call's work is queued.
+class PoolScratch : public Scratch {
+public:
+    explicit PoolScratch(cudaStream_t s) : s_(s) {}
+    ~PoolScratch() override { sfree(owned_, s_); }
+    int take(void **p, size_t bytes) override
+    {
+        const int rc = scratch_alloc(p, bytes, s_);
+        if (!rc) owned_.push_back(*p);
+        return rc;
+    }
+    size_t room() const override { return ~(size_t)0; }
+
+private:
+    cudaStream_t s_;
+    std::vector<void *> owned_;
+};
 
 static int launch(void *fn, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t s)
 {
@@ -302,120 +343,181 @@ int run_device(const RunArgs &a)
 {
     if (int rc = validate(a)) return rc;
     if (a.nt == 0) return 0;
+    cudaStream_t s = a.stream;
+    if (a.precision == 0) {
+        int *err = error_word();
+        if (!err) return fail(2, "could not allocate the device error word");
+        PoolScratch pool(s);
+        return run_mixed(a, pool, err);
+    }
 
-    DeviceInfo *di = nullptr;
-    if (int rc = device_info(di)) return rc;
-    int *err = error_word();
-    if (!err) return fail(2, "could not allocate the device error word");
-
+    // ---- plain FP64: one thread per target, the comparison path
     const int kind = a.mode == kFF ? kKindFF : (a.mode == kScalar ? kKindScalar : kKindNF);
     const int nacc = kind == kKindScalar ? 2 : kAcc;
     const double pif = (double)3.14159265359f;   // the reference's float-literal pi
     const double pref = a.k * a.k / (4.0 * pif);
-    const double kappa = a.k / (2.0 * 3.14159265358979323846);
     const double c_l = (double)2.99792458e8f, mu0 = (double)1.2566370614e-6f;
     const double eps = a.epsilon * (1.0 / (mu0 * c_l * c_l));
-    const double zeta_inv = 1.0 / std::sqrt(mu0 / eps);
-    const int ts = a.t_dir > 0 ? 1 : -1;
-    cudaStream_t s = a.stream;
-
-    // Complex factor folded into each source's weighted current.
+    double zeta_inv = 1.0 / std::sqrt(mu0 / eps);
+    // complex factor folded into each source's weighted current
     double fac_re = pref, fac_im = 0.0;
     if (kind == kKindFF) { fac_re = 0.0; fac_im = -pref; }
-    if (kind == kKindScalar) {
-        fac_re = -pref * (a.precision == 0 ? kappa : 1.0);
-        fac_im = 0.0;
-    }
-
+    if (kind == kKindScalar) fac_re = -pref;
     std::vector<void *> owned;
     int rc = 0;
     const unsigned nblk_s = (unsigned)((a.ns + 255) / 256), nblk_t = (unsigned)((a.nt + 255) / 256);
     long nt = a.nt, ns = a.ns;
-    int mode = a.mode;
-    double t = a.t_dir;
+    int mode = a.mode, gmode = a.gmode, ncx = a.ncx, ncy = a.ncy;
+    double t = a.t_dir, k = a.k;
     const int scalar = kind == kKindScalar;
     const double *src7 = a.src7, *cur = a.cur, *tgt7 = a.tgt7;
-    int gmode = a.gmode, ncx = a.ncx, ncy = a.ncy;
     double *out = a.out;
-
-    if (a.precision == 1) {
-        double *srcd = nullptr, *part = nullptr;
-        if ((rc = salloc(&srcd, (size_t)std::max(ns, 1L) * kRecD, s, owned)) ||
-            (rc = salloc(&part, (size_t)nacc * nt, s, owned))) {
-            sfree(owned, s);
-            return rc;
-        }
-        void *pargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &fac_re, &fac_im, (void *)&scalar, &srcd};
-        if (ns > 0) rc = launch(pack_src_d_kernel(), dim3(nblk_s), dim3(256), pargs, 0, s);
-        double k = a.k;
-        void *fargs[] = {&srcd, &ns, &tgt7, &nt, &k, &t, &part};
-        timing_mark(s, true);
-        if (!rc) rc = launch(fp64_kernel(kind), dim3((unsigned)((nt + kThreadsD - 1) / kThreadsD)),
-                             dim3(kThreadsD), fargs, 0, s);
-        timing_mark(s, false);
-        int one = 1;
-        double zi = zeta_inv;
-        void *eargs[] = {&mode, &one, &nt, &part, &tgt7, &t, &zi, &out};
-        if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
+    double *srcd = nullptr, *part = nullptr;
+    if ((rc = salloc(&srcd, (size_t)std::max(ns, 1L) * kRecD, s, owned)) ||
+        (rc = salloc(&part, (size_t)nacc * nt, s, owned))) {
         sfree(owned, s);
         return rc;
     }
-
-    // ---- mixed precision: pair-packed kernels (two sources per FP32x2 lane pair)
-    const bool has_m = kind != kKindScalar && !a.m_zero;
-    double *bbox = nullptr;
-    Frame *frame = nullptr;
-    float4 *srcpk = nullptr, *tgtpk = nullptr;
-    double *part = nullptr;
-    const size_t src_f4 = (size_t)((std::max(ns, 1L) + 1) / 2) * (scalar ? kRec2Scalar : kRec2);
-    const long ntb = (nt + (long)kThreads * pk_tpt(kind) - 1) / ((long)kThreads * pk_tpt(kind));
-    const int occ = di->occ2[kind][ts > 0][has_m ? 1 : 0];
-    const long nsplit = choose_split(ntb, ns, (long)di->sms * occ, partial_cap(nt, nacc), kTile);
-    const long tiles = std::max(1L, (ns + kTile - 1) / kTile);
-    long chunk = ((tiles + nsplit - 1) / nsplit) * kTile;
-    if ((rc = salloc(&bbox, (size_t)kBboxBlocks * 6, s, owned)) || (rc = salloc(&frame, 1, s, owned)) ||
-        (rc = salloc(&srcpk, src_f4, s, owned)) || (rc = salloc(&tgtpk, (size_t)nt * 2, s, owned)) ||
-        (rc = salloc(&part, (size_t)nsplit * nacc * nt, s, owned))) {
-        sfree(owned, s);
-        return rc;
-    }
-    // Frame: far field keeps the coordinate origin (it is the phase reference).
-    const bool far = kind == kKindFF;
-    long nb = far ? 0 : nt;   // sources, plus targets for the near field
-    void *bargs[] = {&src7, &ns, &tgt7, &nb, &bbox};
-    rc = launch(bbox_kernel(), dim3(kBboxBlocks), dim3(kBboxThreads), bargs, 0, s);
-    int nbb = kBboxBlocks;
-    double kap = kappa;
-    int centred = far ? 0 : 1;
-    void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
-    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(32), frargs, 0, s);
-    float *srcf = reinterpret_cast<float *>(srcpk);
-    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&scalar, &srcf};
-    const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
-    if (!rc && ns > 0) rc = launch(pack_src2_kernel(), dim3(nblk_p), dim3(256), psargs, 0, s);
-    // tile boxes for the lit-tile proof (the scalar kind has no illumination test)
-    float2 *rec2 = reinterpret_cast<float2 *>(srcpk);
-    void *sbargs[] = {&rec2, &ns};
-    int boxes = !scalar && !has_m && ns > 0;   // the lit-tile proof serves the M = 0 kernels
-    if (!rc && boxes) rc = launch(src_box_kernel(), dim3((unsigned)tiles), dim3(32), sbargs, 0, s);
-    int farflag = far ? 1 : 0;
-    void *ptargs[] = {&nt, &tgt7, &frame, &farflag, &tgtpk};
-    if (!rc) rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
-    const float4 *srcc = srcpk, *tgtc = tgtpk;
-    void *margs[] = {&srcc, &ns, &chunk, &tgtc, &nt, &part, &err, &boxes};
+    void *pargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &fac_re, &fac_im, (void *)&scalar, &srcd};
+    if (ns > 0) rc = launch(pack_src_d_kernel(), dim3(nblk_s), dim3(256), pargs, 0, s);
+    void *fargs[] = {&srcd, &ns, &tgt7, &nt, &k, &t, &part};
     timing_mark(s, true);
-    if (!rc)
-        rc = launch(pk_kernel(kind, ts, has_m), dim3((unsigned)ntb, (unsigned)nsplit), dim3(kThreads), margs,
-                    pk_smem_bytes(kind), s);
+    if (!rc) rc = launch(fp64_kernel(kind), dim3((unsigned)((nt + kThreadsD - 1) / kThreadsD)), dim3(kThreadsD),
+                         fargs, 0, s);
     timing_mark(s, false);
-    int nspl = (int)nsplit;
-    double zi = zeta_inv;
-    void *eargs[] = {&mode, &nspl, &nt, &part, &tgt7, &t, &zi, &out};
+    int one = 1;
+    void *eargs[] = {&mode, &one, &nt, &part, &tgt7, &t, &zeta_inv, &out};
     if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
-    if (!rc && a.extent_host) PO_CK_RC(cudaMemcpyAsync(a.extent_host, &frame->m, sizeof(double),
-                                                       cudaMemcpyDeviceToHost, s));
     sfree(owned, s);
     return rc;
+}
+
+int mixed_prepare(const RunArgs &a, Scratch &sc, MixedPlan &p)
+{
+    DeviceInfo *di = nullptr;
+    if (int rc = device_info(di)) return rc;
+    p.kind = a.mode == kFF ? kKindFF : (a.mode == kScalar ? kKindScalar : kKindNF);
+    p.nacc = p.kind == kKindScalar ? 2 : kAcc;
+    const double pif = (double)3.14159265359f;   // the reference's float-literal pi
+    const double pref = a.k * a.k / (4.0 * pif);
+    p.kappa = a.k / (2.0 * 3.14159265358979323846);
+    const double c_l = (double)2.99792458e8f, mu0 = (double)1.2566370614e-6f;
+    const double eps = a.epsilon * (1.0 / (mu0 * c_l * c_l));
+    p.zeta_inv = 1.0 / std::sqrt(mu0 / eps);
+    p.ts = a.t_dir > 0 ? 1 : -1;
+    // complex factor folded into each source's weighted current
+    p.fac_re = pref;
+    p.fac_im = 0.0;
+    if (p.kind == kKindFF) { p.fac_re = 0.0; p.fac_im = -pref; }
+    if (p.kind == kKindScalar) p.fac_re = -pref * p.kappa;
+    const bool scalar = p.kind == kKindScalar;
+    p.far = p.kind == kKindFF;
+    p.has_m = !scalar && !a.m_zero;
+    const long ns = a.ns, nt = a.nt;
+    p.tiles = std::max(1L, (ns + kTile - 1) / kTile);
+    int rc = 0;
+    if ((rc = sc.get(&p.bbox, (size_t)kBboxBlocks * 6)) || (rc = sc.get(&p.frame, 1)) ||
+        (rc = sc.get(&p.tgtpk, (size_t)nt * 2)))
+        return rc;
+    if (p.far) {
+        // the far field's tiles along the sources' Hilbert order
+        const long n1 = std::max(ns, 1L);
+        cudaError_t e = ff_sort(nullptr, &p.sort_bytes, nullptr, nullptr, nullptr, nullptr, n1, a.stream);
+        if (e != cudaSuccess) return fail(2, std::string("sort size query: ") + err_str(e));
+        if ((rc = sc.get(&p.srcpk, (size_t)p.tiles * ff_tile4(p.has_m))) || (rc = sc.get(&p.keys, 2 * (size_t)n1)) ||
+            (rc = sc.get(&p.order, 2 * (size_t)n1)) || (rc = sc.take(&p.sort_tmp, p.sort_bytes)))
+            return rc;
+    } else {
+        const size_t src_f4 = (size_t)((std::max(ns, 1L) + 1) / 2) * (scalar ? kRec2Scalar : kRec2);
+        if ((rc = sc.get(&p.srcpk, src_f4))) return rc;
+    }
+    // source chunks: balance waves over the SMs; the partials must fit the scratch left
+    const int tpt = p.far ? 2 : pk_tpt(p.kind);   // targets per thread
+    p.ntb = (nt + (long)kThreads * tpt - 1) / ((long)kThreads * tpt);
+    const int occ = p.far ? di->occ_ff[p.ts > 0][p.has_m ? 1 : 0] : di->occ2[p.kind][p.ts > 0][p.has_m ? 1 : 0];
+    const size_t room = std::min(sc.room(), (size_t)1 << 30);
+    const long max_chunks = (long)(room / ((size_t)p.nacc * nt * sizeof(double)));
+    if (max_chunks < 1) return sc.get(&p.part, (size_t)p.nacc * nt);   // fails with the source's message
+    p.nsplit = choose_split(p.ntb, ns, (long)di->sms * occ, max_chunks, kTile);
+    const long chunk_tiles = (p.tiles + p.nsplit - 1) / p.nsplit;
+    p.chunk = chunk_tiles * (p.far ? 1 : kTile);   // tiles (far field) or sources per chunk
+    return sc.get(&p.part, (size_t)p.nsplit * p.nacc * nt);
+}
+
+int mixed_launch(const RunArgs &a, MixedPlan &p, int *err)
+{
+    cudaStream_t s = a.stream;
+    long nt = a.nt, ns = a.ns;
+    int mode = a.mode, gmode = a.gmode, ncx = a.ncx, ncy = a.ncy;
+    double t = a.t_dir;
+    const int scalar = p.kind == kKindScalar;
+    const double *src7 = a.src7, *cur = a.cur, *tgt7 = a.tgt7;
+    double *out = a.out;
+    const unsigned nblk_s = (unsigned)((ns + 255) / 256), nblk_t = (unsigned)((nt + 255) / 256);
+    int rc = 0;
+    // ---- frame: far field keeps the coordinate origin (its phase reference)
+    long nb = p.far ? 0 : nt;   // the box covers the sources, plus the targets in the near field
+    void *bargs[] = {&src7, &ns, &tgt7, &nb, &p.bbox};
+    rc = launch(bbox_kernel(), dim3(kBboxBlocks), dim3(kBboxThreads), bargs, 0, s);
+    int nbb = kBboxBlocks;
+    int centred = p.far ? 0 : 1;
+    void *frargs[] = {&p.bbox, &nbb, &p.kappa, &centred, &p.frame};
+    if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(32), frargs, 0, s);
+    int boxes = !scalar && !p.has_m && ns > 0;   // the lit-tile proof serves the M = 0 kernels
+    if (p.far) {
+        // sources in Hilbert order, packed tile by tile with their centres
+        const long n1 = std::max(ns, 1L);
+        unsigned long long *k_in = p.keys, *k_out = p.keys + n1;
+        int *i_in = p.order, *i_out = p.order + n1;
+        void *kargs[] = {&ns, &src7, &p.frame, &k_in, &i_in};
+        if (!rc && ns > 0) rc = launch(ff_key_kernel(), dim3(nblk_s), dim3(256), kargs, 0, s);
+        if (!rc && ns > 0) {
+            cudaError_t e = ff_sort(p.sort_tmp, &p.sort_bytes, k_in, k_out, i_in, i_out, ns, s);
+            if (e != cudaSuccess) rc = fail(2, std::string("source sort: ") + err_str(e));
+            else note_launches(1);
+        }
+        const int *ord = i_out;
+        void *pargs[] = {&ns, &ord, &src7, &cur, &gmode, &ncx, &ncy, &p.frame, &p.fac_re, &p.fac_im, &p.srcpk};
+        if (!rc && ns > 0) rc = launch(ff_pack_kernel(p.has_m), dim3((unsigned)p.tiles), dim3(32), pargs, 0, s);
+    } else {
+        float *srcf = reinterpret_cast<float *>(p.srcpk);
+        void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &p.frame, &p.fac_re, &p.fac_im, (void *)&scalar, &srcf};
+        const unsigned nblk_p = (unsigned)((2 * ((ns + 1) / 2) + 255) / 256);
+        if (!rc && ns > 0) rc = launch(pack_src2_kernel(), dim3(nblk_p), dim3(256), psargs, 0, s);
+        float2 *rec2 = reinterpret_cast<float2 *>(p.srcpk);
+        void *sbargs[] = {&rec2, &ns};
+        if (!rc && boxes) rc = launch(src_box_kernel(), dim3((unsigned)p.tiles), dim3(32), sbargs, 0, s);
+    }
+    int farflag = p.far ? 1 : 0;
+    void *ptargs[] = {&nt, &tgt7, &p.frame, &farflag, &p.tgtpk};
+    if (!rc) rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
+    const float4 *srcc = p.srcpk, *tgtc = p.tgtpk;
+    long ntiles = ns > 0 ? p.tiles : 0;
+    void *margs[] = {&srcc, p.far ? (void *)&ntiles : (void *)&ns, &p.chunk, &tgtc, &nt, &p.part, &err, &boxes};
+    timing_mark(s, true);
+    if (!rc) {
+        if (p.far)
+            rc = launch(ff_kernel(p.ts, p.has_m), dim3((unsigned)p.ntb, (unsigned)p.nsplit), dim3(kThreads), margs,
+                        ff_smem_bytes(p.has_m), s);
+        else
+            rc = launch(pk_kernel(p.kind, p.ts, p.has_m), dim3((unsigned)p.ntb, (unsigned)p.nsplit), dim3(kThreads),
+                        margs, pk_smem_bytes(p.kind), s);
+    }
+    timing_mark(s, false);
+    int nspl = (int)p.nsplit;
+    void *eargs[] = {&mode, &nspl, &nt, &p.part, &tgt7, &t, &p.zeta_inv, &out};
+    if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
+    if (!rc && a.extent_host) PO_CK_RC(cudaMemcpyAsync(a.extent_host, &p.frame->m, sizeof(double),
+                                                       cudaMemcpyDeviceToHost, s));
+    return rc;
+}
+
+int run_mixed(const RunArgs &a, Scratch &sc, int *err)
+{
+    if (a.nt == 0) return 0;
+    MixedPlan p;
+    if (int rc = mixed_prepare(a, sc, p)) return rc;
+    return mixed_launch(a, p, err);
 }
 
 

@@ -73,6 +73,53 @@ void scratch_free(void *p, cudaStream_t s);
 // has not been freed (0 before the pool exists).
 int scratch_used(unsigned long long *bytes);
 
+// Where one mixed-precision propagation takes its scratch. Every buffer is
+// taken before the first launch, so a source that runs out fails before any
+// device work. take() gives 256-byte aligned memory; room() is what is left.
+class Scratch {
+public:
+    virtual ~Scratch() = default;
+    virtual int take(void **p, size_t bytes) = 0;
+    virtual size_t room() const = 0;
+    template <typename T>
+    int get(T **p, size_t count)
+    {
+        void *q = nullptr;
+        const int rc = take(&q, count * sizeof(T));
+        *p = static_cast<T *>(q);
+        return rc;
+    }
+};
+
+// The mixed-precision forward of run_device on a given scratch source and
+// error word (run_device: the library's pool and error word; the
+// allocation-free entry: its static array and status word). In two steps:
+// mixed_prepare takes every buffer (no device work), mixed_launch queues the
+// kernels on a.stream.
+// Constants, buffers and launch shape of one mixed-precision propagation.
+struct MixedPlan {
+    int kind = 0, nacc = 0, ts = -1;
+    bool far = false, has_m = false;
+    double kappa = 0, fac_re = 0, fac_im = 0, zeta_inv = 0;
+    long tiles = 0, ntb = 0, nsplit = 1, chunk = 0;
+    double *bbox = nullptr, *part = nullptr;
+    Frame *frame = nullptr;
+    float4 *srcpk = nullptr, *tgtpk = nullptr;
+    unsigned long long *keys = nullptr;
+    int *order = nullptr;
+    void *sort_tmp = nullptr;
+    size_t sort_bytes = 0;
+};
+int mixed_prepare(const RunArgs &a, Scratch &sc, MixedPlan &p);
+int mixed_launch(const RunArgs &a, MixedPlan &p, int *err);
+int run_mixed(const RunArgs &a, Scratch &sc, int *err);
+
+// Radix sort of (key, index) pairs for the far field's source order
+// (po_farfield.cu); with temp == nullptr it only sets *temp_bytes, on the
+// host, with no device work.
+cudaError_t ff_sort(void *temp, size_t *temp_bytes, const unsigned long long *key_in, unsigned long long *key_out,
+                    const int *idx_in, int *idx_out, long n, cudaStream_t s);
+
 // Number of chunks of a streamed axis (ns items in tiles of `tile`) for a
 // grid of `nb` owning blocks on `slots` resident CTAs: minimises waves times
 // chunk length, with a small cost per extra chunk; at most max_chunks.

@@ -133,47 +133,6 @@ __device__ __forceinline__ void nf_pair2(float2 *acc, const float2 *th, const fl
     }
 }
 
-// Far field, pair-packed: tc = (rh xyz, rl xyz, r xyz) of the thread's
-// direction (r = rh + rl), r = the pair-packed record (slots 0-2 hi position,
-// 3-5 lo position, 6-8 normal, 9-14 J', 15-20 M').
-template <int T, bool HAS_M, bool LIT>
-__device__ __forceinline__ void ff_pair2(float2 *acc, const float2 *tc, const float2 *r)
-{
-    // r' . r_hat in turns: hi products are exact (hi parts have few bits)
-    const float2 Ph = fma2(r[2], tc[2], fma2(r[1], tc[1], mul2(r[0], tc[0])));
-    const float2 Pl = fma2(r[5], tc[8], fma2(r[4], tc[7], fma2(r[3], tc[6], fma2(r[2], tc[5],
-                      fma2(r[1], tc[4], mul2(r[0], tc[3]))))));
-    float2 sn, cs, tq;
-    ff_phase_sincos2(Ph, Pl, sn, cs, tq);
-    // G = e^{-t j theta}; (-1)^q and the illumination mask in one per-lane
-    // factor, or (lit tile) the sign (-1)^q alone, set on the bits
-    float2 gc, gs;
-    if (LIT) {
-        gc = flip_parity(cs, tq);
-        gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
-    } else {
-        const float2 ndr = fma2(r[8], tc[8], fma2(r[7], tc[7], mul2(r[6], tc[6])));
-        const float2 one = flip_parity(dup2(1.0f), tq);
-        const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
-        gc = mul2(cs, m);
-        gs = mul2(T > 0 ? neg2(sn) : sn, m);
-    }
-    acc[0] = fma2(neg2(gs), r[10], fma2(gc, r[9], acc[0]));
-    acc[3] = fma2(gs, r[9], fma2(gc, r[10], acc[3]));
-    acc[1] = fma2(neg2(gs), r[12], fma2(gc, r[11], acc[1]));
-    acc[4] = fma2(gs, r[11], fma2(gc, r[12], acc[4]));
-    acc[2] = fma2(neg2(gs), r[14], fma2(gc, r[13], acc[2]));
-    acc[5] = fma2(gs, r[13], fma2(gc, r[14], acc[5]));
-    if (HAS_M) {
-        acc[6] = fma2(neg2(gs), r[16], fma2(gc, r[15], acc[6]));
-        acc[9] = fma2(gs, r[15], fma2(gc, r[16], acc[9]));
-        acc[7] = fma2(neg2(gs), r[18], fma2(gc, r[17], acc[7]));
-        acc[10] = fma2(gs, r[17], fma2(gc, r[18], acc[10]));
-        acc[8] = fma2(neg2(gs), r[20], fma2(gc, r[19], acc[8]));
-        acc[11] = fma2(gs, r[19], fma2(gc, r[20], acc[11]));
-    }
-}
-
 // Scalar, pair-packed: acc += S' e^{-t j k r} / r. Record slots: 0-2 hi,
 // 3-5 lo, 6-7 S' (re, im) with prefactor, weights and k/2pi folded in.
 template <int T>
@@ -201,12 +160,11 @@ __device__ __forceinline__ void sc_pair2(float2 *acc, const float2 *tc, const fl
 // hi xyz, a bound on |t|_1). The tile's box (po_src_box_kernel: lowest and
 // highest normal xyz, largest n.s, largest |s|_1) travels with the tile in
 // the unused slot 21 of its first four pair records, so it arrives in
-// shared memory with the tile's copy. Near field: n.(t - s) >= min over the
-// boxes of n.t - max n.s, required above a margin of 1e-5 (|t|_1 + |s|_1)
-// for the FP32 rounding of both sides (the test is n.d + 5e-7 R >= 0). Far
-// field: n.r_hat >= 1e-5 (the test is n.r_hat >= -5e-7). The least of n t
-// over n in [a, b], t in [c, d] is the least of the four corner products.
-template <int KIND, int REC>
+// shared memory with the tile's copy: n.(t - s) >= min over the boxes of
+// n.t - max n.s, required above a margin of 1e-5 (|t|_1 + |s|_1) for the
+// FP32 rounding of both sides (the test is n.d + 5e-7 R >= 0). The least of
+// n t over n in [a, b], t in [c, d] is the least of the four corner products.
+template <int REC>
 __device__ __forceinline__ bool tile_lit(const float4 *tile, const float *tb)
 {
     const float *f = reinterpret_cast<const float *>(tile);
@@ -219,18 +177,17 @@ __device__ __forceinline__ bool tile_lit(const float4 *tile, const float *tb)
         const float a = bx[c], b = bx[3 + c];
         L += fminf(fminf(a * tb[c], a * tb[3 + c]), fminf(b * tb[c], b * tb[3 + c]));
     }
-    if (KIND == kKindFF) return L >= 1e-5f;
     return L - bx[6] >= 1e-5f * (tb[6] + bx[7]);
 }
 
 // Pair-packed main kernel of all three kinds. Grid = (target blocks, source
 // chunks): blockIdx.y picks a chunk of sources (a multiple of kTile, so
 // chunks start on a pair boundary), whose tiles of kTile/2 pair records
-// stream through kStages TMA stages. The thread's target is duplicated into
-// both lanes once: near field and scalar (hi xyz, lo xyz), far field
-// (r_hat hi xyz, lo xyz, full xyz). With `boxes` (po_src_box_kernel has run
-// on the records), a tile proven lit for the CTA skips the per-pair
-// illumination test (M = 0 kernels).
+// stream through kStages TMA stages. The thread's target (hi xyz, lo xyz)
+// is duplicated into both lanes once. With `boxes` (po_src_box_kernel has
+// run on the records), a near-field tile proven lit for the CTA skips the
+// per-pair illumination test (M = 0 kernels). The far field has its own
+// kernel (po_farfield.cu).
 template <int KIND, int T, bool HAS_M, int TP>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
 po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt, long nt,
@@ -248,7 +205,7 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
 #pragma unroll
     for (int j = 0; j < TP; ++j) {
         const long ti = tbase + (long)j * kThreads;
-        float4 a = make_float4(0.f, 0.f, KIND == kKindFF ? 0.f : 1.0f, 0.f);   // idle lanes: R > 0
+        float4 a = make_float4(0.f, 0.f, 1.0f, 0.f);   // idle lanes: R > 0
         float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
         if (ti < nt) {
             a = tgt[2 * ti];
@@ -281,7 +238,7 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
             if (tbase + (long)j * kThreads >= nt) continue;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const float x = KIND == kKindFF ? tc[j][6 + c].x : tc[j][c].x + tc[j][3 + c].x;
+                const float x = tc[j][c].x + tc[j][3 + c].x;
                 v[c] = fminf(v[c], x);
                 v[3 + c] = fmaxf(v[3 + c], x);
             }
@@ -372,7 +329,6 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
 #pragma unroll
                 for (int j = 0; j < TP; ++j) {
                     if (KIND == kKindNF) nf_pair2<T, HAS_M, LIT>(acc[j], tc[j], tc[j] + 3, rec);
-                    else if (KIND == kKindFF) ff_pair2<T, HAS_M, LIT>(acc[j], tc[j], rec);
                     else sc_pair2<T>(acc[j], tc[j], rec);
                 }
             }
@@ -380,7 +336,7 @@ po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *
         // block-uniform: every thread reads the same tile box and target box
         // (a tile of fewer than 4 pair records carries no box)
         if constexpr (kLitPath) {
-            if (boxes && cnt >= 4 && tile_lit<KIND, REC>(tile, tbox))
+            if (boxes && cnt >= 4 && tile_lit<REC>(tile, tbox))
                 pairs(std::true_type{});
             else
                 pairs(std::false_type{});
@@ -502,22 +458,10 @@ __global__ void po_frame_kernel(const double *__restrict__ partial, int nblk, do
     fr->q = q;
     fr->inv_q = 1.0 / q;
     fr->m = m;
-}
-
-__device__ __forceinline__ double trap_weight(long i, int gmode, int ncx, int ncy)
-{
-    if (gmode < 0) return 1.0;
-    const long xu = i / ncy, yv = i - xu * ncy;
-    double w = (xu == 0 || xu == ncx - 1) ? 0.5 : 1.0;
-    if (gmode != 1 && (yv == 0 || yv == ncy - 1)) w *= 0.5;
-    return w;
-}
-
-__device__ __forceinline__ void split_hi_lo(double x, const Frame &fr, float &h, float &l)
-{
-    const double hd = rint(x * fr.inv_q) * fr.q;
-    h = (float)hd;
-    l = (float)(x - hd);
+    for (int c = 0; c < 3; ++c) {
+        fr->lo[c] = lo[c];
+        fr->hi[c] = hi[c];
+    }
 }
 
 // One-source records for the adjoint kernels (a thread owns one source),
@@ -967,10 +911,6 @@ void *pk_kernel(int kind, int t_sign, bool has_m)
     if (kind == kKindNF) {
         if (t_sign < 0) return has_m ? pk_ptr<kKindNF, -1, true>() : pk_ptr<kKindNF, -1, false>();
         return has_m ? pk_ptr<kKindNF, 1, true>() : pk_ptr<kKindNF, 1, false>();
-    }
-    if (kind == kKindFF) {
-        if (t_sign < 0) return has_m ? pk_ptr<kKindFF, -1, true>() : pk_ptr<kKindFF, -1, false>();
-        return has_m ? pk_ptr<kKindFF, 1, true>() : pk_ptr<kKindFF, 1, false>();
     }
     return t_sign < 0 ? pk_ptr<kKindScalar, -1, false>() : pk_ptr<kKindScalar, 1, false>();
 }

@@ -40,11 +40,10 @@ constexpr int kBoxF = 8;        // floats per source-tile box (lit-tile proof)
 #ifndef PO_MUFU_SINCOS
 #define PO_MUFU_SINCOS 1         // 0: the polynomial sin/cos (accuracy comparisons)
 #endif
-// Targets per thread of the pair-packed kernel: two directions for the far
-// field (its pair has few FP32 operations per record load, so sharing each
-// load between two targets pays: -2.8 % on the dish_ff forward), one target
-// elsewhere (a second one costs the near field 0.9 %: 162 registers).
-__host__ __device__ constexpr int pk_tpt(int kind) { return kind == kKindFF ? 2 : 1; }
+// Targets per thread of the pair-packed kernel (near field, scalar): one; a
+// second costs the near field 0.9 % (162 registers). The far-field kernel
+// (po_farfield.cu) takes two directions per thread.
+__host__ __device__ constexpr int pk_tpt(int) { return 1; }
 constexpr uint32_t kWaitLimit = 1u << 24;   // bounded mbarrier polls
 
 // Adjoint kernels: one source (or target) per thread; 12 current
@@ -92,7 +91,19 @@ struct Frame {
     double q;
     double inv_q;
     double m;   // half-extent in wavelengths (turns), which sets q and the precision
+    double lo[3], hi[3];   // the points' box (mm), from which the far field orders its sources
 };
+
+// Far-field forward (po_farfield.cu): sources in tiles of kTile along a
+// Hilbert curve, each tile a 64-byte header and kTile / 2 pair records of
+// ff_rec4 float4 (offset from the tile centre, J', normal, M').
+constexpr int kFFHead = 4;
+__host__ __device__ constexpr int ff_rec4(bool has_m) { return has_m ? 9 : 6; }
+__host__ __device__ constexpr int ff_tile4(bool has_m) { return kFFHead + (kTile / 2) * ff_rec4(has_m); }
+int ff_smem_bytes(bool has_m);
+void *ff_key_kernel();
+void *ff_pack_kernel(bool has_m);
+void *ff_kernel(int t_sign, bool has_m);
 
 // Pair-packed main kernel: stages plus the compensation words.
 inline int pk_smem_bytes(int kind)
