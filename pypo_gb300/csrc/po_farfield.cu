@@ -18,12 +18,19 @@
 //     (ff_phase_sincos2, the two directions of a thread in the two lanes),
 //     the tile's sums rotated by e^{-t j k r.c} and folded into float-float
 //     totals (two-sum).
+// FP32 holds p to about 2^-24 of the tile's radius, so a tile wider than
+// kFFNarrow turns (a sparsely sampled surface) splits its offsets instead:
+// hi parts on a power-of-two quantum with at most 11 significant bits (their
+// products with the directions' hi parts, on 2^-11, are exact) and small lo
+// parts, and reduces p as the tile phase is reduced; the choice is per tile
+// and block-uniform.
 // Each tile is one record block: a 64-byte header (centre hi xyz, lo xyz on
-// the frame's quantum; the tile's box of normals for the lit-tile proof)
-// followed by 64 pair records (float2 slots: offset xyz, J' re xyz, J' im
-// xyz, normal xyz, then M' re xyz, im xyz). The main kernel streams tiles
-// through shared memory with 1-D TMA bulk copies on mbarriers, 3 stages deep,
-// with the bounded waits of the other kernels.
+// the frame's quantum; the tile's box of normals for the lit-tile proof; the
+// wide-tile flag) followed by 64 pair records (float2 slots: offset (or its
+// hi part) xyz, J' re xyz, J' im xyz, normal xyz, the offset's lo part xyz
+// (wide tiles), a spare slot, then M' re xyz, im xyz). The main kernel
+// streams tiles through shared memory with 1-D TMA bulk copies on
+// mbarriers, 3 stages deep, with the bounded waits of the other kernels.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -142,9 +149,18 @@ po_ff_pack_kernel(long ns, const int *__restrict__ order, const double *__restri
             nlo[c] = fminf(nlo[c], __shfl_xor_sync(0xffffffffu, nlo[c], o));
             nhi[c] = fmaxf(nhi[c], __shfl_xor_sync(0xffffffffu, nhi[c], o));
         }
-    double cen[3];
+    double cen[3], half[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) cen[c] = 0.5 * (lo[c] + hi[c]);
+    for (int c = 0; c < 3; ++c) {
+        cen[c] = 0.5 * (lo[c] + hi[c]);
+        half[c] = 0.5 * (hi[c] - lo[c]);
+    }
+    // narrow: the box's half-diagonal within kFFNarrow turns; a wide tile's
+    // offsets split on the smallest power of two q with max |offset| <= 1024 q
+    const bool wide = !(sqrt(half[0] * half[0] + half[1] * half[1] + half[2] * half[2]) <= (double)kFFNarrow);
+    const double hmax = fmax(half[0], fmax(half[1], half[2]));
+    double qt = 0x1p-40;
+    for (int g = 0; g < 1100 && wide && qt * 1024.0 < hmax; ++g) qt *= 2.0;
     if (lane < 3) {
         float h, l;
         split_hi_lo(cen[lane], fr, h, l);
@@ -153,7 +169,7 @@ po_ff_pack_kernel(long ns, const int *__restrict__ order, const double *__restri
         bf[6 + lane] = nlo[lane];
         bf[9 + lane] = nhi[lane];
     } else if (lane < 7) {
-        bf[9 + lane] = 0.0f;   // floats 12-15
+        bf[9 + lane] = lane == 3 && wide ? 1.0f : 0.0f;   // float 12: the wide-tile flag; 13-15 spare
     }
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
@@ -164,17 +180,21 @@ po_ff_pack_kernel(long ns, const int *__restrict__ order, const double *__restri
         const double fr_ = fac_re * w, fi_ = fac_im * w;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            rec[2 * c] = (float)(p[q][c] - cen[c]);
+            const double off = p[q][c] - cen[c];
+            const double oh = wide ? rint(off / qt) * qt : off;
+            rec[2 * c] = (float)oh;
+            rec[2 * (12 + c)] = (float)(off - oh);   // 0 in a narrow tile
             const double jr = cur[c * ns + k], ji = cur[(3 + c) * ns + k];
             rec[2 * (3 + c)] = (float)(fr_ * jr - fi_ * ji);
             rec[2 * (6 + c)] = (float)(fr_ * ji + fi_ * jr);
             rec[2 * (9 + c)] = (float)src7[(3 + c) * ns + k];
             if (HAS_M) {
                 const double mr = cur[(6 + c) * ns + k], mi = cur[(9 + c) * ns + k];
-                rec[2 * (12 + c)] = (float)(fr_ * mr - fi_ * mi);
-                rec[2 * (15 + c)] = (float)(fr_ * mi + fi_ * mr);
+                rec[2 * (16 + c)] = (float)(fr_ * mr - fi_ * mi);
+                rec[2 * (19 + c)] = (float)(fr_ * mi + fi_ * mr);
             }
         }
+        rec[2 * 15] = 0.0f;
     }
     __syncwarp();
     float4 *dst = out + (size_t)blockIdx.x * T4;
@@ -305,11 +325,13 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
 #pragma unroll
             for (int a = 0; a < NA; ++a) acc[j][a] = make_float2(0.f, 0.f);
 
-        auto pairs = [&](auto lit_c) {
-            constexpr bool LIT = decltype(lit_c)::value;
-            // float4 read per pair record: offsets and J' (and the normal when
-            // the tile is not proven lit, and M')
-            constexpr int NLD = HAS_M ? R4 : (LIT ? 5 : 6);
+        // VAR 0: narrow tile proven lit (M = 0); 1: narrow tile; 2: wide tile
+        auto pairs = [&](auto var_c) {
+            constexpr int VAR = decltype(var_c)::value;
+            // float4 read per pair record: offsets and J' (and the normal
+            // unless the tile is proven lit; the lo offsets in a wide tile;
+            // M')
+            constexpr int NLD = HAS_M ? R4 : (VAR == 0 ? 5 : (VAR == 1 ? 6 : 8));
             const float4 *recs = tile + kFFHead;
 #pragma unroll 2
             for (int s = 0; s < kTile / 2; ++s) {
@@ -322,16 +344,33 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
                 }
 #pragma unroll
                 for (int j = 0; j < TP; ++j) {
-                    // p = r . (s - c) in turns; y = p - rint(p), exact, |y| <= 1/2
-                    const float2 P = fma2(r[2], rf[j][2], fma2(r[1], rf[j][1], mul2(r[0], rf[j][0])));
-                    const float2 y = sub2(P, sub2(add2(P, magic), magic));
-                    const float2 ang = mul2(y, twopi);
-                    float2 sn, cs;
-                    __sincosf(ang.x, &sn.x, &cs.x);
-                    __sincosf(ang.y, &sn.y, &cs.y);
-                    // G = e^{-t j 2 pi p} = cos - t j sin
-                    float2 gc = cs, gs = T > 0 ? neg2(sn) : sn;
-                    if (!LIT) {
+                    float2 gc, gs;
+                    if (VAR < 2) {
+                        // p = r . (s - c) in turns; y = p - rint(p), exact, |y| <= 1/2
+                        const float2 P = fma2(r[2], rf[j][2], fma2(r[1], rf[j][1], mul2(r[0], rf[j][0])));
+                        const float2 y = sub2(P, sub2(add2(P, magic), magic));
+                        const float2 ang = mul2(y, twopi);
+                        float2 sn, cs;
+                        __sincosf(ang.x, &sn.x, &cs.x);
+                        __sincosf(ang.y, &sn.y, &cs.y);
+                        // G = e^{-t j 2 pi p} = cos - t j sin
+                        gc = cs;
+                        gs = T > 0 ? neg2(sn) : sn;
+                    } else {
+                        // p = r_hi . s_hi (exact) + (r . s_lo + r_lo . s_hi), reduced in half turns
+                        const float2 hx = dup2(j == 0 ? rh[0].x : rh[0].y), hy = dup2(j == 0 ? rh[1].x : rh[1].y),
+                                     hz = dup2(j == 0 ? rh[2].x : rh[2].y);
+                        const float2 lx = dup2(j == 0 ? rl[0].x : rl[0].y), ly = dup2(j == 0 ? rl[1].x : rl[1].y),
+                                     lz = dup2(j == 0 ? rl[2].x : rl[2].y);
+                        const float2 Ph = fma2(r[2], hz, fma2(r[1], hy, mul2(r[0], hx)));
+                        const float2 Pl = fma2(r[14], rf[j][2], fma2(r[13], rf[j][1], fma2(r[12], rf[j][0],
+                                          fma2(r[2], lz, fma2(r[1], ly, mul2(r[0], lx))))));
+                        float2 sn, cs, tq;
+                        ff_phase_sincos2(Ph, Pl, sn, cs, tq);
+                        gc = flip_parity(cs, tq);
+                        gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
+                    }
+                    if (VAR != 0) {
                         const float2 ndr = fma2(r[11], rf[j][2], fma2(r[10], rf[j][1], mul2(r[9], rf[j][0])));
                         const float2 m = make_float2(ndr.x >= -kTangentTol32 ? 1.0f : 0.0f,
                                                      ndr.y >= -kTangentTol32 ? 1.0f : 0.0f);
@@ -343,8 +382,8 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
                         acc[j][c] = fma2(neg2(gs), r[6 + c], fma2(gc, r[3 + c], acc[j][c]));
                         acc[j][3 + c] = fma2(gs, r[3 + c], fma2(gc, r[6 + c], acc[j][3 + c]));
                         if (HAS_M) {
-                            acc[j][6 + c] = fma2(neg2(gs), r[15 + c], fma2(gc, r[12 + c], acc[j][6 + c]));
-                            acc[j][9 + c] = fma2(gs, r[12 + c], fma2(gc, r[15 + c], acc[j][9 + c]));
+                            acc[j][6 + c] = fma2(neg2(gs), r[19 + c], fma2(gc, r[16 + c], acc[j][6 + c]));
+                            acc[j][9 + c] = fma2(gs, r[16 + c], fma2(gc, r[19 + c], acc[j][9 + c]));
                         }
                     }
                 }
@@ -364,14 +403,13 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
             }
             lit = L >= 1e-5f;   // block-uniform: every thread reads the same boxes
         }
-        if constexpr (kLitPath) {
-            if (lit)
-                pairs(std::true_type{});
-            else
-                pairs(std::false_type{});
-        } else {
-            pairs(std::false_type{});
-        }
+        // block-uniform as well
+        if (hdr[12] != 0.0f)
+            pairs(std::integral_constant<int, 2>{});
+        else if (kLitPath && lit)
+            pairs(std::integral_constant<int, 0>{});
+        else
+            pairs(std::integral_constant<int, 1>{});
 
         // The tile's phase r . c for both directions (lanes): hi products
         // exact, the rest in one FP32 sum; reduced exactly to half turns.

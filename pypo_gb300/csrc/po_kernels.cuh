@@ -96,9 +96,13 @@ struct Frame {
 
 // Far-field forward (po_farfield.cu): sources in tiles of kTile along a
 // Hilbert curve, each tile a 64-byte header and kTile / 2 pair records of
-// ff_rec4 float4 (offset from the tile centre, J', normal, M').
+// ff_rec4 float4 (offset from the tile centre, J', normal, the offset's lo
+// part in a wide tile, M').
 constexpr int kFFHead = 4;
-__host__ __device__ constexpr int ff_rec4(bool has_m) { return has_m ? 9 : 6; }
+__host__ __device__ constexpr int ff_rec4(bool has_m) { return has_m ? 11 : 8; }
+// Tiles up to this radius (turns) take the per-pair phase in plain FP32;
+// wider ones (sparse sampling) split their offsets into hi + lo.
+constexpr float kFFNarrow = 32.0f;
 __host__ __device__ constexpr int ff_tile4(bool has_m) { return kFFHead + (kTile / 2) * ff_rec4(has_m); }
 int ff_smem_bytes(bool has_m);
 void *ff_key_kernel();

@@ -82,7 +82,7 @@ public:
             return fail(5, "po_run_dev_static: this problem needs more scratch than the " +
                                std::to_string(kStaticScratchBytes) + "-byte static array holds (" +
                                std::to_string(used_ + need) + " bytes by the time it ran out; roughly 88*ns + "
-                               "128*nt near field, 72*ns + 128*nt far field)");
+                               "128*nt near field, 90*ns + 128*nt far field)");
         *p = base_ + kOffScratch + used_;
         used_ += need;
         return 0;
