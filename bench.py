@@ -543,7 +543,7 @@ def run_ours(args):
         peak = max(peak, blocks * 256 * iters * 16 / (p0.elapsed_time(p1) * 1e-3) / 1e12)
     mk = ("EH" if not far else "FF", not m_zero)
     # pair-packed forward and adjoint (near field: the fused adjoint)
-    names = ["forward po_pk_kernel", "adjoint po_adj_pk_kernel"]
+    names = ["forward " + ("po_ff_kernel" if far else "po_pk_kernel"), "adjoint po_adj_pk_kernel"]
     flops = [FWD_FLOPS[mk], ADJ_FLOPS[mk]]
     kernels = []
     for j in range(kernels_per_step):

@@ -165,10 +165,29 @@ int po_generate_grid(reflparams refl, reflcontainer *container, int transform, i
  * of 7 rows x n_cells[0]*n_cells[1] doubles (x, y, z, nx, ny, nz, area), the
  * layout po_run_dev takes, queued on `stream`. The reflparams arrays are host
  * memory, read during the call. With rms > 0 the surface-error deviates are
- * drawn on the host in the reference's sequence (mt19937, Random.h:112-116)
- * and the call synchronises `stream`. Replaces the host loops of
+ * drawn on the device in the reference's sequence (mt19937 seeded with
+ * rms_seed, a fresh normal distribution per point, Random.h:112-116,
+ * InterfaceReflector.cpp:852-866). Replaces the host loops of
  * InterfaceReflector.cpp:882-1081 when the grid is only needed on the GPU. */
 int po_generate_grid_dev(reflparams refl, double *out7, int transform, int spheric, void *stream);
+
+/* Correlated surface error (no counterpart in the reference, whose surface
+ * error is uncorrelated, InterfaceReflector.cpp:852-866): a Gaussian random
+ * surface with covariance rms^2 exp(-r^2 / (2 corr_len^2)) over the points'
+ * (x, y), by spectral synthesis
+ *   delta_i = rms sqrt(2 / M) sum_m cos(kx_m x_i + ky_m y_i + ph_m),
+ * M = n_modes, with the modes from the reference's generator (mt19937 seeded
+ * with `seed`, a fresh normal deviate per draw): four deviates g per mode,
+ * (kx, ky) = (g0, g1) / corr_len, ph = atan2(g2, g3). grid7 is a 7-row grid
+ * (x, y, z, nx, ny, nz, area) of n points; delta (n, or NULL) receives the
+ * displacement; with apply != 0 the points also move by it along their
+ * normals. po_correlated_error works on host memory, po_correlated_error_dev
+ * on device memory, queued on `stream`; both give the same numbers to
+ * rounding. */
+int po_correlated_error(long n, double *grid7, double rms, double corr_len, unsigned seed, int n_modes,
+                        double *delta, int apply);
+int po_correlated_error_dev(long n, double *grid7, double rms, double corr_len, unsigned seed, int n_modes,
+                            double *delta, int apply, void *stream);
 
 /* ---- source producers on the device --------------------------------------
  * po_gauss_beam_dev: the vector Gaussian feed of makeGaussBeam

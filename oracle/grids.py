@@ -286,3 +286,26 @@ def normal_deviates(seed, n, stdev):
             ya, ra = y[ok][:n], r2[ok][:n]
             return ya * np.sqrt(-2.0 * np.log(ra) / ra) * stdev
         words *= 2
+
+
+# -------------------------------------------------- correlated surface error
+
+def correlated_error(x, y, rms, corr_len, seed, n_modes=512):
+    """Gaussian-correlated random surface by spectral synthesis, evaluated at
+    the points (x, y): delta = rms sqrt(2 / M) sum_m cos(kx_m x + ky_m y + ph_m)
+    over M = n_modes modes, whose covariance is rms^2 exp(-r^2 / (2 corr_len^2)).
+    The modes come from the reference's generator (mt19937 seeded with `seed`,
+    a fresh normal deviate per draw, as normal_deviates): four deviates g per
+    mode, kx = g0 / corr_len, ky = g1 / corr_len, ph = atan2(g2, g3) (uniform
+    for independent normals)."""
+    m = int(n_modes)
+    g = normal_deviates(int(seed), 4 * m, 1.0).reshape(m, 4)
+    kx, ky = g[:, 0] / corr_len, g[:, 1] / corr_len
+    ph = np.arctan2(g[:, 2], g[:, 3])
+    x = np.asarray(x, dtype=float)
+    y = np.asarray(y, dtype=float)
+    out = np.zeros(x.shape)
+    for c in range(0, m, 64):   # modes in blocks, points vectorised
+        arg = np.outer(x, kx[c:c + 64]) + np.outer(y, ky[c:c + 64]) + ph[c:c + 64]
+        out += np.cos(arg).sum(axis=1)
+    return rms * np.sqrt(2.0 / m) * out

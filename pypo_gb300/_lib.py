@@ -11,7 +11,8 @@ from . import Structs as S
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "libpo_gb300.so"
 
 #: every symbol declared in include/po_gb300.h
-EXPORTS = ("po_last_error", "po_n_out", "po_last_launches", "po_generate_grid", "po_generate_grid_dev", "po_gauss_beam_dev", "po_calc_jm_dev",
+EXPORTS = ("po_last_error", "po_n_out", "po_last_launches", "po_generate_grid", "po_generate_grid_dev",
+           "po_correlated_error", "po_correlated_error_dev", "po_gauss_beam_dev", "po_calc_jm_dev",
            "po_efficiency_sums_dev", "po_fit_gauss_abs_dev", "po_generate_gauss_dev", "po_fmin", "po_run_d",
            "po_run_dev", "po_run_dev_static", "po_last_extent", "po_adjoint_dev", "po_adjoint_d", "po_device_error", "po_wait_selftest", "po_scratch_in_use", "po_timing_enable", "po_timing_collect", "po_fp32_probe",
            "callKernelf_JM", "callKernelf_EH", "callKernelf_JMEH", "callKernelf_EHP",
@@ -98,6 +99,11 @@ def load():
     lib.po_timing_collect.argtypes = [P(ctypes.c_float), c_int]
     lib.po_fp32_probe.restype = c_int
     lib.po_fp32_probe.argtypes = [c_int, c_int, c_void_p, c_void_p]
+    lib.po_correlated_error.restype = c_int
+    lib.po_correlated_error.argtypes = [c_long, c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_uint, c_int,
+                                        c_void_p, c_int]
+    lib.po_correlated_error_dev.restype = c_int
+    lib.po_correlated_error_dev.argtypes = lib.po_correlated_error.argtypes + [c_void_p]
     lib.po_wait_selftest.restype = c_int
     lib.po_wait_selftest.argtypes = [ctypes.c_uint, c_void_p, c_int, c_void_p]
     lib.po_scratch_in_use.restype = c_int

@@ -97,16 +97,6 @@ def farfield_minus_z(n, half_deg):
     return g
 
 
-def surface_error(x, y, rms, corr_len, seed, n_modes=512):
-    """Seeded Gaussian-correlated random surface (spectral synthesis): covariance
-    rms^2 exp(-r^2 / (2 corr_len^2)), evaluated at (x, y)."""
-    rng = np.random.default_rng(seed)
-    kv = rng.normal(0.0, 1.0 / corr_len, (n_modes, 2))
-    ph = rng.uniform(0.0, 2 * np.pi, n_modes)
-    arg = np.outer(x, kv[:, 0]) + np.outer(y, kv[:, 1]) + ph
-    return rms * np.sqrt(2.0 / n_modes) * np.cos(arg).sum(axis=1)
-
-
 def feed_dish_jm(scale=1.0):
     """Gaussian feed (lambda 3 mm, w0 10 mm, 101x101 plane over +-50 mm) radiating
     onto an f 300 mm, D 300 mm paraboloid (uv 101x101) that faces it. JM."""
@@ -131,8 +121,9 @@ def dish_chain(scale=1.0):
     plane, f7, fcur = feed_plane(lam, 10.0, 50.0, nf)
     dish = dish_facing_feed(400.0, 600.0, nd)
     d7 = engine.generate_grid(dish)
-    # the error is a function of the dish's own aperture coordinates (x, -y after the flip)
-    delta = surface_error(d7[0], d7[1], lam / 40.0, 30.0, seed=4)
+    # the error is a function of the dish's own aperture coordinates (x, -y after the flip):
+    # a Gaussian-correlated surface, rms lambda/40, correlation length 30 mm
+    delta = engine.correlated_error(d7, lam / 40.0, 30.0, seed=4)
     ff7 = farfield_minus_z(nff, 1.0)
     return dict(name="dish_chain", lam=lam, k=2 * np.pi / lam, feed7=f7, feed_cur=fcur, feed_grid=(0, nf, nf),
                 dish7=d7, dish_grid=(1, nd, nd), delta=delta, ff7=ff7,

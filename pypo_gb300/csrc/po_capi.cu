@@ -310,6 +310,23 @@ int po_generate_grid_dev(reflparams refl, double *out7, int transform, int spher
     return po::generate_grid_dev(refl, out7, transform != 0, spheric != 0, static_cast<cudaStream_t>(stream));
 }
 
+int po_correlated_error(long n, double *grid7, double rms, double corr_len, unsigned seed, int n_modes,
+                        double *delta, int apply)
+{
+    po::clear_error();
+    if (po::correlated_error_host(n, grid7, rms, corr_len, seed, n_modes, delta, apply))
+        return fail(1, "po_correlated_error: bad arguments (n >= 0, n_modes >= 1, corr_len > 0, rms >= 0, grid)");
+    return 0;
+}
+
+int po_correlated_error_dev(long n, double *grid7, double rms, double corr_len, unsigned seed, int n_modes,
+                            double *delta, int apply, void *stream)
+{
+    po::clear_error();
+    return po::correlated_error_dev(n, grid7, rms, corr_len, seed, n_modes, delta, apply,
+                                    static_cast<cudaStream_t>(stream));
+}
+
 int po_gauss_beam_dev(long n, const double *grid7, double lam, double w0, double z, double power, int mode,
                       double *fields, double *currents, void *stream)
 {

@@ -11,6 +11,7 @@
 // (polar angle, azimuth) in radians.
 #include <cmath>
 #include <random>
+#include <vector>
 
 #include "../../include/po_gb300.h"
 
@@ -190,19 +191,62 @@ void transform_all(const reflparams &r, reflcontainer *c, int n)
     }
 }
 
+// n deviates N(0, stdev) in the reference's sequence: mt19937 seeded with
+// `seed` and a fresh normal distribution per draw (Random.h:112-116).
+void normal_deviates(unsigned seed, long n, double stdev, double *out)
+{
+    std::mt19937 gen(seed);
+    for (long i = 0; i < n; ++i) {
+        std::normal_distribution<double> dist(0.0, stdev);
+        out[i] = dist(gen);
+    }
+}
+
 void surface_error(const reflparams &r, reflcontainer *c, int n)
 {
-    std::mt19937 gen(r.rms_seed);
+    std::vector<double> d(n);
+    normal_deviates((unsigned)r.rms_seed, n, r.rms, d.data());
     for (int i = 0; i < n; ++i) {
-        std::normal_distribution<double> dist(0.0, r.rms);
-        const double s = dist(gen);
-        c->x[i] += s * c->nx[i];
-        c->y[i] += s * c->ny[i];
-        c->z[i] += s * c->nz[i];
+        c->x[i] += d[i] * c->nx[i];
+        c->y[i] += d[i] * c->ny[i];
+        c->z[i] += d[i] * c->nz[i];
     }
 }
 
 }  // namespace
+
+namespace po {
+
+// Correlated surface error on the host, the twin of correlated_error_dev:
+// delta_i = rms sqrt(2 / M) sum_m cos(kx_m x_i + ky_m y_i + ph_m) over M
+// modes, kx, ky = g0, g1 / corr_len, ph = atan2(g2, g3) from four deviates
+// N(0, 1) per mode in the reference's sequence; covariance
+// rms^2 exp(-r^2 / (2 corr_len^2)). With `apply`, points move along their
+// normals by delta.
+int correlated_error_host(long n, double *g7, double rms, double corr_len, unsigned seed, int n_modes, double *delta,
+                          int apply)
+{
+    if (n < 0 || n_modes < 1 || !(corr_len > 0.0) || !(rms >= 0.0) || (n > 0 && !g7)) return 1;
+    std::vector<double> g(4 * (size_t)n_modes), kx(n_modes), ky(n_modes), ph(n_modes);
+    normal_deviates(seed, 4L * n_modes, 1.0, g.data());
+    for (int m = 0; m < n_modes; ++m) {
+        kx[m] = g[4 * m] * (1.0 / corr_len);
+        ky[m] = g[4 * m + 1] * (1.0 / corr_len);
+        ph[m] = std::atan2(g[4 * m + 2], g[4 * m + 3]);
+    }
+    const double scale = rms * std::sqrt(2.0 / n_modes);
+    for (long i = 0; i < n; ++i) {
+        double sum = 0.0;
+        for (int m = 0; m < n_modes; ++m) sum += std::cos(kx[m] * g7[i] + ky[m] * g7[n + i] + ph[m]);
+        const double d = scale * sum;
+        if (delta) delta[i] = d;
+        if (apply)
+            for (int c = 0; c < 3; ++c) g7[c * n + i] += d * g7[(3 + c) * n + i];
+    }
+    return 0;
+}
+
+}  // namespace po
 
 // Host-side grid generation used by the drop-in entry points; the transform
 // is applied per point after the surface parametrisation, as the reference does.

@@ -6,15 +6,18 @@
 // AoE :645-686, :712-768, :794-849, 4x4 transform :35-57), one thread per grid
 // point, written straight into the 7-row device layout the propagation entry
 // points take (x, y, z, nx, ny, nz, area; index i*ncy + j). The optional
-// surface error (:852-866) keeps the reference's random sequence: mt19937
-// with a fresh normal distribution per point (Random.h:112-116) is
-// sequential, so the deviates are drawn on the host, copied, and applied
-// along the normals by a second kernel.
+// surface error (:852-866) keeps the reference's random sequence, drawn on
+// the device (po_mt_normals_kernel): mt19937 seeded with rms_seed and a fresh
+// normal distribution per point (src/include/Random.h:112-116), applied along
+// the normals by a second kernel.
+//
+// The correlated surface error (po_correlated_error_dev) is a spectral
+// synthesis over random modes drawn from the same generator, evaluated on
+// the device at every grid point.
 #include <cuda_runtime.h>
 
-#include <random>
+#include <cstdint>
 #include <string>
-#include <vector>
 
 #include "po_internal.h"
 
@@ -192,28 +195,211 @@ int generate_grid_dev(const reflparams &r, double *out7, bool transform, bool sp
     if (e != cudaSuccess) return fail(2, std::string("grid kernel launch: ") + cudaGetErrorString(e));
     note_launches(1);
     if (r.rms > 0) {
-        std::vector<double> dev(n);
-        std::mt19937 gen(r.rms_seed);
-        for (long i = 0; i < n; ++i) {
-            std::normal_distribution<double> dist(0.0, r.rms);
-            dev[i] = dist(gen);
-        }
         double *d = nullptr;
-        if (int rc = po::scratch_alloc(reinterpret_cast<void **>(&d), sizeof(double) * n, s)) return rc;
-        e = cudaMemcpyAsync(d, dev.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) {
+        int *err = error_word();
+        if (!err) return fail(2, "could not allocate the device error word");
+        if (int rc = scratch_alloc(reinterpret_cast<void **>(&d), sizeof(double) * n, s)) return rc;
+        int rc = normal_deviates_dev((unsigned)r.rms_seed, n, r.rms, d, err, s);
+        if (!rc) {
             po_grid_error_kernel<<<nblk, 256, 0, s>>>(n, d, out7);
             e = cudaGetLastError();
             if (e == cudaSuccess) note_launches(1);
+            else rc = fail(2, std::string("surface error: ") + cudaGetErrorString(e));
         }
-        cudaError_t e2 = cudaFreeAsync(d, s);
-        // the pageable source of the copy must outlive it
-        cudaError_t e3 = cudaStreamSynchronize(s);
-        if (e != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
-            return fail(2, std::string("surface error: ") +
-                               cudaGetErrorString(e != cudaSuccess ? e : (e2 != cudaSuccess ? e2 : e3)));
+        scratch_free(d, s);
+        return rc;
     }
     return 0;
+}
+
+// ------------------------------------------------- mt19937 normal deviates
+//
+// MT19937 (Matsumoto and Nishimura, 1998) and the reference's draw of one
+// normal deviate per fresh distribution: a double in [0, 1) from two
+// outputs, low word first, (w0 + w1 2^32) 2^-64 (at most the double below 1);
+// Marsaglia's polar method, x, y = 2U - 1 until 0 < r2 = x^2 + y^2 <= 1, then
+// y sqrt(-2 ln r2 / r2) stdev, the other deviate of the pair dropped. So each
+// attempt takes four outputs, and a block of 624 outputs is exactly 156
+// attempts. One CTA: per block, the twist in three phases (each phase reads
+// only words that are old or already final), the tempering (thread t holds
+// output t), the 156 attempts in parallel, and a warp-ballot scan that
+// places the accepted deviates in order.
+
+namespace {
+
+constexpr int kMtN = 624;
+constexpr int kMtThreads = 640;
+
+__device__ __forceinline__ uint32_t mt_twist(uint32_t cur, uint32_t next, uint32_t tap)
+{
+    const uint32_t y = (cur & 0x80000000u) | (next & 0x7fffffffu);
+    return tap ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+}
+
+__device__ __forceinline__ double mt_canonical(uint32_t w0, uint32_t w1)
+{
+    const double u = __dmul_rn(__dadd_rn((double)w0, __dmul_rn((double)w1, 4294967296.0)), 0x1p-64);
+    return u < 1.0 ? u : 1.0 - 0x1p-53;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kMtThreads)
+po_mt_normals_kernel(unsigned seed, long n, double stdev, double *__restrict__ out, int *__restrict__ err)
+{
+    __shared__ uint32_t mt[kMtN];
+    __shared__ int warp_ok[kMtThreads / 32];
+    __shared__ int warp_off[kMtThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) {
+        uint32_t v = seed;
+        mt[0] = v;
+        for (int i = 1; i < kMtN; ++i) {
+            v = 1812433253u * (v ^ (v >> 30)) + (uint32_t)i;
+            mt[i] = v;
+        }
+    }
+    __syncthreads();
+    long count = 0;   // block-uniform
+    // 156 attempts a block accept about 122.5 deviates on average: the bound
+    // is never reached in practice, and ends the loop if it were
+    const long max_blocks = n / 100 + 64;
+    for (long b = 0; b < max_blocks && count < n; ++b) {
+        uint32_t v = 0;
+        if (t < 227) v = mt_twist(mt[t], mt[t + 1], mt[t + 397]);
+        __syncthreads();
+        if (t < 227) mt[t] = v;
+        __syncthreads();
+        if (t >= 227 && t < 454) v = mt_twist(mt[t], mt[t + 1], mt[t - 227]);
+        __syncthreads();
+        if (t >= 227 && t < 454) mt[t] = v;
+        __syncthreads();
+        if (t >= 454 && t < 623) v = mt_twist(mt[t], mt[t + 1], mt[t - 227]);
+        else if (t == 623) v = mt_twist(mt[623], mt[0], mt[396]);
+        __syncthreads();
+        if (t >= 454 && t < kMtN) mt[t] = v;
+        __syncthreads();
+        uint32_t w = 0;
+        if (t < kMtN) {
+            w = mt[t];
+            w ^= w >> 11;
+            w ^= (w << 7) & 0x9d2c5680u;
+            w ^= (w << 15) & 0xefc60000u;
+            w ^= w >> 18;
+        }
+        // attempt a = t / 4 takes the outputs of threads 4a .. 4a + 3 (one warp)
+        const int base = lane & ~3;
+        const uint32_t w0 = __shfl_sync(0xffffffffu, w, base), w1 = __shfl_sync(0xffffffffu, w, base + 1);
+        const uint32_t w2 = __shfl_sync(0xffffffffu, w, base + 2), w3 = __shfl_sync(0xffffffffu, w, base + 3);
+        bool ok = false;
+        double val = 0.0;
+        if ((t & 3) == 0 && t < kMtN) {
+            const double x = __dsub_rn(__dmul_rn(2.0, mt_canonical(w0, w1)), 1.0);
+            const double y = __dsub_rn(__dmul_rn(2.0, mt_canonical(w2, w3)), 1.0);
+            const double r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+            ok = r2 <= 1.0 && r2 != 0.0;
+            if (ok) val = __dmul_rn(__dmul_rn(y, __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log(r2)), r2))), stdev);
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, ok);
+        if (lane == 0) warp_ok[warp] = __popc(ball);
+        __syncthreads();
+        if (t == 0) {
+            int o = 0;
+            for (int q = 0; q < kMtThreads / 32; ++q) {
+                warp_off[q] = o;
+                o += warp_ok[q];
+            }
+        }
+        __syncthreads();
+        if (ok) {
+            const long at = count + warp_off[warp] + __popc(ball & ((1u << lane) - 1u));
+            if (at < n) out[at] = val;
+        }
+        count += warp_off[kMtThreads / 32 - 1] + warp_ok[kMtThreads / 32 - 1];
+        __syncthreads();
+    }
+    if (t == 0 && count < n) atomicExch(err, kErrRngBound);
+}
+
+int normal_deviates_dev(unsigned seed, long n, double stdev, double *out, int *err, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    po_mt_normals_kernel<<<1, kMtThreads, 0, s>>>(seed, n, stdev, out, err);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(2, std::string("normal deviates: ") + cudaGetErrorString(e));
+    note_launches(1);
+    return 0;
+}
+
+// ------------------------------------------------- correlated surface error
+
+// Modes of the synthesis from four standard normal deviates each:
+// (kx, ky) = (g0, g1) / corr_len, phase atan2(g2, g3).
+__global__ void po_modes_kernel(int m, const double *__restrict__ g, double inv_len, double *__restrict__ modes)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    modes[i] = g[4 * i] * inv_len;
+    modes[m + i] = g[4 * i + 1] * inv_len;
+    modes[2 * m + i] = atan2(g[4 * i + 2], g[4 * i + 3]);
+}
+
+// delta_i = scale sum_m cos(kx_m x_i + ky_m y_i + ph_m), modes in order,
+// staged through shared memory 256 at a time; with `apply`, the point also
+// moves by delta_i along its normal.
+__global__ void __launch_bounds__(256)
+po_correlated_kernel(long n, double *__restrict__ g7, int m, const double *__restrict__ modes, double scale,
+                     double *__restrict__ delta, int apply)
+{
+    __shared__ double sk[3][256];
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const double x = i < n ? g7[i] : 0.0, y = i < n ? g7[n + i] : 0.0;
+    double sum = 0.0;
+    for (int c = 0; c < m; c += 256) {
+        const int cnt = min(256, m - c);
+        __syncthreads();
+        if ((int)threadIdx.x < cnt)
+            for (int q = 0; q < 3; ++q) sk[q][threadIdx.x] = modes[q * m + c + threadIdx.x];
+        __syncthreads();
+        for (int j = 0; j < cnt; ++j) sum += cos(sk[0][j] * x + sk[1][j] * y + sk[2][j]);
+    }
+    if (i >= n) return;
+    const double d = scale * sum;
+    if (delta) delta[i] = d;
+    if (apply) {
+        g7[i] += d * g7[3 * n + i];
+        g7[n + i] += d * g7[4 * n + i];
+        g7[2 * n + i] += d * g7[5 * n + i];
+    }
+}
+
+int correlated_error_dev(long n, double *g7, double rms, double corr_len, unsigned seed, int n_modes, double *delta,
+                         int apply, cudaStream_t s)
+{
+    if (n < 0 || n_modes < 1 || !(corr_len > 0.0) || !(rms >= 0.0)) return fail(1, "bad surface-error arguments");
+    if (n > 0 && !g7) return fail(1, "null grid");
+    if (n == 0) return 0;
+    int *err = error_word();
+    if (!err) return fail(2, "could not allocate the device error word");
+    double *g = nullptr, *modes = nullptr;
+    int rc = 0;
+    if ((rc = scratch_alloc(reinterpret_cast<void **>(&g), sizeof(double) * 4 * n_modes, s)) ||
+        (rc = scratch_alloc(reinterpret_cast<void **>(&modes), sizeof(double) * 3 * n_modes, s))) {
+        scratch_free(g, s);
+        return rc;
+    }
+    rc = normal_deviates_dev(seed, 4L * n_modes, 1.0, g, err, s);
+    if (!rc) {
+        po_modes_kernel<<<(n_modes + 127) / 128, 128, 0, s>>>(n_modes, g, 1.0 / corr_len, modes);
+        po_correlated_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+            n, g7, n_modes, modes, rms * sqrt(2.0 / n_modes), delta, apply);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = fail(2, std::string("surface error: ") + cudaGetErrorString(e));
+        else note_launches(2);
+    }
+    scratch_free(g, s);
+    scratch_free(modes, s);
+    return rc;
 }
 
 }  // namespace po

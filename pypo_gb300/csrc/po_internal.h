@@ -127,6 +127,15 @@ long choose_split(long nb, long ns, long slots, long max_chunks, long tile);
 
 // FP64 grid generation on the device into a 7-row layout (po_grid_dev.cu).
 int generate_grid_dev(const reflparams &r, double *out7, bool transform, bool spheric, cudaStream_t s);
+// n normal deviates N(0, stdev) in the reference's sequence (mt19937 seeded
+// with `seed`, a fresh distribution per draw), on the device.
+int normal_deviates_dev(unsigned seed, long n, double stdev, double *out, int *err, cudaStream_t s);
+// Correlated surface error at the n points of a 7-row device grid (delta
+// and/or the points moved along their normals), and its host twin (po_grid.cpp).
+int correlated_error_dev(long n, double *g7, double rms, double corr_len, unsigned seed, int n_modes, double *delta,
+                         int apply, cudaStream_t s);
+int correlated_error_host(long n, double *g7, double rms, double corr_len, unsigned seed, int n_modes, double *delta,
+                          int apply);
 
 // Source producers on the device (po_sources_dev.cu).
 int gauss_beam_dev(long n, const double *g7, double lam, double w0, double z, double power, int mode,

@@ -82,6 +82,7 @@ constexpr float kTangentTol32 = 5e-7f;
 
 // Device error codes (written to the call's error word).
 constexpr int kErrWaitTimeout = 101;
+constexpr int kErrRngBound = 102;   // the device normal generator ran past its bound (never expected)
 
 // Frame of the split representation: positions in turns (mm * kappa),
 // relative to origin o, hi parts on multiples of q.

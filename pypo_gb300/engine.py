@@ -55,6 +55,37 @@ def generate_grid_dev(refl, transform=True, spheric=True, device=None, stream=No
     return out
 
 
+def correlated_error(g7, rms, corr_len, seed, n_modes=512, apply=False):
+    """Correlated surface error at the points of a (7, n) host grid
+    (po_correlated_error): covariance rms^2 exp(-r^2 / (2 corr_len^2)) over
+    (x, y), spectral synthesis over n_modes modes from mt19937(seed). Returns
+    delta (n,); with apply, g7 (C-contiguous float64) is also moved along
+    its normals in place."""
+    lib = load()
+    if not (isinstance(g7, np.ndarray) and g7.dtype == np.float64 and g7.flags.c_contiguous and g7.shape[0] == 7):
+        raise POError("g7 must be a C-contiguous (7, n) float64 array")
+    n = g7.shape[1]
+    delta = np.empty(n)
+    check(lib.po_correlated_error(n, g7.ctypes.data, float(rms), float(corr_len), int(seed), int(n_modes),
+                                  delta.ctypes.data, 1 if apply else 0))
+    return delta
+
+
+def correlated_error_dev(g7, rms, corr_len, seed, n_modes=512, apply=False, stream=None):
+    """correlated_error on a (7, n) float64 CUDA tensor (po_correlated_error_dev),
+    queued on `stream`; returns delta as a CUDA tensor."""
+    import torch
+    lib = load()
+    if not (g7.is_cuda and g7.dtype == torch.float64 and g7.is_contiguous() and g7.shape[0] == 7):
+        raise POError("g7 must be a contiguous (7, n) float64 CUDA tensor")
+    n = g7.shape[1]
+    delta = torch.empty(n, dtype=torch.float64, device=g7.device)
+    st = torch.cuda.current_stream(g7.device) if stream is None else stream
+    check(lib.po_correlated_error_dev(n, g7.data_ptr(), float(rms), float(corr_len), int(seed), int(n_modes),
+                                      delta.data_ptr(), 1 if apply else 0, ctypes.c_void_p(st.cuda_stream)))
+    return delta
+
+
 def _shape_checks(mode, src7, cur, tgt7, gmode, ncx, ncy):
     if mode not in MODE_ID:
         raise POError(f"unknown mode {mode!r}; expected one of {tuple(MODE_ID)}")
