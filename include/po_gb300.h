@@ -319,14 +319,18 @@ int po_run_dev_static(int mode, long ns, const double *src7, int gmode, int ncx,
  * propagation's outputs, `cot` holds dL/d(output) in the output's row layout
  * (po_n_out(mode) rows x nt, real and imaginary parts as separate rows).
  * Returns, for any non-NULL destination:
- *   grad_cur  dL/d(cur), 12 rows x ns (c2Bundle order, real rows)
+ *   grad_cur  dL/d(cur), 12 rows x ns (c2Bundle order, real rows); for the
+ *             scalar mode 2 rows (re, im) of the source field
  *   grad_ds   dL/d(delta_s), ns: displacement of each source point along its
  *             normal, normals and areas frozen (the reference's surface-error
  *             convention, InterfaceReflector.cpp:852-866)
- *   grad_dt   dL/d(delta_t), nt: the same for target points (near field)
- * Modes JM, EH, JMEH and FF (EHP is nonlinear in the fields; scalar is not
- * built). The Green's function is recomputed, nothing of size ns*nt is
- * stored. precision 0 mixed, 1 plain FP64. flags bit 0: M == 0 on the source.
+ *   grad_dt   dL/d(delta_t), nt: the same for target points (near field and
+ *             scalar)
+ * Every mode. EHP is nonlinear in the target's fields: its adjoint runs the
+ * EH forward again and maps the cotangents through the EHP reflection's
+ * Jacobian there (forward-mode dual numbers) before the EH adjoint. The
+ * Green's function is recomputed, nothing of size ns*nt is stored.
+ * precision 0 mixed, 1 plain FP64. flags bit 0: M == 0 on the source.
  * po_adjoint_dev queues on `stream` (device pointers); po_adjoint_d takes host
  * buffers and synchronises. */
 int po_adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,

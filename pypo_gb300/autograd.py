@@ -4,9 +4,11 @@
 returns the mode's output rows (n_out, nt) as a float64 CUDA tensor and is
 differentiable with respect to:
 
-  cur  (12, ns)  the source currents (c2Bundle row order, real rows)
+  cur  (12, ns)  the source currents (c2Bundle row order, real rows); for
+                 the scalar mode the (2, ns) field (re, im)
   ds   (ns,)     displacement of each source point along its normal
-  dt   (nt,)     displacement of each target point along its normal (near field)
+  dt   (nt,)     displacement of each target point along its normal (near
+                 field and scalar)
 
 Displaced points move along their (frozen) normals with their areas frozen,
 the reference's surface-error convention (reference
@@ -51,7 +53,7 @@ class POFunction(torch.autograd.Function):
         want_cur = ctx.needs_input_grad[0]
         want_ds = has_ds and ctx.needs_input_grad[1]
         want_dt = has_dt and ctx.needs_input_grad[2] and mode != "FF"
-        gc = torch.empty((12, ns), dtype=torch.float64, device=s7.device) if want_cur else None
+        gc = torch.empty(tuple(cur.shape), dtype=torch.float64, device=s7.device) if want_cur else None
         gs = torch.empty(ns, dtype=torch.float64, device=s7.device) if want_ds else None
         gt = torch.empty(nt, dtype=torch.float64, device=s7.device) if want_dt else None
         if want_cur or want_ds or want_dt:
@@ -63,6 +65,4 @@ class POFunction(torch.autograd.Function):
 def propagate(mode, src7, cur, gmode, ncx, ncy, tgt7, k, ds=None, dt=None, epsilon=1.0, t_dir=-1.0,
               precision="mixed"):
     """Differentiable propagation (see the module docstring)."""
-    if mode in ("EHP", "scalar"):
-        raise ValueError("the adjoint covers modes JM, EH, JMEH and FF")
     return POFunction.apply(cur, ds, dt, mode, src7, gmode, ncx, ncy, tgt7, k, epsilon, t_dir, precision)

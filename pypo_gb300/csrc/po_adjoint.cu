@@ -256,6 +256,10 @@ __global__ void po_adj_cot_kernel(int mode, long nt, const double *__restrict__ 
             gh[c] = row(6 + c);
         }
     }
+    if (mode == kScalar) {   // (re, im) of the one complex output, in the E.x slot
+        ge[0] = row(0);
+        ge[3] = row(1);
+    }
     if (mode == kJMEH) {
         for (int c = 0; c < 6; ++c) {
             ge[c] = row(12 + c);
@@ -296,6 +300,29 @@ __global__ void po_adj_cot_kernel(int mode, long nt, const double *__restrict__ 
     for (int c = 0; c < 6; ++c) {
         gam[(long)c * nt + i] = ge[c];
         gam[(long)(6 + c) * nt + i] = gh[c];
+    }
+}
+
+// EHP: the outputs are a pointwise nonlinear function of the incident E, H at
+// the target (ehp_reflect). Its vector-Jacobian product at the forward's
+// fields, one forward-mode pass per input (E re xyz, E im, H re, H im):
+// gam_k = sum_rows cot_row d(out_row)/d(in_k) is dL/d(in_k), i.e. gE and gH
+// for the EH adjoint that follows. `eh` holds the EH forward's 12 rows.
+__global__ void po_adj_ehp_cot_kernel(long nt, const double *__restrict__ cot, const double *__restrict__ eh,
+                                      const double *__restrict__ tgt7, double zeta_inv, double *__restrict__ gam)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    const double n[3] = {tgt7[3 * nt + i], tgt7[4 * nt + i], tgt7[5 * nt + i]};
+    double base[12];
+    for (int q = 0; q < 12; ++q) base[q] = eh[(long)q * nt + i];
+    for (int kq = 0; kq < 12; ++kq) {
+        Dual in[12], out[15];
+        for (int q = 0; q < 12; ++q) in[q] = Dual(base[q], q == kq ? 1.0 : 0.0);
+        ehp_reflect(in, in + 3, in + 6, in + 9, n, zeta_inv, out);
+        double g = 0.0;
+        for (int r = 0; r < 15; ++r) g += cot[(long)r * nt + i] * out[r].d;
+        gam[(long)kq * nt + i] = g;
     }
 }
 
@@ -354,7 +381,21 @@ po_adj_src_fp64_kernel(const double *__restrict__ srcd, long ns, const double *_
             const double *r = tile + s * 15;
             const cx<double> gE[3] = {{r[3], r[6]}, {r[4], r[7]}, {r[5], r[8]}};
             const cx<double> gH[3] = {{r[9], r[12]}, {r[10], r[13]}, {r[11], r[14]}};
-            if (KIND == kKindNF) {
+            if (KIND == kKindScalar) {
+                // c = e^{-t j k R} / R; Sbar' += conj(c) g; n . grad_d phi = Re[conj(g) S' dc/dR] (n.d) / R
+                const double dx = r[0] - sp[0], dy = r[1] - sp[1], dz = r[2] - sp[2];
+                const double R = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / R;
+                double sn, cs;
+                sincos(k * R, &sn, &cs);
+                const cx<double> c = {cs * rinv, -T * sn * rinv};
+                const cx<double> g = gE[0];
+                const cx<double> sb = cmul(cconj(c), g);
+                acc[0] += sb.r;
+                acc[3] += sb.i;
+                const cx<double> y = cmul(cmul(cconj(g), sc.J[0]), c);
+                const double dphi = -y.r * rinv + T * k * y.i;
+                acc[12] += dphi * rinv * (sc.n[0] * dx + sc.n[1] * dy + sc.n[2] * dz);
+            } else if (KIND == kKindNF) {
                 const double dx = r[0] - sp[0], dy = r[1] - sp[1], dz = r[2] - sp[2];
                 const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                                       __dmul_rn(dz, dz)));
@@ -392,8 +433,8 @@ po_adj_src_fp64_kernel(const double *__restrict__ srcd, long ns, const double *_
         for (int a = 0; a < kAccAdj; ++a) part[(long)a * ns + si] = acc[a];
 }
 
-// Plain FP64 target-side displacement adjoint (near field).
-template <int T>
+// Plain FP64 target-side displacement adjoint (near field, scalar).
+template <int KIND, int T>
 __global__ void __launch_bounds__(kThreadsD)
 po_adj_tgt_fp64_kernel(const double *__restrict__ srcd, long ns, const double *__restrict__ tgt7,
                        const double *__restrict__ gam, long nt, double k, double *__restrict__ part)
@@ -425,6 +466,15 @@ po_adj_tgt_fp64_kernel(const double *__restrict__ srcd, long ns, const double *_
         for (int s = 0; s < cnt; ++s) {
             const double *r = tile + s * kRecD;
             const double dx = p[0] - r[0], dy = p[1] - r[1], dz = p[2] - r[2];
+            if (KIND == kKindScalar) {
+                const double R = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / R;
+                double sn, cs;
+                sincos(k * R, &sn, &cs);
+                const cx<double> c = {cs * rinv, -T * sn * rinv};
+                const cx<double> y = cmul(cmul(a[0], cx<double>{r[6], r[7]}), c);   // a = conj(g)
+                acc += (-y.r * rinv + T * k * y.i) * rinv * (n[0] * dx + n[1] * dy + n[2] * dz);
+                continue;
+            }
             const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                                   __dmul_rn(dz, dz)));
             const double rinv = __ddiv_rn(1.0, R);
@@ -463,7 +513,11 @@ __global__ void po_adj_src_epilogue_kernel(int kind, int nsplit, long ns, const 
         if (gmode != 1 && (yv == 0 || yv == ncy - 1)) w *= 0.5;
     }
     const double fr = fac_re * w, fi = fac_im * w;
-    if (grad_cur)
+    if (grad_cur && kind == kKindScalar) {
+        // conj(f) * (re + j im), two rows
+        grad_cur[i] = fr * a[0] + fi * a[3];
+        grad_cur[ns + i] = fr * a[3] - fi * a[0];
+    } else if (grad_cur)
         for (int g = 0; g < 2; ++g)
             for (int c = 0; c < 3; ++c) {
                 const double re = a[6 * g + c], im = a[6 * g + 3 + c];
@@ -471,7 +525,6 @@ __global__ void po_adj_src_epilogue_kernel(int kind, int nsplit, long ns, const 
                 grad_cur[(long)(6 * g + c) * ns + i] = fr * re + fi * im;
                 grad_cur[(long)(6 * g + 3 + c) * ns + i] = fr * im - fi * re;
             }
-    (void)kind;
     if (grad_ds) grad_ds[i] = dscale * a[12];
 }
 
@@ -489,6 +542,9 @@ __global__ void po_adj_tgt_epilogue_kernel(int nsplit, long nt, const double *__
 
 void *adj_src_fp64_kernel(int kind, int t_sign)
 {
+    if (kind == kKindScalar)
+        return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindScalar, -1>)
+                          : reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindScalar, 1>);
     if (kind == kKindNF)
         return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindNF, -1>)
                           : reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindNF, 1>);
@@ -496,13 +552,17 @@ void *adj_src_fp64_kernel(int kind, int t_sign)
                       : reinterpret_cast<void *>(&po_adj_src_fp64_kernel<kKindFF, 1>);
 }
 
-void *adj_tgt_fp64_kernel(int t_sign)
+void *adj_tgt_fp64_kernel(int kind, int t_sign)
 {
-    return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<-1>)
-                      : reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<1>);
+    if (kind == kKindScalar)
+        return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<kKindScalar, -1>)
+                          : reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<kKindScalar, 1>);
+    return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<kKindNF, -1>)
+                      : reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<kKindNF, 1>);
 }
 
 void *adj_cot_kernel() { return reinterpret_cast<void *>(&po_adj_cot_kernel); }
+void *adj_ehp_cot_kernel() { return reinterpret_cast<void *>(&po_adj_ehp_cot_kernel); }
 void *adj_src_epilogue_kernel() { return reinterpret_cast<void *>(&po_adj_src_epilogue_kernel); }
 void *adj_tgt_epilogue_kernel() { return reinterpret_cast<void *>(&po_adj_tgt_epilogue_kernel); }
 

@@ -43,7 +43,7 @@ namespace po {
 //   18-20 r_hat = hi + lo (11 float4).
 __host__ __device__ constexpr int adj2_rec(int kind, bool has_m, bool want_t)
 {
-    return kind == kKindFF ? 11 : (want_t ? (has_m ? 13 : 12) : 9);
+    return kind == kKindFF ? 11 : (want_t ? (has_m ? 13 : 12) : 9);   // scalar: the near-field layout
 }
 
 constexpr int kPairsA2 = PO_PAIRS_A;   // target pairs per shared-memory stage
@@ -271,6 +271,47 @@ __device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const floa
     }
 }
 
+// Scalar pair of targets against the thread's source (S' in the J.x slot,
+// the cotangent g in the gE.x slot): the forward term is S' c with
+// c = e^{-t j k R} / R, so
+//   Sbar' += conj(c) g,
+//   n . grad_d phi = (dphi/dR) (n . d) / R with phi = Re[conj(g) S' c] and
+//   dc/dR = c (-t j k - 1 / R)   (k = 2 pi in turns);
+// no illumination test (the reference's scalar sum has none).
+template <int T, bool WANT_D, bool WANT_T>
+__device__ __forceinline__ void adj_sc_pair2(float2 *acc, float2 &vt, const float2 *r, const SrcC &s)
+{
+    const float2 dhx = sub2(r[0], dup2(s.sh[0])), dhy = sub2(r[1], dup2(s.sh[1])), dhz = sub2(r[2], dup2(s.sh[2]));
+    const float2 dlx = sub2(r[3], dup2(s.sl[0])), dly = sub2(r[4], dup2(s.sl[1])), dlz = sub2(r[5], dup2(s.sl[2]));
+    const float2 two = dup2(2.0f);
+    const float2 S0 = fma2(dhz, dhz, fma2(dhy, dhy, mul2(dhx, dhx)));
+    const float2 S1 = fma2(dlz, fma2(two, dhz, dlz), fma2(dly, fma2(two, dhy, dly), mul2(dlx, fma2(two, dhx, dlx))));
+    const float2 R2 = add2(S0, S1);
+    const float2 rinv = make_float2(rsqrt_ftz(R2.x), rsqrt_ftz(R2.y));
+    const float2 Rh = mul2(R2, rinv);
+    float2 sn, cs, tq;
+    phase_sincos2(S0, S1, Rh, rinv, sn, cs, tq);
+    // c = G / R, G = e^{-t j 2 pi R} = cos - t j sin
+    const float2 rs = flip_parity(rinv, tq);
+    const float2 cr = mul2(cs, rs), ci = mul2(T > 0 ? neg2(sn) : sn, rs);
+    const float2 gr = r[6], gi = r[7];
+    acc[0] = fma2(cr, gr, fma2(ci, gi, acc[0]));
+    acc[3] = fma2(cr, gi, fma2(neg2(ci), gr, acc[3]));
+    if (!WANT_D && !WANT_T) return;
+    // X = conj(g) S', Y = X c, dphi/dR = Re[Y (-1/R - t j 2 pi)] = -Y.re / R + t 2 pi Y.im
+    const float2 Sr = dup2(s.J[0]), Si = dup2(s.J[1]);
+    const float2 xr = fma2(gr, Sr, mul2(gi, Si)), xi = fma2(gr, Si, mul2(neg2(gi), Sr));
+    const float2 yr = fma2(xr, cr, mul2(neg2(xi), ci)), yi = fma2(xr, ci, mul2(xi, cr));
+    const float2 dphi = fma2(neg2(yr), rinv, mul2(yi, dup2(T > 0 ? 6.28318530717958647f : -6.28318530717958647f)));
+    const float2 dx = add2(dhx, dlx), dy = add2(dhy, dly), dz = add2(dhz, dlz);
+    const float2 g = mul2(dphi, rinv);
+    if (WANT_D) {
+        const float2 ndd = fma2(dup2(s.n[2]), dz, fma2(dup2(s.n[1]), dy, mul2(dup2(s.n[0]), dx)));
+        acc[12] = fma2(g, ndd, acc[12]);
+    }
+    if (WANT_T) vt = mul2(g, fma2(r[20], dz, fma2(r[19], dy, mul2(r[18], dx))));
+}
+
 // Far-field pair of targets against the thread's source:
 //   Jbar' += conj(G) gS_J, Mbar' += conj(G) gS_M (G = e^{-t j k r'.r_hat}),
 //   source displacement: Re[-t j k G (conj(gS_J).J' + conj(gS_M).M')] (n_s . r_hat),
@@ -363,7 +404,7 @@ __global__ void __launch_bounds__(kThreadsA, kMinBlocksA2)
 po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
                  double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err, int boxes)
 {
-    static_assert(KIND == kKindNF || !WANT_T, "far-field targets do not move");
+    static_assert(KIND != kKindFF || !WANT_T, "far-field targets do not move");
     constexpr int RT = adj2_rec(KIND, HAS_M, WANT_T);
     constexpr int NL = 2 * RT;                    // float2 slots read per pair
     extern __shared__ __align__(128) float4 stage[];   // kStages * kPairsA2 * RT, lo, transpose buffer
@@ -522,6 +563,7 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
                     }
                     float2 vt = make_float2(0.f, 0.f);
                     if (KIND == kKindNF) adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s);
+                    else if (KIND == kKindScalar) adj_sc_pair2<T, WANT_D, WANT_T>(acc, vt, rec, s);
                     else adj_ff_pair2<T, HAS_M, WANT_D, false>(acc, rec, s);
                     if (WANT_T) vbuf[(p - fb) * kThreadsA + threadIdx.x] = vt;
                 }
@@ -594,6 +636,11 @@ static void *adj_pk_sel(int kind, bool want_d, bool want_t)
 {
     if (kind == kKindFF) return want_d ? adj_pk_ptr<kKindFF, T, HAS_M, true, false>()
                                        : adj_pk_ptr<kKindFF, T, HAS_M, false, false>();
+    if (kind == kKindScalar) {
+        if (want_d) return want_t ? adj_pk_ptr<kKindScalar, T, false, true, true>()
+                                  : adj_pk_ptr<kKindScalar, T, false, true, false>();
+        return want_t ? adj_pk_ptr<kKindScalar, T, false, false, true>() : adj_pk_ptr<kKindScalar, T, false, false, false>();
+    }
     if (want_d) return want_t ? adj_pk_ptr<kKindNF, T, HAS_M, true, true>() : adj_pk_ptr<kKindNF, T, HAS_M, true, false>();
     return want_t ? adj_pk_ptr<kKindNF, T, HAS_M, false, true>() : adj_pk_ptr<kKindNF, T, HAS_M, false, false>();
 }

@@ -470,16 +470,17 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     double *ext = extent_slot(&extent);
     *ext = 0.0;
     const size_t ns1 = std::max(ns, 1L), nt1 = std::max(nt, 1L);
+    const int ncur = mode == po::kScalar ? 2 : 12;
     PO_SCRATCH(d_src, sizeof(double) * 7 * ns1);
-    PO_SCRATCH(d_cur, sizeof(double) * 12 * ns1);
+    PO_SCRATCH(d_cur, sizeof(double) * ncur * ns1);
     PO_SCRATCH(d_tgt, sizeof(double) * 7 * nt1);
     PO_SCRATCH(d_cot, sizeof(double) * nout * nt1);
-    if (grad_cur) PO_SCRATCH(d_gc, sizeof(double) * 12 * ns1);
+    if (grad_cur) PO_SCRATCH(d_gc, sizeof(double) * ncur * ns1);
     if (grad_ds) PO_SCRATCH(d_gs, sizeof(double) * ns1);
     if (grad_dt) PO_SCRATCH(d_gt, sizeof(double) * nt1);
     if (ns > 0) {
         CK(cudaMemcpyAsync(d_src, src7, sizeof(double) * 7 * ns, cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(d_cur, cur, sizeof(double) * 12 * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_cur, cur, sizeof(double) * ncur * ns, cudaMemcpyHostToDevice, s));
     }
     if (nt > 0) {
         CK(cudaMemcpyAsync(d_tgt, tgt7, sizeof(double) * 7 * nt, cudaMemcpyHostToDevice, s));
@@ -487,12 +488,13 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     }
     {
         bool mz = false;
-        if (ns > 0 && (rc = m_is_zero(cur, d_cur, ns, s, mz))) goto done;
+        if (ns > 0 && mode != po::kScalar && (rc = m_is_zero(cur, d_cur, ns, s, mz))) goto done;
         rc = adjoint_dev(mode, ns, d_src, gmode, ncx, ncy, d_cur, nt, d_tgt, k, epsilon, t_direction, precision,
                          mz ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s, ext);
     }
     if (rc) goto done;
-    if (grad_cur && ns > 0) CK(cudaMemcpyAsync(grad_cur, d_gc, sizeof(double) * 12 * ns, cudaMemcpyDeviceToHost, s));
+    if (grad_cur && ns > 0)
+        CK(cudaMemcpyAsync(grad_cur, d_gc, sizeof(double) * ncur * ns, cudaMemcpyDeviceToHost, s));
     if (grad_ds && ns > 0) CK(cudaMemcpyAsync(grad_ds, d_gs, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
     if (grad_dt && nt > 0) CK(cudaMemcpyAsync(grad_dt, d_gt, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
     rc = po::read_device_error(s, &code);   // the call's one synchronisation

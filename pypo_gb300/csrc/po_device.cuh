@@ -202,4 +202,97 @@ __device__ __forceinline__ void split_hi_lo(double x, const Frame &fr, float &h,
     l = (float)(x - hd);
 }
 
+// --------------------------------------------------- EHP reflection, generic
+//
+// The reflected field of mode EHP (reference src/CPU/Propagation.h:840-913,
+// Snell's law Utils.h:421-432): the incident Poynting direction
+// s_i = Re(E x conj H) / |.|, the reflected direction s_r = s_i - 2 (s_i.n) n,
+// the incident and reflected polarisation bases, E_r = -(E.p_r) p_i -
+// (E.a_r) a_i and H_r = zeta_inv s_r x E_r. Written for any real type F with
+// the arithmetic operators (double in the epilogue; a dual number in the
+// adjoint's cotangent mapping, which differentiates it forward mode).
+// out: E_r re xyz, im xyz, H_r re xyz, im xyz, s_r xyz (15).
+template <typename F>
+__device__ __forceinline__ void ehp_cross(const F *a, const F *b, F *o)
+{
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+template <typename F>
+__device__ __forceinline__ void ehp_normalize(const F *v, F *o)
+{
+    F n = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (n <= 4.9406564584124654e-324) n = 4.9406564584124654e-324;
+    for (int c = 0; c < 3; ++c) o[c] = v[c] / n;
+}
+
+template <typename F>
+__device__ __forceinline__ void ehp_reflect(const F *er, const F *ei, const F *hr, const F *hi, const double *nd,
+                                            double zeta_inv, F *out)
+{
+    F s[3], si[3], tmp[3], pip[3], pia[3], sr[3], prp[3], pra[3], n[3];
+    for (int c = 0; c < 3; ++c) {
+        n[c] = nd[c];
+        // Re(E x conj(H))_c
+        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+        s[c] = (er[a1] * hr[a2] + ei[a1] * hi[a2]) - (er[a2] * hr[a1] + ei[a2] * hi[a1]);
+    }
+    ehp_normalize(s, si);
+    ehp_cross(si, n, tmp);
+    ehp_normalize(tmp, pip);
+    ehp_cross(pip, si, pia);
+    const F f = 2.0 * (si[0] * n[0] + si[1] * n[1] + si[2] * n[2]);
+    for (int c = 0; c < 3; ++c) sr[c] = si[c] - n[c] * f;
+    ehp_cross(sr, n, tmp);
+    ehp_normalize(tmp, prp);
+    ehp_cross(sr, prp, pra);
+    const F epr = er[0] * prp[0] + er[1] * prp[1] + er[2] * prp[2];
+    const F epi = ei[0] * prp[0] + ei[1] * prp[1] + ei[2] * prp[2];
+    const F ear = er[0] * pra[0] + er[1] * pra[1] + er[2] * pra[2];
+    const F eai = ei[0] * pra[0] + ei[1] * pra[1] + ei[2] * pra[2];
+    F rr[3], ri[3], xr[3], xi[3];
+    for (int c = 0; c < 3; ++c) {
+        rr[c] = -epr * pip[c] - ear * pia[c];
+        ri[c] = -epi * pip[c] - eai * pia[c];
+    }
+    ehp_cross(sr, rr, xr);
+    ehp_cross(sr, ri, xi);
+    for (int c = 0; c < 3; ++c) {
+        out[c] = rr[c];
+        out[3 + c] = ri[c];
+        out[6 + c] = xr[c] * zeta_inv;
+        out[9 + c] = xi[c] * zeta_inv;
+        out[12 + c] = sr[c];
+    }
+}
+
+// Forward-mode dual number: value and derivative along one seed direction.
+// (sqrt is a hidden friend, found by argument-dependent lookup only, so it
+// does not hide ::sqrt for doubles in this namespace.)
+struct Dual {
+    double v, d;
+    __device__ Dual() : v(0.0), d(0.0) {}
+    __device__ Dual(double x) : v(x), d(0.0) {}
+    __device__ Dual(double x, double dx) : v(x), d(dx) {}
+    __device__ friend Dual sqrt(Dual a)
+    {
+        const double r = ::sqrt(a.v);
+        return Dual(r, r > 0.0 ? a.d / (2.0 * r) : 0.0);
+    }
+};
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+__device__ __forceinline__ Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+__device__ __forceinline__ Dual operator*(double a, Dual b) { return Dual(a * b.v, a * b.d); }
+__device__ __forceinline__ Dual operator*(Dual a, double b) { return Dual(a.v * b, a.d * b); }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b)
+{
+    const double q = a.v / b.v;
+    return Dual(q, (a.d - q * b.d) / b.v);
+}
+__device__ __forceinline__ bool operator<=(Dual a, double b) { return a.v <= b; }
+
 }  // namespace po

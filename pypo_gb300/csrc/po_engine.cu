@@ -526,8 +526,6 @@ int run_mixed(const RunArgs &a, Scratch &sc, int *err)
 int run_adjoint(const AdjArgs &a)
 {
     if (int rc = validate(a)) return rc;
-    if (a.mode == kEHP || a.mode == kScalar)
-        return fail(1, "the adjoint covers modes JM, EH, JMEH and FF (EHP is nonlinear, scalar not built)");
     if (a.mode == kFF && a.grad_dt) return fail(1, "far-field targets are directions: no target displacement");
     if (a.nt > 0 && !a.cot) return fail(1, "null cotangent buffer");
     if (a.ns == 0) {
@@ -537,7 +535,8 @@ int run_adjoint(const AdjArgs &a)
     }
     if (a.nt == 0) {
         // no targets: every gradient is zero
-        if (a.grad_cur) PO_CK(cudaMemsetAsync(a.grad_cur, 0, sizeof(double) * 12 * a.ns, a.stream));
+        if (a.grad_cur)
+            PO_CK(cudaMemsetAsync(a.grad_cur, 0, sizeof(double) * (a.mode == kScalar ? 2 : 12) * a.ns, a.stream));
         if (a.grad_ds) PO_CK(cudaMemsetAsync(a.grad_ds, 0, sizeof(double) * a.ns, a.stream));
         return 0;
     }
@@ -546,15 +545,16 @@ int run_adjoint(const AdjArgs &a)
     int *err = error_word();
     if (!err) return fail(2, "could not allocate the device error word");
 
-    const int kind = a.mode == kFF ? kKindFF : kKindNF;
+    const int kind = a.mode == kFF ? kKindFF : (a.mode == kScalar ? kKindScalar : kKindNF);
     const double pif = (double)3.14159265359f;
     const double pref = a.k * a.k / (4.0 * pif);
     const double kappa = a.k / (2.0 * 3.14159265358979323846);
     double fac_re = pref, fac_im = 0.0;
     if (kind == kKindFF) { fac_re = 0.0; fac_im = -pref; }
+    if (kind == kKindScalar) fac_re = -pref * (a.precision == 0 ? kappa : 1.0);
     const int ts = a.t_dir > 0 ? 1 : -1;
     const bool far = kind == kKindFF;
-    const bool has_m = !a.m_zero;
+    const bool has_m = kind != kKindScalar && !a.m_zero;
     const bool want_d = a.grad_ds != nullptr;
     cudaStream_t s = a.stream;
     long ns = a.ns, nt = a.nt;
@@ -567,9 +567,28 @@ int run_adjoint(const AdjArgs &a)
     int rc = 0;
     double *gam = nullptr;
     if ((rc = salloc(&gam, (size_t)12 * nt, s, owned))) { sfree(owned, s); return rc; }
-    void *cargs[] = {&mode, &nt, &cot, &tgt7, &t, &gam};
-    rc = launch(adj_cot_kernel(), dim3(nblk_t), dim3(256), cargs, 0, s);
-    const int zero_scalar = 0;
+    if (a.mode == kEHP) {
+        // EHP is nonlinear in the target's fields: the EH forward at the same
+        // inputs and precision, then the EHP map's vector-Jacobian product
+        // there (po_adj_ehp_cot_kernel) gives the EH adjoint's cotangents
+        double *eh = nullptr;
+        if ((rc = salloc(&eh, (size_t)12 * nt, s, owned))) { sfree(owned, s); return rc; }
+        RunArgs fa = a;
+        fa.mode = kEH;
+        fa.out = eh;
+        fa.extent_host = nullptr;
+        rc = run_device(fa);
+        const double c_l = (double)2.99792458e8f, mu0 = (double)1.2566370614e-6f;
+        double zi = 1.0 / std::sqrt(mu0 / (a.epsilon * (1.0 / (mu0 * c_l * c_l))));
+        void *eargs[] = {&nt, &cot, &eh, &tgt7, &zi, &gam};
+        if (!rc) rc = launch(adj_ehp_cot_kernel(), dim3((unsigned)((nt + 127) / 128)), dim3(128), eargs, 0, s);
+    } else {
+        void *cargs[] = {&mode, &nt, &cot, &tgt7, &t, &gam};
+        rc = launch(adj_cot_kernel(), dim3(nblk_t), dim3(256), cargs, 0, s);
+    }
+    // scalar sources: 2-row currents (FP64 record: S' in its J.x slot; mixed
+    // one-source record: the same, the other currents zero)
+    const int fp64_scalar = kind == kKindScalar ? 1 : 0, mixed_scalar = kind == kKindScalar ? 2 : 0;
 
     if (a.precision == 1) {
         double *srcd = nullptr, *part = nullptr, *partt = nullptr;
@@ -579,7 +598,7 @@ int run_adjoint(const AdjArgs &a)
             sfree(owned, s);
             return rc;
         }
-        void *pargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &fac_re, &fac_im, (void *)&zero_scalar, &srcd};
+        void *pargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &fac_re, &fac_im, (void *)&fp64_scalar, &srcd};
         if (!rc) rc = launch(pack_src_d_kernel(), dim3(nblk_s), dim3(256), pargs, 0, s);
         void *sargs[] = {&srcd, &ns, &tgt7, &gam, &nt, &k, &part};
         timing_mark(s, true);
@@ -594,7 +613,7 @@ int run_adjoint(const AdjArgs &a)
         if (!rc && grad_dt) {
             void *targs[] = {&srcd, &ns, &tgt7, &gam, &nt, &k, &partt};
             timing_mark(s, true);
-            rc = launch(adj_tgt_fp64_kernel(ts), dim3((unsigned)((nt + kThreadsD - 1) / kThreadsD)), dim3(kThreadsD),
+            rc = launch(adj_tgt_fp64_kernel(kind, ts), dim3((unsigned)((nt + kThreadsD - 1) / kThreadsD)), dim3(kThreadsD),
                         targs, 0, s);
             timing_mark(s, false);
             double one_d = 1.0;
@@ -622,7 +641,7 @@ int run_adjoint(const AdjArgs &a)
     int centred = far ? 0 : 1;
     void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
     if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(32), frargs, 0, s);
-    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&zero_scalar, &srcpk};
+    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&mixed_scalar, &srcpk};
     if (!rc) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
     // Pair-packed adjoint: sources in registers, pairs of targets streamed.
     // Near field fused (currents, source and target displacement in one pass).

@@ -472,7 +472,9 @@ __global__ void po_frame_kernel(const double *__restrict__ partial, int nblk, do
 //   r3 = (Jz.re, Jz.im, Mx.re, Mx.im)
 //   r4 = (My.re, My.im, Mz.re, Mz.im)
 //   r5 = (n.z, 0, 0, 0)
-// Scalar record, 2 float4 (kRecScalar): (sh, S'.re), (sl, S'.im).
+// Scalar record, 2 float4 (kRecScalar): (sh, S'.re), (sl, S'.im), with
+// scalar == 1; scalar == 2 puts S' in the J.x slot of the 6-float4 record
+// (the scalar adjoint).
 // fac: complex factor folded into the currents (times weight * area).
 __global__ void po_pack_src_kernel(long ns, const double *__restrict__ src7, const double *__restrict__ cur,
                                    int gmode, int ncx, int ncy, const Frame *__restrict__ frp, double fac_re,
@@ -485,7 +487,7 @@ __global__ void po_pack_src_kernel(long ns, const double *__restrict__ src7, con
     for (int c = 0; c < 3; ++c) split_hi_lo((src7[c * ns + i] - fr.o[c]) * fr.kappa, fr, h[c], l[c]);
     const double w = trap_weight(i, gmode, ncx, ncy) * src7[6 * ns + i];
     const double fr_ = fac_re * w, fi_ = fac_im * w;
-    if (scalar) {
+    if (scalar == 1) {
         const double re = cur[i], im = cur[ns + i];
         out[2 * i] = make_float4(h[0], h[1], h[2], (float)(fr_ * re - fi_ * im));
         out[2 * i + 1] = make_float4(l[0], l[1], l[2], (float)(fr_ * im + fi_ * re));
@@ -494,8 +496,9 @@ __global__ void po_pack_src_kernel(long ns, const double *__restrict__ src7, con
     float c[12];   // J.re/im x y z interleaved, then M
     for (int q = 0; q < 6; ++q) {
         const int grp = q / 3, ax = q % 3;
-        const double re = cur[(grp * 6 + ax) * ns + i];
-        const double im = cur[(grp * 6 + 3 + ax) * ns + i];
+        // scalar == 2: the 2-row scalar field S in the J.x slot, the rest zero
+        const double re = scalar ? (q == 0 ? cur[i] : 0.0) : cur[(grp * 6 + ax) * ns + i];
+        const double im = scalar ? (q == 0 ? cur[ns + i] : 0.0) : cur[(grp * 6 + 3 + ax) * ns + i];
         c[2 * q] = (float)(fr_ * re - fi_ * im);
         c[2 * q + 1] = (float)(fr_ * im + fi_ * re);
     }
@@ -751,13 +754,6 @@ __device__ __forceinline__ void cross_d(const double a[3], const double b[3], do
     o[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-__device__ __forceinline__ void normalize_d(const double v[3], double o[3])
-{
-    double n = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    if (n <= 4.9406564584124654e-324) n = 4.9406564584124654e-324;
-    for (int c = 0; c < 3; ++c) o[c] = v[c] / n;
-}
-
 // Sums the source chunks in order and writes the mode's outputs (FP64).
 // Output rows follow the reference's bundle order.
 __global__ void po_epilogue_kernel(int mode, int nsplit, long nt, const double *__restrict__ part,
@@ -835,40 +831,9 @@ __global__ void po_epilogue_kernel(int mode, int nsplit, long nt, const double *
         return;
     }
     // EHP: reflected field from the incident Poynting direction (Snell).
-    double s[3], si[3], tmp[3], pip[3], pia[3], sr[3], prp[3], pra[3];
-    for (int c = 0; c < 3; ++c) {
-        // Re(E x conj(H))_c
-        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-        s[c] = (er[a1] * hr[a2] + ei[a1] * hi[a2]) - (er[a2] * hr[a1] + ei[a2] * hi[a1]);
-    }
-    normalize_d(s, si);
-    cross_d(si, n, tmp);
-    normalize_d(tmp, pip);
-    cross_d(pip, si, pia);
-    const double f = 2.0 * (si[0] * n[0] + si[1] * n[1] + si[2] * n[2]);
-    for (int c = 0; c < 3; ++c) sr[c] = si[c] - n[c] * f;
-    cross_d(sr, n, tmp);
-    normalize_d(tmp, prp);
-    cross_d(sr, prp, pra);
-    const double epr = er[0] * prp[0] + er[1] * prp[1] + er[2] * prp[2];
-    const double epi = ei[0] * prp[0] + ei[1] * prp[1] + ei[2] * prp[2];
-    const double ear = er[0] * pra[0] + er[1] * pra[1] + er[2] * pra[2];
-    const double eai = ei[0] * pra[0] + ei[1] * pra[1] + ei[2] * pra[2];
-    double rr[3], ri[3];
-    for (int c = 0; c < 3; ++c) {
-        rr[c] = -epr * pip[c] - ear * pia[c];
-        ri[c] = -epi * pip[c] - eai * pia[c];
-    }
-    double xr[3], xi[3];
-    cross_d(sr, rr, xr);
-    cross_d(sr, ri, xi);
-    for (int c = 0; c < 3; ++c) {
-        put(c, rr[c]);
-        put(3 + c, ri[c]);
-        put(6 + c, xr[c] * zeta_inv);
-        put(9 + c, xi[c] * zeta_inv);
-        put(12 + c, sr[c]);
-    }
+    double o[15];
+    ehp_reflect(er, ei, hr, hi, n, zeta_inv, o);
+    for (int q = 0; q < 15; ++q) put(q, o[q]);
 }
 
 // ------------------------------------------------------------- FP32 probe

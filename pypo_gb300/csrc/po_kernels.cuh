@@ -130,8 +130,9 @@ void *epilogue_kernel();
 void *fp32_probe_kernel();
 void *wait_selftest_kernel();
 void *adj_src_fp64_kernel(int kind, int t_sign);
-void *adj_tgt_fp64_kernel(int t_sign);
+void *adj_tgt_fp64_kernel(int kind, int t_sign);
 void *adj_cot_kernel();
+void *adj_ehp_cot_kernel();
 void *adj_src_epilogue_kernel();
 // Pair-packed adjoint: near field fused (currents, source and target
 // displacement), far field (currents, source displacement).

@@ -213,7 +213,8 @@ def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-
     """Host-buffer adjoint (po_adjoint_d).
 
     cot: (n_out(mode), nt) float64, dL/d(output rows). Returns a dict with the
-    requested gradients: "cur" (12, ns), "ds" (ns,) and "dt" (nt,) (near field),
+    requested gradients: "cur" (the shape of cur: 12 or, scalar, 2 rows), "ds"
+    (ns,) and "dt" (nt,) (near field and scalar),
     written into the arrays of `out` (a dict of C-contiguous float64 arrays of
     those shapes, e.g. page-locked ones) where it has them.
     """
@@ -237,7 +238,7 @@ def adjoint(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-
         return a
 
     out = {}
-    gc = buf("cur", (12, ns)) if "cur" in want else None
+    gc = buf("cur", cur.shape) if "cur" in want else None
     gs = buf("ds", (ns,)) if "ds" in want else None
     gt = buf("dt", (nt,)) if ("dt" in want and mode != "FF") else None
     ptr = lambda a: a.ctypes.data if a is not None else None

@@ -19,7 +19,7 @@ def _case(rng, mode):
     else:
         t7 = engine.generate_grid(SF.translate(SF.plane([6, 5], gmode=0, lims_a=[-1, 1]), dz=3.0))
         t7[3:6] *= -1.0
-    cur = rng.standard_normal((12, s7.shape[1]))
+    cur = rng.standard_normal((2 if mode == "scalar" else 12, s7.shape[1]))
     cot = rng.standard_normal((engine.n_out(mode), t7.shape[1]))
     return s7, cur, t7, cot, (1, 9, 10)
 
@@ -33,7 +33,7 @@ def _fd(oracle_mod, mode, s7, cur, t7, cot, grid, k, t, rng, nsamp=6):
     """Central FD of the oracle loss: current entries, source and target displacements."""
     f = lambda s, c, tt: _loss(oracle_mod, mode, s, c, tt, cot, grid, k, t)
     h_c, h_d = 1e-3, 1e-6 * (2 * np.pi / k)
-    rows = rng.integers(0, 12, nsamp)
+    rows = rng.integers(0, cur.shape[0], nsamp)
     cols = rng.integers(0, s7.shape[1], nsamp)
     fc = []
     for r, c in zip(rows, cols):
@@ -63,11 +63,11 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
-@pytest.mark.parametrize("mode", ["EH", "JM", "JMEH", "FF"])
+@pytest.mark.parametrize("mode", ["EH", "JM", "JMEH", "FF", "scalar"])
 @pytest.mark.parametrize("t", [-1.0, 1.0])
 def test_adjoint_matches_finite_differences(cuda, lib, oracle_mod, mode, t):
     from pypo_gb300 import engine
-    rng = np.random.default_rng({"EH": 10, "JM": 20, "JMEH": 30, "FF": 40}[mode] + (t > 0))
+    rng = np.random.default_rng({"EH": 10, "JM": 20, "JMEH": 30, "FF": 40, "scalar": 50}[mode] + (t > 0))
     s7, cur, t7, cot, grid = _case(rng, mode)
     k = 2 * np.pi / 0.9
     (rows, cols, fc), (si, fs), (ti, ft) = _fd(oracle_mod, mode, s7, cur, t7, cot, grid, k, t, rng)
@@ -244,3 +244,59 @@ def test_empty_adjoints_write_their_zeros(cuda, lib):
                                       grad_dt=nan(12))
         torch.cuda.synchronize()
         assert torch.all(gt == 0), prec
+
+
+@pytest.mark.parametrize("mode", ["EH", "JM", "JMEH", "FF", "scalar"])
+@pytest.mark.parametrize("t", [-1.0, 1.0])
+def test_adjoint_matches_oracle_adjoint(cuda, lib, oracle_mod, mode, t):
+    """Every gradient, every source and target, against the oracle's FP64
+    adjoint: mixed within 1e-5, FP64 within 1e-10 (relative L2)."""
+    from pypo_gb300 import engine
+    rng = np.random.default_rng({"EH": 11, "JM": 21, "JMEH": 31, "FF": 41, "scalar": 51}[mode] + (t > 0))
+    s7, cur, t7, cot, grid = _case(rng, mode)
+    k = 2 * np.pi / 0.9
+    ref = oracle_mod.adjoint(mode, s7, cur, *grid, t7, k, cot, 1.0, t)
+    for prec, tol in (("mixed", 1e-5), ("fp64", 1e-10)):
+        g = engine.adjoint(mode, s7, cur, *grid, t7, k, cot, 1.0, t, prec)
+        for name, want in ref.items():
+            assert _rel(g[name], want) <= tol, (prec, name, _rel(g[name], want))
+
+
+@pytest.mark.parametrize("t", [-1.0, 1.0])
+def test_ehp_adjoint_matches_finite_differences(cuda, lib, oracle_mod, t):
+    """EHP (nonlinear in the target's fields): the FP64 adjoint against
+    central differences of the oracle (1e-4, the differences' own truncation
+    at this nonlinearity), the mixed adjoint against the FP64 one (1e-5)."""
+    from pypo_gb300 import engine
+    rng = np.random.default_rng(60 + (t > 0))
+    s7, cur, t7, cot, grid = _case(rng, "EHP")
+    k = 2 * np.pi / 0.9
+    (rows, cols, fc), (si, fs), (ti, ft) = _fd(oracle_mod, "EHP", s7, cur, t7, cot, grid, k, t, rng)
+    gd = engine.adjoint("EHP", s7, cur, *grid, t7, k, cot, 1.0, t, "fp64")
+    assert _rel(gd["cur"][rows, cols], fc) <= 1e-4, (gd["cur"][rows, cols], fc)
+    assert _rel(gd["ds"][si], fs) <= 1e-4, (gd["ds"][si], fs)
+    assert _rel(gd["dt"][ti], ft) <= 1e-4, (gd["dt"][ti], ft)
+    gm = engine.adjoint("EHP", s7, cur, *grid, t7, k, cot, 1.0, t, "mixed")
+    for name in ("cur", "ds", "dt"):
+        assert _rel(gm[name], gd[name]) <= 1e-5, (name, _rel(gm[name], gd[name]))
+
+
+def test_scalar_and_ehp_through_autograd(cuda, lib):
+    """The autograd function covers the scalar and EHP modes: its gradients
+    equal the C-ABI adjoint's."""
+    import torch
+    from pypo_gb300 import autograd as A, engine
+    rng = np.random.default_rng(70)
+    for mode in ("scalar", "EHP"):
+        s7, cur, t7, cot, grid = _case(rng, mode)
+        k = 2 * np.pi / 0.9
+        T = lambda a: torch.tensor(a, device=cuda)
+        c = T(cur).requires_grad_(True)
+        ds = torch.zeros(s7.shape[1], dtype=torch.float64, device=cuda, requires_grad=True)
+        dt = torch.zeros(t7.shape[1], dtype=torch.float64, device=cuda, requires_grad=True)
+        out = A.propagate(mode, T(s7), c, *grid, T(t7), k, ds=ds, dt=dt)
+        (out * T(cot)).sum().backward()
+        g = engine.adjoint(mode, s7, cur, *grid, t7, k, cot)
+        assert _rel(c.grad.cpu().numpy(), g["cur"]) <= 1e-12
+        assert _rel(ds.grad.cpu().numpy(), g["ds"]) <= 1e-12
+        assert _rel(dt.grad.cpu().numpy(), g["dt"]) <= 1e-12
