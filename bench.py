@@ -41,6 +41,11 @@ pairs per second. The arm imports only oracle/ (inputs from
 oracle/workloads.py, equal to pypo_gb300/configs.py's): no product code
 runs on it.
 
+The default run (dish_eh, full size, one GPU) also measures the far-field
+configuration (dish_ff: 1001x1001 dish -> 401x401 far field, 1.6e11 pairs)
+and the Cassegrain chain the same way in shorter runs (3 timed steps) and
+reports them under `other_configs`; --no-others skips them.
+
 Multi-GPU: one process per GPU (torchrun); each rank runs its own replica of
 the workload (targets are independent, no collective on the data path);
 value = all ranks' pairs / max-over-ranks time ("scaling": "weak").
@@ -477,7 +482,7 @@ def run_ours(args):
     # its rate (cpu_baseline) and the GPU results against its outputs
     threads = os.cpu_count() or 1
     crng = np.random.default_rng(123)
-    ncpu = cpu_sample_size(w, cot_np, 10.0, threads, crng)
+    ncpu = cpu_sample_size(w, cot_np, args.cpu_sample_s, threads, crng)
     cidx = np.sort(crng.choice(nt, size=ncpu, replace=False))
     ref_out, ref_g, cpu_tf, cpu_ta = cpu_step(w, cot_np, cidx, threads)
     cpu_rate = ns * ncpu / (cpu_tf + cpu_ta)
@@ -597,9 +602,9 @@ def run_ours(args):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
     }
-    print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+    return line
 
 
 def run_chain(args):
@@ -776,11 +781,11 @@ def run_chain(args):
         grad_fd = dish_chain_fd(c, dvars["dish7"].grad.detach().cpu().numpy(), cot_np, k)
 
     if rank != 0:
-        return
+        return None
     threads = os.cpu_count() or 1
     ws = chain_stage_workloads(c, stages)
     crng = np.random.default_rng(123)
-    frac = cpu_chain_fraction(ws, 6.0, threads, crng)
+    frac = cpu_chain_fraction(ws, args.cpu_sample_s * 0.6, threads, crng)
     cpu_pairs, cpu_s, cpu_parts = cpu_chain_step(ws, frac, threads, crng)
     line = {
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
@@ -802,7 +807,7 @@ def run_chain(args):
                          f" (a fraction {frac:.2e} of every stage's targets), forward + adjoint, FP64 oracle"},
         "gpu_launches": launches[0] * args.steps, "clocks": clocks,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 def main():
     ap = argparse.ArgumentParser()
@@ -817,15 +822,33 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=90.0,
                     help="reference arm: host time of the whole run (warm-up and timed steps), which sizes "
                          "each step's target sample")
+    ap.add_argument("--no-others", action="store_true",
+                    help="default run: skip the shorter runs of the far-field and Cassegrain configurations "
+                         "that the line carries under other_configs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    args.cpu_sample_s = 10.0
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload in CHAINS:
-        run_chain(args)
-    else:
-        run_ours(args)
+        return
+    line = run_chain(args) if args.workload in CHAINS else run_ours(args)
+    if line is None:
+        return
+    rank, world, _ = dist_env()
+    if args.workload == "dish_eh" and args.scale == 1.0 and world == 1 and not args.no_others:
+        # the far-field (1.6e11 pairs) and Cassegrain-chain (2.1e11 pairs)
+        # configurations, each measured the same way in a shorter run
+        others = {}
+        for name in ("dish_ff", "cassegrain"):
+            sub = argparse.Namespace(**vars(args))
+            sub.workload, sub.steps, sub.warmup, sub.cpu_sample_s = name, min(args.steps, 3), 3, 4.0
+            o = run_chain(sub) if name in CHAINS else run_ours(sub)
+            if o is not None:
+                o.pop("metric", None)
+                others[name] = o
+        line["other_configs"] = others
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":
