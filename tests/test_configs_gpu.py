@@ -3,10 +3,13 @@
 Gaussian feed -> dish, JM (full size, 1e8 pairs) against the oracle; the
 D 1000 mm dish to its focal plane (EH, 2.3e10 pairs) and the D 2000 mm dish to
 its far field (FF, 1.6e11 pairs), full size, against the plain FP64 GPU sum on
-sampled targets and the oracle on a few; feed -> perturbed dish -> far field
+a 2 % target sample and against the oracle (the reference's CPU algorithm)
+on 128 / 64 targets, forward and adjoint; feed -> perturbed dish -> far field
 with gradients of sum |E_ff - E_ideal|^2 against central finite differences
-(h = 1e-6 lambda) on 64 random dish nodes; the Cassegrain chain (reduced
-grids) against the FP64 chain, forward and gradients.
+of the oracle chain (h = 1e-6 lambda) on 64 random dish nodes; the Cassegrain
+chain at full size stage by stage (each stage's mixed output against the FP64
+GPU sum on 2 % of its targets and the oracle on 16, from the same inputs) and
+on reduced grids end to end against the FP64 chain, forward and gradients.
 """
 import numpy as np
 import pytest
@@ -30,10 +33,11 @@ def test_feed_to_dish_jm_full_size(cuda, lib, oracle_mod):
     assert e <= REL_L2_TOL and p <= PHASE_TOL, (e, p)
 
 
-@pytest.mark.parametrize("name", ["dish_eh", "dish_ff"])
-def test_dish_workloads_full_size_sampled(cuda, lib, oracle_mod, name):
+@pytest.mark.parametrize("name,n_oracle", [("dish_eh", 128), ("dish_ff", 64)])
+def test_dish_workloads_full_size_sampled(cuda, lib, oracle_mod, name, n_oracle):
     """Full-size run; per-point error on a 2 % random target sample against the
-    FP64 GPU sum, and on 16 targets against the oracle."""
+    FP64 GPU sum, and on n_oracle targets against the oracle, forward (rel L2
+    and phase) and adjoint (every source, those targets)."""
     import torch
     from pypo_gb300 import configs, engine
     w = getattr(configs, name)()
@@ -48,10 +52,17 @@ def test_dish_workloads_full_size_sampled(cuda, lib, oracle_mod, name):
     ref = engine.propagate_dev(w["mode"], s7, cur, *grid, t7s, w["k"], precision="fp64").cpu().numpy()
     e, p = errors(got[:, idx], ref, w["mode"])
     assert e <= REL_L2_TOL and p <= PHASE_TOL, (name, e, p)
-    sub = idx[:: max(1, idx.size // 16)][:16]
+    sub = np.sort(rng.choice(nt, size=n_oracle, replace=False))
     oref = oracle_mod.run(w["mode"], w["s7"], w["cur"], *grid, w["t7"], w["k"], tidx=sub)
-    e2, _ = errors(got[:, sub], oref, w["mode"])
-    assert e2 <= REL_L2_TOL, (name, e2)
+    e2, p2 = errors(got[:, sub], oref, w["mode"])
+    assert e2 <= REL_L2_TOL and p2 <= PHASE_TOL, (name, e2, p2)
+    # the adjoint over every source and those targets, against the oracle's
+    cot = rng.standard_normal((engine.n_out(w["mode"]), sub.size))
+    t7o = np.ascontiguousarray(w["t7"][:, sub])
+    gm = engine.adjoint(w["mode"], w["s7"], w["cur"], *grid, t7o, w["k"], cot)
+    go = oracle_mod.adjoint(w["mode"], w["s7"], w["cur"], *grid, t7o, w["k"], cot)
+    for g_name, want in go.items():
+        assert _rel(gm[g_name], want) <= REL_L2_TOL, (name, g_name, _rel(gm[g_name], want))
 
 
 def _trap_weight(i, gmode, ncx, ncy):
@@ -62,10 +73,10 @@ def _trap_weight(i, gmode, ncx, ncy):
     return w
 
 
-def test_perturbed_dish_chain_gradients_against_finite_differences(cuda, lib):
+def test_perturbed_dish_chain_gradients_against_finite_differences(cuda, lib, oracle_mod):
     """feed -> dish (JM) -> far field (FF), dish displaced by a correlated surface
     error; L = sum |E_ff - E_ideal|^2 (E rows). Autograd (mixed) gradients against
-    central FD of the FP64 GPU chain on 64 random nodes, and against the FP64
+    central FD of the oracle chain on 64 random nodes, and against the FP64
     autograd gradients on every node."""
     import torch
     from pypo_gb300 import autograd as A, configs, engine
@@ -95,20 +106,21 @@ def test_perturbed_dish_chain_gradients_against_finite_differences(cuda, lib):
     assert _rel(g_mixed, g_fp64) <= 1e-4
     assert _rel(gf_mixed, gf_fp64) <= 1e-4
 
-    # central FD of the FP64 chain, one node at a time (exact by linearity:
-    # moving node i changes its induced current and its far-field term only)
+    # central FD of the oracle chain (the reference's CPU algorithm), one node
+    # at a time (exact by linearity: moving node i changes its induced current
+    # and its far-field term only)
     disp = d7.copy()
     disp[:3] += c["delta"][None, :] * d7[3:6]
-    jd = engine.propagate("JM", f7, fcur, *fg, disp, k, precision="fp64")
-    base = engine.propagate("FF", disp, jd, *dg, ff7, k, precision="fp64")
+    jd = oracle_mod.run("JM", f7, fcur, *fg, disp, k)
+    base = oracle_mod.run("FF", disp, jd, *dg, ff7, k)
 
     def one(i, pos):
         p7 = disp[:, i:i + 1].copy()
         p7[:3, 0] = pos
-        ji = engine.propagate("JM", f7, fcur, *fg, p7, k, precision="fp64")
+        ji = oracle_mod.run("JM", f7, fcur, *fg, p7, k, nthreads=1)
         s1 = p7.copy()
         s1[6, 0] = d7[6, i] * _trap_weight(i, *dg)
-        return engine.propagate("FF", s1, ji, -1, 0, 0, ff7, k, precision="fp64")
+        return oracle_mod.run("FF", s1, ji, -1, 0, 0, ff7, k)
 
     def loss_at(i, pos):
         e = base - one(i, disp[:3, i]) + one(i, pos)
@@ -150,3 +162,31 @@ def test_cassegrain_chain_against_fp64(cuda, lib):
     assert e <= REL_L2_TOL and p <= PHASE_TOL, (e, p)
     assert _rel(out["mixed"][1], out["fp64"][1]) <= 1e-4
     assert _rel(out["mixed"][2], out["fp64"][2]) <= 1e-4
+
+
+def test_cassegrain_full_size_stage_by_stage(cuda, lib, oracle_mod):
+    """The Cassegrain chain at full size (feed 201^2 -> hyperboloid 401^2 ->
+    paraboloid 1001^2 -> far field 201^2, 2.1e11 pairs): every stage's mixed
+    output, from the previous stage's mixed output, against the plain FP64 GPU
+    sum of the same inputs on 2 % of its targets and against the oracle on 16.
+    The stages are linear, so the chain's error is bounded by theirs."""
+    from pypo_gb300 import configs, engine
+    c = configs.cassegrain()
+    k = c["k"]
+    rng = np.random.default_rng(5)
+    stages = [("JM", "feed7", "feed_grid", "sec7"), ("JM", "sec7", "sec_grid", "prim7"),
+              ("FF", "prim7", "prim_grid", "ff7")]
+    cur = c["feed_cur"]
+    for mode, sk, gk, tk in stages:
+        src, tgt, grid = c[sk], c[tk], c[gk]
+        out = engine.propagate(mode, src, cur, *grid, tgt, k)
+        nt = tgt.shape[1]
+        idx = np.sort(rng.choice(nt, size=max(16, nt // 50), replace=False))
+        ref = engine.propagate(mode, src, cur, *grid, np.ascontiguousarray(tgt[:, idx]), k, precision="fp64")
+        e, p = errors(out[:, idx], ref, mode)
+        assert e <= REL_L2_TOL and p <= PHASE_TOL, (sk, tk, e, p)
+        sub = np.sort(rng.choice(nt, size=16, replace=False))
+        oref = oracle_mod.run(mode, src, cur, *grid, tgt, k, tidx=sub)
+        e2, _ = errors(out[:, sub], oref, mode)
+        assert e2 <= REL_L2_TOL, (sk, tk, e2)
+        cur = out
