@@ -298,8 +298,9 @@ int po_run_dev(int mode, long ns, const double *src7, int gmode, int ncx, int nc
  * latency-critical loop that cannot take the device-wide synchronisation of
  * cudaFree. Same arguments and results as po_run_dev in mixed precision, plus
  * `status`: an optional device int, cleared at the start of the call and set
- * to 101 if a kernel gave up a bounded wait. With status == NULL the 101 goes
- * to an internal word inside the array instead, which stays set across calls
+ * to a device error code (101 a kernel gave up a bounded wait, 103 more than
+ * 16,384 near-tangent pairs; see po_device_error). With status == NULL the
+ * code goes to an internal word inside the array instead, which stays set across calls
  * until po_device_error reads and clears it (po_device_error allocates
  * nothing).
  * The scratch is a fixed 64 MiB device array inside the library, held by
@@ -347,7 +348,10 @@ int po_last_launches(void);
 
 /* Synchronises `stream`, then returns (and clears) the device error words in
  * *code: 0 when every kernel finished normally, 101 when a kernel gave up a
- * bounded wait for a tile copy (its results are then invalid). It reads the
+ * bounded wait for a tile copy, 103 when a call met more near-tangent
+ * (source, target) pairs than its list holds (1,048,576; 16,384 for
+ * po_run_dev_static), 102 when the device normal generator overran its
+ * bound; the results of such a call are invalid. It reads the
  * word of the allocating entries and the internal word of po_run_dev_static
  * (calls made with status == NULL); it allocates nothing. */
 int po_device_error(void *stream, int *code);

@@ -328,13 +328,62 @@ __global__ void po_adj_ehp_cot_kernel(long nt, const double *__restrict__ cot, c
 
 // ------------------------------------------------------------- FP64 kernels
 
-// The forward FP64 kernel's illumination test: the reference's operation
-// order and rounding (R_hat = d * (1/R), n . R_hat left to right, no FMA).
-__device__ __forceinline__ bool lit_fp64(const double *n, double dx, double dy, double dz, double rinv)
+// One (source, target) pair of the plain FP64 source-side adjoint, added into
+// acc (kAccAdj): sp the source position (mm), sc its constants, r the target
+// as the kernel stages it (point or direction, then the 12 cotangent rows
+// gE re xyz, gE im, gH re, gH im). Unlit pairs add nothing.
+template <int KIND, int T>
+__device__ __forceinline__ void adj_src_pair_fp64(const double *sp, const SrcConst<double> &sc, const double *r,
+                                                  double k, double *acc)
 {
-    const double ndr = __dadd_rn(__dadd_rn(__dmul_rn(n[0], __dmul_rn(dx, rinv)), __dmul_rn(n[1], __dmul_rn(dy, rinv))),
-                                 __dmul_rn(n[2], __dmul_rn(dz, rinv)));
-    return !(ndr < 0.0);
+    const cx<double> gE[3] = {{r[3], r[6]}, {r[4], r[7]}, {r[5], r[8]}};
+    const cx<double> gH[3] = {{r[9], r[12]}, {r[10], r[13]}, {r[11], r[14]}};
+    if (KIND == kKindScalar) {
+        // c = e^{-t j k R} / R; Sbar' += conj(c) g; n . grad_d phi = Re[conj(g) S' dc/dR] (n.d) / R
+        const double dx = r[0] - sp[0], dy = r[1] - sp[1], dz = r[2] - sp[2];
+        const double R = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / R;
+        double sn, cs;
+        sincos(k * R, &sn, &cs);
+        const cx<double> c = {cs * rinv, -T * sn * rinv};
+        const cx<double> g = gE[0];
+        const cx<double> sb = cmul(cconj(c), g);
+        acc[0] += sb.r;
+        acc[3] += sb.i;
+        const cx<double> y = cmul(cmul(cconj(g), sc.J[0]), c);
+        const double dphi = -y.r * rinv + T * k * y.i;
+        acc[12] += dphi * rinv * (sc.n[0] * dx + sc.n[1] * dy + sc.n[2] * dz);
+    } else if (KIND == kKindNF) {
+        const double dx = r[0] - sp[0], dy = r[1] - sp[1], dz = r[2] - sp[2];
+        const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                              __dmul_rn(dz, dz)));
+        const double rinv = __ddiv_rn(1.0, R);
+        if (lit_fp64(sc.n, dx, dy, dz, rinv) == false) return;
+        const double ndd = sc.n[0] * dx + sc.n[1] * dy + sc.n[2] * dz;
+        double sn, cs;
+        sincos(k * R, &sn, &cs);
+        nf_adj_src_algebra<double, T, true, true>(acc, dx, dy, dz, rinv, rinv / k, cs, T * sn, ndd, gE, gH,
+                                                  sc);
+    } else {
+        const double ndr = sc.n[0] * r[0] + sc.n[1] * r[1] + sc.n[2] * r[2];
+        if (__dadd_rn(__dadd_rn(__dmul_rn(sc.n[0], r[0]), __dmul_rn(sc.n[1], r[1])),
+                      __dmul_rn(sc.n[2], r[2])) < 0.0)
+            return;
+        double sn, cs;
+        sincos(k * (sp[0] * r[0] + sp[1] * r[1] + sp[2] * r[2]), &sn, &cs);
+        const cx<double> G = {cs, -T * sn};
+        const cx<double> Gc = cconj(G);
+        for (int c = 0; c < 3; ++c) {
+            const cx<double> jb = cmul(Gc, gE[c]), mb = cmul(Gc, gH[c]);
+            acc[c] += jb.r;
+            acc[3 + c] += jb.i;
+            acc[6 + c] += mb.r;
+            acc[9 + c] += mb.i;
+        }
+        cx<double> gEc[3] = {cconj(gE[0]), cconj(gE[1]), cconj(gE[2])};
+        cx<double> gHc[3] = {cconj(gH[0]), cconj(gH[1]), cconj(gH[2])};
+        const cx<double> Z = cmul(G, cadd(cdot_c(gEc, sc.J), cdot_c(gHc, sc.M)));
+        acc[12] += T * k * Z.i * ndr;
+    }
 }
 
 // Plain FP64 source-side adjoint: thread = source, loop over every target.
@@ -377,60 +426,60 @@ po_adj_src_fp64_kernel(const double *__restrict__ srcd, long ns, const double *_
         }
         __syncthreads();
         if (si >= ns) continue;
-        for (int s = 0; s < cnt; ++s) {
-            const double *r = tile + s * 15;
-            const cx<double> gE[3] = {{r[3], r[6]}, {r[4], r[7]}, {r[5], r[8]}};
-            const cx<double> gH[3] = {{r[9], r[12]}, {r[10], r[13]}, {r[11], r[14]}};
-            if (KIND == kKindScalar) {
-                // c = e^{-t j k R} / R; Sbar' += conj(c) g; n . grad_d phi = Re[conj(g) S' dc/dR] (n.d) / R
-                const double dx = r[0] - sp[0], dy = r[1] - sp[1], dz = r[2] - sp[2];
-                const double R = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / R;
-                double sn, cs;
-                sincos(k * R, &sn, &cs);
-                const cx<double> c = {cs * rinv, -T * sn * rinv};
-                const cx<double> g = gE[0];
-                const cx<double> sb = cmul(cconj(c), g);
-                acc[0] += sb.r;
-                acc[3] += sb.i;
-                const cx<double> y = cmul(cmul(cconj(g), sc.J[0]), c);
-                const double dphi = -y.r * rinv + T * k * y.i;
-                acc[12] += dphi * rinv * (sc.n[0] * dx + sc.n[1] * dy + sc.n[2] * dz);
-            } else if (KIND == kKindNF) {
-                const double dx = r[0] - sp[0], dy = r[1] - sp[1], dz = r[2] - sp[2];
-                const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                                                      __dmul_rn(dz, dz)));
-                const double rinv = __ddiv_rn(1.0, R);
-                if (lit_fp64(sc.n, dx, dy, dz, rinv) == false) continue;
-                const double ndd = sc.n[0] * dx + sc.n[1] * dy + sc.n[2] * dz;
-                double sn, cs;
-                sincos(k * R, &sn, &cs);
-                nf_adj_src_algebra<double, T, true, true>(acc, dx, dy, dz, rinv, rinv / k, cs, T * sn, ndd, gE, gH,
-                                                          sc);
-            } else {
-                const double ndr = sc.n[0] * r[0] + sc.n[1] * r[1] + sc.n[2] * r[2];
-                if (__dadd_rn(__dadd_rn(__dmul_rn(sc.n[0], r[0]), __dmul_rn(sc.n[1], r[1])),
-                              __dmul_rn(sc.n[2], r[2])) < 0.0)
-                    continue;
-                double sn, cs;
-                sincos(k * (sp[0] * r[0] + sp[1] * r[1] + sp[2] * r[2]), &sn, &cs);
-                const cx<double> G = {cs, -T * sn};
-                const cx<double> Gc = cconj(G);
-                for (int c = 0; c < 3; ++c) {
-                    const cx<double> jb = cmul(Gc, gE[c]), mb = cmul(Gc, gH[c]);
-                    acc[c] += jb.r;
-                    acc[3 + c] += jb.i;
-                    acc[6 + c] += mb.r;
-                    acc[9 + c] += mb.i;
-                }
-                cx<double> gEc[3] = {cconj(gE[0]), cconj(gE[1]), cconj(gE[2])};
-                cx<double> gHc[3] = {cconj(gH[0]), cconj(gH[1]), cconj(gH[2])};
-                const cx<double> Z = cmul(G, cadd(cdot_c(gEc, sc.J), cdot_c(gHc, sc.M)));
-                acc[12] += T * k * Z.i * ndr;
-            }
-        }
+        for (int s = 0; s < cnt; ++s) adj_src_pair_fp64<KIND, T>(sp, sc, tile + s * 15, k, acc);
     }
     if (si < ns)
         for (int a = 0; a < kAccAdj; ++a) part[(long)a * ns + si] = acc[a];
+}
+
+// The constants of a target for the FP64 target-side adjoint: its point and
+// normal, a = conj(gE), b = conj(gH), n x a, n x b, a.n and b.n.
+struct TgtConst {
+    double p[3], n[3];
+    cx<double> a[3], b[3], nxa[3], nxb[3], an, bn;
+};
+
+__device__ __forceinline__ void tgt_const(const double *tgt7, const double *gam, long nt, long ti, TgtConst &tc)
+{
+    for (int c = 0; c < 3; ++c) {
+        tc.p[c] = tgt7[c * nt + ti];
+        tc.n[c] = tgt7[(3 + c) * nt + ti];
+        tc.a[c] = {gam[c * nt + ti], -gam[(3 + c) * nt + ti]};
+        tc.b[c] = {gam[(6 + c) * nt + ti], -gam[(9 + c) * nt + ti]};
+    }
+    cx<double> t3[3];
+    ccross_r(tc.a, tc.n[0], tc.n[1], tc.n[2], t3);
+    for (int c = 0; c < 3; ++c) tc.nxa[c] = {-t3[c].r, -t3[c].i};
+    ccross_r(tc.b, tc.n[0], tc.n[1], tc.n[2], t3);
+    for (int c = 0; c < 3; ++c) tc.nxb[c] = {-t3[c].r, -t3[c].i};
+    tc.an = cdot_r(tc.a, tc.n[0], tc.n[1], tc.n[2]);
+    tc.bn = cdot_r(tc.b, tc.n[0], tc.n[1], tc.n[2]);
+}
+
+// One (source, target) pair of the plain FP64 target-side adjoint: n_t .
+// grad_d phi for the source record r (kRecD). Unlit pairs give 0.
+template <int KIND, int T>
+__device__ __forceinline__ double adj_tgt_pair_fp64(const TgtConst &tc, const double *r, double k)
+{
+    const double dx = tc.p[0] - r[0], dy = tc.p[1] - r[1], dz = tc.p[2] - r[2];
+    if (KIND == kKindScalar) {
+        const double R = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / R;
+        double sn, cs;
+        sincos(k * R, &sn, &cs);
+        const cx<double> c = {cs * rinv, -T * sn * rinv};
+        const cx<double> y = cmul(cmul(tc.a[0], cx<double>{r[6], r[7]}), c);   // a = conj(g)
+        return (-y.r * rinv + T * k * y.i) * rinv * (tc.n[0] * dx + tc.n[1] * dy + tc.n[2] * dz);
+    }
+    const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    const double rinv = __ddiv_rn(1.0, R);
+    if (!lit_fp64(r + 3, dx, dy, dz, rinv)) return 0.0;
+    double sn, cs;
+    sincos(k * R, &sn, &cs);
+    const cx<double> J[3] = {{r[6], r[7]}, {r[8], r[9]}, {r[10], r[11]}};
+    const cx<double> M[3] = {{r[12], r[13]}, {r[14], r[15]}, {r[16], r[17]}};
+    const double ndn = tc.n[0] * dx + tc.n[1] * dy + tc.n[2] * dz;
+    return nf_adj_tgt_algebra<double, T, true>(dx, dy, dz, rinv, rinv / k, cs, T * sn, ndn, tc.a, tc.b, tc.nxa,
+                                               tc.nxb, tc.an, tc.bn, tc.n, J, M);
 }
 
 // Plain FP64 target-side displacement adjoint (near field, scalar).
@@ -441,21 +490,8 @@ po_adj_tgt_fp64_kernel(const double *__restrict__ srcd, long ns, const double *_
 {
     __shared__ double tile[kTileD * kRecD];
     const long ti = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    double p[3] = {0, 0, 0}, n[3] = {0, 0, 0};
-    cx<double> a[3] = {{0, 0}, {0, 0}, {0, 0}}, b[3] = {{0, 0}, {0, 0}, {0, 0}};
-    if (ti < nt)
-        for (int c = 0; c < 3; ++c) {
-            p[c] = tgt7[c * nt + ti];
-            n[c] = tgt7[(3 + c) * nt + ti];
-            a[c] = {gam[c * nt + ti], -gam[(3 + c) * nt + ti]};
-            b[c] = {gam[(6 + c) * nt + ti], -gam[(9 + c) * nt + ti]};
-        }
-    cx<double> nxa[3], nxb[3], t3[3];
-    ccross_r(a, n[0], n[1], n[2], t3);
-    for (int c = 0; c < 3; ++c) nxa[c] = {-t3[c].r, -t3[c].i};
-    ccross_r(b, n[0], n[1], n[2], t3);
-    for (int c = 0; c < 3; ++c) nxb[c] = {-t3[c].r, -t3[c].i};
-    const cx<double> an = cdot_r(a, n[0], n[1], n[2]), bn = cdot_r(b, n[0], n[1], n[2]);
+    TgtConst tc;
+    tgt_const(tgt7, gam, nt, ti < nt ? ti : 0, tc);
     double acc = 0.0;
     for (long base = 0; base < ns; base += kTileD) {
         const int cnt = (int)min((long)kTileD, ns - base);
@@ -463,32 +499,58 @@ po_adj_tgt_fp64_kernel(const double *__restrict__ srcd, long ns, const double *_
         for (int w = threadIdx.x; w < cnt * kRecD; w += blockDim.x) tile[w] = srcd[base * kRecD + w];
         __syncthreads();
         if (ti >= nt) continue;
-        for (int s = 0; s < cnt; ++s) {
-            const double *r = tile + s * kRecD;
-            const double dx = p[0] - r[0], dy = p[1] - r[1], dz = p[2] - r[2];
-            if (KIND == kKindScalar) {
-                const double R = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / R;
-                double sn, cs;
-                sincos(k * R, &sn, &cs);
-                const cx<double> c = {cs * rinv, -T * sn * rinv};
-                const cx<double> y = cmul(cmul(a[0], cx<double>{r[6], r[7]}), c);   // a = conj(g)
-                acc += (-y.r * rinv + T * k * y.i) * rinv * (n[0] * dx + n[1] * dy + n[2] * dz);
-                continue;
-            }
-            const double R = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                                                  __dmul_rn(dz, dz)));
-            const double rinv = __ddiv_rn(1.0, R);
-            if (lit_fp64(r + 3, dx, dy, dz, rinv) == false) continue;
-            double sn, cs;
-            sincos(k * R, &sn, &cs);
-            const cx<double> J[3] = {{r[6], r[7]}, {r[8], r[9]}, {r[10], r[11]}};
-            const cx<double> M[3] = {{r[12], r[13]}, {r[14], r[15]}, {r[16], r[17]}};
-            const double ndn = n[0] * dx + n[1] * dy + n[2] * dz;
-            acc += nf_adj_tgt_algebra<double, T, true>(dx, dy, dz, rinv, rinv / k, cs, T * sn, ndn, a, b, nxa, nxb,
-                                                       an, bn, n, J, M);
-        }
+        for (int s = 0; s < cnt; ++s) acc += adj_tgt_pair_fp64<KIND, T>(tc, tile + s * kRecD, k);
     }
     if (ti < nt) part[ti] = acc;
+}
+
+// The pairs the mixed adjoint left out as inside the tangent band: each is
+// decided by the reference's FP64 rounding and, if lit, its FP64 terms go
+// into the first source chunk's partials (currents; the source displacement
+// and the target displacement in the mixed kernel's units, per turn:
+// inv_kappa = 2 pi / k), before the epilogues. Order of the additions varies
+// between runs for a point with several such pairs (last bits there only).
+template <int KIND, int T, bool WANT_T>
+__global__ void __launch_bounds__(256)
+po_adj_band_fixup_kernel(BandList bl, long ns, const double *__restrict__ src7, const double *__restrict__ cur,
+                         int gmode, int ncx, int ncy, double fac_re, double fac_im, long nt,
+                         const double *__restrict__ tgt7, const double *__restrict__ gam, double k,
+                         double inv_kappa, double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err)
+{
+    const unsigned total = *bl.count;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && total > bl.cap) atomicExch(err, kErrBandOverflow);
+    const unsigned n = min(total, bl.cap);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int2 pr = bl.pairs[i];
+        const long si = pr.x, ti = pr.y;
+        double rec[kRecD];
+        src_record_d(si, ns, src7, cur, gmode, ncx, ncy, fac_re, fac_im, 0, rec);
+        SrcConst<double> sc;
+        for (int c = 0; c < 3; ++c) {
+            sc.n[c] = rec[3 + c];
+            sc.J[c] = {rec[6 + 2 * c], rec[7 + 2 * c]};
+            sc.M[c] = {rec[12 + 2 * c], rec[13 + 2 * c]};
+        }
+        src_const_finish<double, true>(sc);
+        double r[15];
+        if (KIND == kKindFF) ff_direction_d(tgt7, nt, ti, r);
+        else
+            for (int c = 0; c < 3; ++c) r[c] = tgt7[c * nt + ti];
+        for (int q = 0; q < 12; ++q) r[3 + q] = gam[(long)q * nt + ti];
+        double acc[kAccAdj];
+        for (int a = 0; a < kAccAdj; ++a) acc[a] = 0.0;
+        adj_src_pair_fp64<KIND, T>(rec, sc, r, k, acc);
+        for (int a = 0; a < kAccAdj; ++a) {
+            const double v = a < 12 ? acc[a] : acc[a] * inv_kappa;
+            if (v != 0.0) atomicAdd(&part[(long)a * ns + si], v);
+        }
+        if (WANT_T) {
+            TgtConst tc;
+            tgt_const(tgt7, gam, nt, ti, tc);
+            const double v = adj_tgt_pair_fp64<KIND, T>(tc, rec, k) * inv_kappa;
+            if (v != 0.0) atomicAdd(&gt[ti], v);
+        }
+    }
 }
 
 // ---------------------------------------------------------------- epilogues
@@ -559,6 +621,19 @@ void *adj_tgt_fp64_kernel(int kind, int t_sign)
                           : reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<kKindScalar, 1>);
     return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<kKindNF, -1>)
                       : reinterpret_cast<void *>(&po_adj_tgt_fp64_kernel<kKindNF, 1>);
+}
+
+void *adj_band_fixup_kernel(int kind, int t_sign, bool want_d, bool want_t)
+{
+    (void)want_d;   // the source displacement term is always kept (it is one partial row)
+    if (kind == kKindFF)
+        return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_band_fixup_kernel<kKindFF, -1, false>)
+                          : reinterpret_cast<void *>(&po_adj_band_fixup_kernel<kKindFF, 1, false>);
+    if (want_t)
+        return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_band_fixup_kernel<kKindNF, -1, true>)
+                          : reinterpret_cast<void *>(&po_adj_band_fixup_kernel<kKindNF, 1, true>);
+    return t_sign < 0 ? reinterpret_cast<void *>(&po_adj_band_fixup_kernel<kKindNF, -1, false>)
+                      : reinterpret_cast<void *>(&po_adj_band_fixup_kernel<kKindNF, 1, false>);
 }
 
 void *adj_cot_kernel() { return reinterpret_cast<void *>(&po_adj_cot_kernel); }

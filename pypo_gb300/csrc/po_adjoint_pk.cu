@@ -110,27 +110,49 @@ struct SrcC {
     float Jn[2], Mn[2];          // J.n_s, M.n_s
 };
 
-// One pair of targets against the thread's source. acc: 12 current
-// accumulators + the source displacement term; vt: the two targets' terms.
-template <int T, bool HAS_M, bool WANT_D, bool WANT_T>
-__device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const float2 *r, const SrcC &s)
+// The geometry of a target pair record against the thread's source, in the
+// split representation: S0 = |d_hi|^2 (exact), S1 the rest of |d|^2, 1/R
+// (approximate), R, d = t - s, and n_s . d. adj_nf_pair2 and
+// adj_nf_band_scan both use these, so the scan's band decision is the pair
+// loop's, bit for bit.
+struct AdjGeo2 {
+    float2 S0, S1, rinv0, Rh, dx, dy, dz, ndd;
+};
+
+__device__ __forceinline__ AdjGeo2 adj_geo2(const float2 *r, const SrcC &s)
 {
+    AdjGeo2 g;
     const float2 dhx = sub2(r[0], dup2(s.sh[0])), dhy = sub2(r[1], dup2(s.sh[1])), dhz = sub2(r[2], dup2(s.sh[2]));
     const float2 dlx = sub2(r[3], dup2(s.sl[0])), dly = sub2(r[4], dup2(s.sl[1])), dlz = sub2(r[5], dup2(s.sl[2]));
     const float2 two = dup2(2.0f);
-    const float2 S0 = fma2(dhz, dhz, fma2(dhy, dhy, mul2(dhx, dhx)));
-    const float2 S1 = fma2(dlz, fma2(two, dhz, dlz), fma2(dly, fma2(two, dhy, dly), mul2(dlx, fma2(two, dhx, dlx))));
-    const float2 R2 = add2(S0, S1);
-    const float2 rinv0 = make_float2(rsqrt_ftz(R2.x), rsqrt_ftz(R2.y));
-    const float2 Rh = mul2(R2, rinv0);
+    g.S0 = fma2(dhz, dhz, fma2(dhy, dhy, mul2(dhx, dhx)));
+    g.S1 = fma2(dlz, fma2(two, dhz, dlz), fma2(dly, fma2(two, dhy, dly), mul2(dlx, fma2(two, dhx, dlx))));
+    const float2 R2 = add2(g.S0, g.S1);
+    g.rinv0 = make_float2(rsqrt_ftz(R2.x), rsqrt_ftz(R2.y));
+    g.Rh = mul2(R2, g.rinv0);
+    g.dx = add2(dhx, dlx);
+    g.dy = add2(dhy, dly);
+    g.dz = add2(dhz, dlz);
+    g.ndd = fma2(dup2(s.n[2]), g.dz, fma2(dup2(s.n[1]), g.dy, mul2(dup2(s.n[0]), g.dx)));
+    return g;
+}
+
+// One pair of targets against the thread's source. acc: 12 current
+// accumulators + the source displacement term; vt: the two targets' terms.
+// band: set when a pair lies inside the tangent band (left out here; the
+// kernel lists it afterwards with adj_band_scan).
+template <int T, bool HAS_M, bool WANT_D, bool WANT_T>
+__device__ __forceinline__ void adj_nf_pair2(float2 *acc, float2 &vt, const float2 *r, const SrcC &s, bool &band)
+{
+    const AdjGeo2 g = adj_geo2(r, s);
+    const float2 S0 = g.S0, S1 = g.S1, rinv0 = g.rinv0, Rh = g.Rh, dx = g.dx, dy = g.dy, dz = g.dz, ndd = g.ndd;
     float2 sn, cs, tq;
     phase_sincos2(S0, S1, Rh, rinv0, sn, cs, tq);
     cs = flip_parity(cs, tq);   // cos, sin of k R
     sn = flip_parity(sn, tq);
-    const float2 dx = add2(dhx, dlx), dy = add2(dhy, dly), dz = add2(dhz, dlz);
-    const float2 ndd = fma2(dup2(s.n[2]), dz, fma2(dup2(s.n[1]), dy, mul2(dup2(s.n[0]), dx)));
-    const float2 w = fma2(dup2(kTangentTol32), Rh, ndd);
-    const float2 rinv = make_float2(w.x >= 0.0f ? rinv0.x : 0.0f, w.y >= 0.0f ? rinv0.y : 0.0f);
+    const float2 bw = mul2(dup2(kTangentBand), Rh);
+    band = band || (fabsf(ndd.x) < bw.x) || (fabsf(ndd.y) < bw.y);
+    const float2 rinv = make_float2(ndd.x >= bw.x ? rinv0.x : 0.0f, ndd.y >= bw.y ? rinv0.y : 0.0f);
     const float2 ex = mul2(dx, rinv), ey = mul2(dy, rinv), ez = mul2(dz, rinv);
     const float2 u = mul2(rinv, dup2(0.159154943091895336f));
     // c1 = Gu (t u + j(u^2 - 1)), C2 = -3 c1 - 2 j Gu, C3 = Gu (-u + j t)
@@ -319,22 +341,28 @@ __device__ __forceinline__ void adj_sc_pair2(float2 *acc, float2 &vt, const floa
 // LIT: the tile is proven lit for the CTA's sources (every pair passes the
 // illumination test), so the sign (-1)^q is set on the bits and the mask is
 // left out; the result is the same bits.
+__device__ __forceinline__ float2 adj_ff_ndr2(const float2 *r, const SrcC &s)
+{
+    return fma2(dup2(s.n[2]), r[20], fma2(dup2(s.n[1]), r[19], mul2(dup2(s.n[0]), r[18])));
+}
+
 template <int T, bool HAS_M, bool WANT_D, bool LIT>
-__device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const SrcC &s)
+__device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const SrcC &s, bool &band)
 {
     const float2 Ph = fma2(dup2(s.sh[2]), r[2], fma2(dup2(s.sh[1]), r[1], mul2(dup2(s.sh[0]), r[0])));
     const float2 Pl = fma2(dup2(s.sl[2]), r[20], fma2(dup2(s.sl[1]), r[19], fma2(dup2(s.sl[0]), r[18],
                       fma2(dup2(s.sh[2]), r[5], fma2(dup2(s.sh[1]), r[4], mul2(dup2(s.sh[0]), r[3]))))));
     float2 sn, cs, tq;
     ff_phase_sincos2(Ph, Pl, sn, cs, tq);
-    const float2 ndr = fma2(dup2(s.n[2]), r[20], fma2(dup2(s.n[1]), r[19], mul2(dup2(s.n[0]), r[18])));
+    const float2 ndr = adj_ff_ndr2(r, s);
     float2 gc, gs;                                          // G = (gc, gs)
     if (LIT) {
         gc = flip_parity(cs, tq);
         gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
     } else {
         const float2 one = flip_parity(dup2(1.0f), tq);
-        const float2 m = make_float2(ndr.x >= -kTangentTol32 ? one.x : 0.0f, ndr.y >= -kTangentTol32 ? one.y : 0.0f);
+        band = band || (fabsf(ndr.x) < kTangentBand) || (fabsf(ndr.y) < kTangentBand);
+        const float2 m = make_float2(ndr.x >= kTangentBand ? one.x : 0.0f, ndr.y >= kTangentBand ? one.y : 0.0f);
         gc = mul2(cs, m);
         gs = mul2(T > 0 ? neg2(sn) : sn, m);
     }
@@ -399,10 +427,45 @@ __global__ void po_adj_tgt_box_kernel(float2 *__restrict__ rec, long nt)
     }
 }
 
+// The rare path of a tile in which some pair fell inside the tangent band:
+// the thread's source is tested again against the tile's targets, with the
+// pair loop's operations, and each pair inside the band is listed for the
+// FP64 fixup (an idle source or padding target is only left out). tile:
+// cnt target pair records (RT float4 each), the first with target index
+// 2 * pfirst.
+template <int KIND, int RT>
+__device__ __forceinline__ void adj_band_scan(const float4 *tile, int cnt, long pfirst, const SrcC &s, long si,
+                                              long ns, long nt, BandList bl)
+{
+    if (si >= ns) return;
+#pragma unroll 1
+    for (int p = 0; p < cnt; ++p) {
+        float2 r[22];
+        if (KIND == kKindFF) {
+            const float4 v0 = tile[p * RT + 9], v1 = tile[p * RT + 10];   // float2 slots 18-21
+            r[18] = make_float2(v0.x, v0.y);
+            r[19] = make_float2(v0.z, v0.w);
+            r[20] = make_float2(v1.x, v1.y);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float4 v = tile[p * RT + c];
+                r[2 * c] = make_float2(v.x, v.y);
+                r[2 * c + 1] = make_float2(v.z, v.w);
+            }
+        }
+        const float2 nd = KIND == kKindFF ? adj_ff_ndr2(r, s) : adj_geo2(r, s).ndd;
+        const float2 bw = KIND == kKindFF ? dup2(kTangentBand) : mul2(dup2(kTangentBand), adj_geo2(r, s).Rh);
+        const long t0 = 2 * (pfirst + p);
+        if (fabsf(nd.x) < bw.x && t0 < nt) band_defer(bl, si, t0);
+        if (fabsf(nd.y) < bw.y && t0 + 1 < nt) band_defer(bl, si, t0 + 1);
+    }
+}
+
 template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
 __global__ void __launch_bounds__(kThreadsA, kMinBlocksA2)
 po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
-                 double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err, int boxes)
+                 double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err, int boxes, BandList bl)
 {
     static_assert(KIND != kKindFF || !WANT_T, "far-field targets do not move");
     constexpr int RT = adj2_rec(KIND, HAS_M, WANT_T);
@@ -513,6 +576,7 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
         float2 acc[kAccAdj];
 #pragma unroll
         for (int a = 0; a < kAccAdj; ++a) acc[a] = make_float2(0.f, 0.f);
+        bool band = false;   // a pair of this tile fell inside the tangent band
         // block-uniform: the tile's direction box (in the first three pair
         // records, as po_adj_tgt_box_kernel wrote it) against the CTA's normals
         [[maybe_unused]] bool lit = false;
@@ -544,7 +608,7 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
                             rec[2 * c] = make_float2(v.x, v.y);
                             rec[2 * c + 1] = make_float2(v.z, v.w);
                         }
-                        adj_ff_pair2<T, HAS_M, WANT_D, LIT>(acc, rec, s);
+                        adj_ff_pair2<T, HAS_M, WANT_D, LIT>(acc, rec, s, band);
                     }
                 };
                 if (lit)
@@ -562,9 +626,10 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
                         rec[2 * c + 1] = make_float2(v.z, v.w);
                     }
                     float2 vt = make_float2(0.f, 0.f);
-                    if (KIND == kKindNF) adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s);
+                    if (KIND == kKindNF)
+                        adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s, band);
                     else if (KIND == kKindScalar) adj_sc_pair2<T, WANT_D, WANT_T>(acc, vt, rec, s);
-                    else adj_ff_pair2<T, HAS_M, WANT_D, false>(acc, rec, s);
+                    else adj_ff_pair2<T, HAS_M, WANT_D, false>(acc, rec, s, band);
                     if (WANT_T) vbuf[(p - fb) * kThreadsA + threadIdx.x] = vt;
                 }
             }
@@ -604,6 +669,7 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
             float &l = lo[a * kThreadsA + threadIdx.x];
             l = __fadd_rn(l, e);
         }
+        if (KIND != kKindScalar && band) adj_band_scan<KIND, RT>(tile, cnt, pfirst, s, si, ns, nt, bl);
         __syncthreads();
         if (threadIdx.x == 0 && it + kStages < ntiles) issue(it + kStages);
     }

@@ -23,6 +23,16 @@ cudaStream_t g_streams[64] = {};
 thread_local double t_extent = 0.0;
 
 // Private non-blocking stream of the host-buffer entry points, one per device.
+// The message of a device error code of the kernels (kErr* in po_kernels.cuh).
+std::string device_error_text(int code)
+{
+    const char *what = code == po::kErrWaitTimeout     ? "a kernel gave up waiting for a tile copy"
+                       : code == po::kErrBandOverflow ? "more near-tangent pairs than the band list holds"
+                       : code == po::kErrRngBound     ? "the device normal generator ran past its bound"
+                                                      : "a kernel reported an error";
+    return std::string(what) + " (device error " + std::to_string(code) + "); results are invalid";
+}
+
 int lib_stream(cudaStream_t *s)
 {
     int dev = 0;
@@ -189,8 +199,7 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
     CK(cudaMemcpyAsync(out, d_out, sizeof(double) * nout * nt, cudaMemcpyDeviceToHost, s));
     rc = po::read_device_error(s, &code);   // the call's one synchronisation
     if (!rc && precision == 0) t_extent = *a.extent_host;
-    if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
-                                      std::to_string(code) + "); results are invalid");
+    if (!rc && code) rc = fail(4, device_error_text(code));
 done:
     if (d_src) cudaFreeAsync(d_src, s);
     if (d_cur) cudaFreeAsync(d_cur, s);
@@ -499,8 +508,7 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     if (grad_dt && nt > 0) CK(cudaMemcpyAsync(grad_dt, d_gt, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
     rc = po::read_device_error(s, &code);   // the call's one synchronisation
     if (!rc && precision == 0) t_extent = *ext;
-    if (!rc && code) rc = fail(4, "a kernel gave up waiting for a tile copy (device error " +
-                                      std::to_string(code) + "); results are invalid");
+    if (!rc && code) rc = fail(4, device_error_text(code));
 done:
     for (double *p : {d_src, d_cur, d_tgt, d_cot, d_gc, d_gs, d_gt})
         if (p) cudaFreeAsync(p, s);

@@ -202,6 +202,64 @@ __device__ __forceinline__ void split_hi_lo(double x, const Frame &fr, float &h,
     l = (float)(x - hd);
 }
 
+// ------------------------------------- the reference's illumination decision
+//
+// The reference skips a source when its FP64 n . R_hat < 0 (near field;
+// far field n . r_hat < 0), with R_hat = d (1/R) and the dot product summed
+// left to right (src/CPU/Propagation.h:977-1144, :1656-1781). The FP64
+// kernels repeat that rounding exactly; the mixed kernels use it for the
+// pairs their FP32 test cannot decide (kTangentBand), through the band list.
+__device__ __forceinline__ bool lit_fp64(const double *n, double dx, double dy, double dz, double rinv)
+{
+    const double ndr = __dadd_rn(__dadd_rn(__dmul_rn(n[0], __dmul_rn(dx, rinv)), __dmul_rn(n[1], __dmul_rn(dy, rinv))),
+                                 __dmul_rn(n[2], __dmul_rn(dz, rinv)));
+    return !(ndr < 0.0);
+}
+
+// A pair inside the tangent band: listed for the FP64 fixup (one atomic; the
+// rare branch of the pair loops). A full list drops the entry; the fixup
+// then reports the overflow.
+__device__ __forceinline__ void band_defer(const BandList &bl, long si, long ti)
+{
+    const unsigned i = atomicAdd(bl.count, 1u);
+    if (i < bl.cap) bl.pairs[i] = make_int2((int)si, (int)ti);
+}
+
+// One source's FP64 record (kRecD doubles: x y z nx ny nz, J' (re, im) x y z,
+// M' likewise; scalar: S' in the J'x slot): the currents times the trapezoid
+// weight, the area and the complex factor (fac_re, fac_im).
+__device__ __forceinline__ void src_record_d(long i, long ns, const double *src7, const double *cur, int gmode,
+                                             int ncx, int ncy, double fac_re, double fac_im, int scalar, double *o)
+{
+    for (int c = 0; c < 6; ++c) o[c] = src7[c * ns + i];
+    const double w = trap_weight(i, gmode, ncx, ncy) * src7[6 * ns + i];
+    const double fr_ = fac_re * w, fi_ = fac_im * w;
+    if (scalar) {
+        const double re = cur[i], im = cur[ns + i];
+        o[6] = fr_ * re - fi_ * im;
+        o[7] = fr_ * im + fi_ * re;
+        for (int q = 8; q < kRecD; ++q) o[q] = 0.0;
+        return;
+    }
+    for (int q = 0; q < 6; ++q) {
+        const int grp = q / 3, ax = q % 3;
+        const double re = cur[(grp * 6 + ax) * ns + i];
+        const double im = cur[(grp * 6 + 3 + ax) * ns + i];
+        o[6 + 2 * q] = fr_ * re - fi_ * im;
+        o[7 + 2 * q] = fr_ * im + fi_ * re;
+    }
+}
+
+// The direction of far-field target i from its (polar, azimuth), as the FP64
+// kernels form it.
+__device__ __forceinline__ void ff_direction_d(const double *tgt7, long nt, long i, double *p)
+{
+    const double th = tgt7[i], ph = tgt7[nt + i];
+    p[0] = cos(ph) * sin(th);
+    p[1] = sin(ph) * sin(th);
+    p[2] = cos(th);
+}
+
 // --------------------------------------------------- EHP reflection, generic
 //
 // The reflected field of mode EHP (reference src/CPU/Propagation.h:840-913,

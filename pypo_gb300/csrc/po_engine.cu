@@ -419,6 +419,10 @@ int mixed_prepare(const RunArgs &a, Scratch &sc, MixedPlan &p)
     if ((rc = sc.get(&p.bbox, (size_t)kBboxBlocks * 6)) || (rc = sc.get(&p.frame, 1)) ||
         (rc = sc.get(&p.tgtpk, (size_t)nt * 2)))
         return rc;
+    if (!scalar) {
+        p.band.cap = sc.band_cap();
+        if ((rc = sc.get(&p.band.pairs, p.band.cap)) || (rc = sc.get(&p.band.count, 1))) return rc;
+    }
     if (p.far) {
         // the far field's tiles along the sources' Hilbert order
         const long n1 = std::max(ns, 1L);
@@ -493,7 +497,10 @@ int mixed_launch(const RunArgs &a, MixedPlan &p, int *err)
     if (!rc) rc = launch(pack_tgt_kernel(), dim3(nblk_t), dim3(256), ptargs, 0, s);
     const float4 *srcc = p.srcpk, *tgtc = p.tgtpk;
     long ntiles = ns > 0 ? p.tiles : 0;
-    void *margs[] = {&srcc, p.far ? (void *)&ntiles : (void *)&ns, &p.chunk, &tgtc, &nt, &p.part, &err, &boxes};
+    const int *sorted = p.order ? p.order + std::max(ns, 1L) : nullptr;   // far field: curve position -> source
+    if (!rc && p.band.count) PO_CK_RC(cudaMemsetAsync(p.band.count, 0, sizeof(unsigned), s));
+    void *margs[] = {&srcc, p.far ? (void *)&ntiles : (void *)&ns, &p.chunk, &tgtc, &nt, &p.part, &err, &boxes,
+                     &p.band, &ns, &sorted};
     timing_mark(s, true);
     if (!rc) {
         if (p.far)
@@ -504,6 +511,13 @@ int mixed_launch(const RunArgs &a, MixedPlan &p, int *err)
                         margs, pk_smem_bytes(p.kind), s);
     }
     timing_mark(s, false);
+    if (!rc && p.band.count && ns > 0) {
+        // the near-tangent pairs, decided and summed in FP64 into chunk 0
+        double k = a.k;
+        void *xargs[] = {&p.band, &ns, &src7, &cur, &gmode, &ncx, &ncy, &p.fac_re, &p.fac_im, &nt, &tgt7, &k, &t,
+                         &p.part, &err};
+        rc = launch(band_fixup_kernel(p.kind), dim3(kFixupBlocks), dim3(256), xargs, 0, s);
+    }
     int nspl = (int)p.nsplit;
     void *eargs[] = {&mode, &nspl, &nt, &p.part, &tgt7, &t, &p.zeta_inv, &out};
     if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
@@ -665,6 +679,15 @@ int run_adjoint(const AdjArgs &a)
     const unsigned ntile_a = (unsigned)((npair + adj_pk_pairs_per_tile() - 1) / adj_pk_pairs_per_tile());
     if (!rc && boxes) rc = launch(adj_tgt_box_kernel(), dim3(ntile_a), dim3(32), tbargs, 0, s);
     if (want_t) PO_CK_RC(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
+    BandList band{nullptr, nullptr, 0};   // near-tangent pairs (not the scalar kind)
+    if (!rc && kind != kKindScalar) {
+        band.cap = kBandCap;
+        if ((rc = salloc(&band.pairs, band.cap, s, owned)) || (rc = salloc(&band.count, 1, s, owned))) {
+            sfree(owned, s);
+            return rc;
+        }
+        PO_CK_RC(cudaMemsetAsync(band.count, 0, sizeof(unsigned), s));
+    }
     void *fk = adj_pk_kernel(kind, ts, has_m, want_d, want_t);
     const int smem2 = adj_pk_smem_bytes(kind, has_m, want_t);
     int occ2 = 1;
@@ -689,10 +712,17 @@ int run_adjoint(const AdjArgs &a)
     double *part = nullptr;
     if (!rc && (rc = salloc(&part, (size_t)split * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
     const float4 *srcc = srcpk, *trc2 = reinterpret_cast<const float4 *>(trec2);
-    void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err, &boxes};
+    void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err, &boxes, &band};
     timing_mark(s, true);
     if (!rc) rc = launch(fk, dim3((unsigned)nsb, (unsigned)split), dim3(kThreadsA), fargs, smem2, s);
     timing_mark(s, false);
+    if (!rc && band.count) {
+        // the near-tangent pairs, decided and summed in FP64 into chunk 0 (and gt)
+        double inv_kappa = 1.0 / kappa;
+        void *xargs[] = {&band, &ns, &src7, &cur, &gmode, &ncx, &ncy, &fac_re, &fac_im, &nt, &tgt7, &gam, &k,
+                         &inv_kappa, &part, &gt, &err};
+        rc = launch(adj_band_fixup_kernel(kind, ts, want_d, want_t), dim3(kFixupBlocks), dim3(256), xargs, 0, s);
+    }
     int nspl = (int)split;
     double dsc = far ? kappa : -kappa;
     void *eargs[] = {(void *)&kind, &nspl, &ns, &part, &src7, &gmode, &ncx, &ncy, &fac_re, &fac_im, &dsc,

@@ -203,6 +203,44 @@ po_ff_pack_kernel(long ns, const int *__restrict__ order, const double *__restri
 
 // ---------------------------------------------------------------- main kernel
 
+// n_s . r_hat for a pair record's two sources (normals in float2 slots 9-11)
+// and one direction duplicated into both lanes; the pair loop and the band
+// scan both use it, so the scan's decision is the loop's, bit for bit.
+__device__ __forceinline__ float2 ff_ndr2(const float2 *r, const float2 *rf)
+{
+    return fma2(r[11], rf[2], fma2(r[10], rf[1], mul2(r[9], rf[0])));
+}
+
+// The rare path of a tile in which some pair fell inside the tangent band:
+// the thread's pairs are tested again and each one inside the band is
+// listed for the FP64 fixup under the source's original index (curve
+// position -> order); padding sources and idle directions are only left
+// out. recs: the tile's kTile / 2 pair records (R4 float4 each); pos0: the
+// curve position of its first source.
+template <int TP, int R4>
+__device__ __forceinline__ void ff_band_scan(const float4 *recs, long pos0, const float2 (*rf)[3], long tbase, long ns,
+                                             long nt, const int *__restrict__ order, BandList bl)
+{
+#pragma unroll 1
+    for (int s = 0; s < kTile / 2; ++s) {
+        float2 r[12];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float4 v = recs[s * R4 + q];
+            r[2 * q] = make_float2(v.x, v.y);
+            r[2 * q + 1] = make_float2(v.z, v.w);
+        }
+        const long pos = pos0 + 2 * s;
+#pragma unroll
+        for (int j = 0; j < TP; ++j) {
+            const long ti = tbase + (long)j * kThreads;
+            const float2 ndr = ff_ndr2(r, rf[j]);
+            if (fabsf(ndr.x) < kTangentBand && ti < nt && pos < ns) band_defer(bl, order[pos], ti);
+            if (fabsf(ndr.y) < kTangentBand && ti < nt && pos + 1 < ns) band_defer(bl, order[pos + 1], ti);
+        }
+    }
+}
+
 // Grid = (direction blocks of 2 * kThreads, tile chunks). Every thread owns
 // two directions (lanes of the per-tile phase); each pair record's two
 // sources are the two lanes of every packed operation of the pair loop.
@@ -211,7 +249,8 @@ po_ff_pack_kernel(long ns, const int *__restrict__ order, const double *__restri
 template <int T, bool HAS_M>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
 po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const float4 *__restrict__ tgt, long nt,
-             double *__restrict__ part, int *__restrict__ err, int boxes)
+             double *__restrict__ part, int *__restrict__ err, int boxes, BandList bl, long ns,
+             const int *__restrict__ order)
 {
     constexpr int R4 = ff_rec4(HAS_M), T4 = ff_tile4(HAS_M), TP = 2;
     constexpr int NA = HAS_M ? 12 : 6;   // accumulators in use: S_J (re xyz, im xyz), then S_M
@@ -325,6 +364,7 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
 #pragma unroll
             for (int a = 0; a < NA; ++a) acc[j][a] = make_float2(0.f, 0.f);
 
+        bool band = false;   // a pair of this tile fell inside the tangent band
         // VAR 0: narrow tile proven lit (M = 0); 1: narrow tile; 2: wide tile
         auto pairs = [&](auto var_c) {
             constexpr int VAR = decltype(var_c)::value;
@@ -371,9 +411,11 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
                         gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
                     }
                     if (VAR != 0) {
-                        const float2 ndr = fma2(r[11], rf[j][2], fma2(r[10], rf[j][1], mul2(r[9], rf[j][0])));
-                        const float2 m = make_float2(ndr.x >= -kTangentTol32 ? 1.0f : 0.0f,
-                                                     ndr.y >= -kTangentTol32 ? 1.0f : 0.0f);
+                        // lit when n . r >= the band, not when below minus it; a pair
+                        // inside it is left out here and listed afterwards (ff_band_scan)
+                        const float2 ndr = ff_ndr2(r, rf[j]);
+                        band = band || (fabsf(ndr.x) < kTangentBand) || (fabsf(ndr.y) < kTangentBand);
+                        const float2 m = make_float2(ndr.x >= kTangentBand ? 1.0f : 0.0f, ndr.y >= kTangentBand ? 1.0f : 0.0f);
                         gc = mul2(gc, m);
                         gs = mul2(gs, m);
                     }
@@ -443,6 +485,7 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
                     l1 = __fadd_rn(l1, e);
                 }
         }
+        if (band) ff_band_scan<TP, R4>(tile + kFFHead, (t0 + it) * kTile, rf, tbase, ns, nt, order, bl);
         __syncthreads();
         if (threadIdx.x == 0 && it + kStages < ntl) issue(it + kStages);
     }

@@ -81,6 +81,8 @@ public:
     virtual ~Scratch() = default;
     virtual int take(void **p, size_t bytes) = 0;
     virtual size_t room() const = 0;
+    // entries of the list of near-tangent pairs a call takes (BandList)
+    virtual unsigned band_cap() const { return kBandCap; }
     template <typename T>
     int get(T **p, size_t count)
     {
@@ -109,6 +111,7 @@ struct MixedPlan {
     int *order = nullptr;
     void *sort_tmp = nullptr;
     size_t sort_bytes = 0;
+    BandList band{nullptr, nullptr, 0};   // near-tangent pairs (not the scalar kind)
 };
 int mixed_prepare(const RunArgs &a, Scratch &sc, MixedPlan &p);
 int mixed_launch(const RunArgs &a, MixedPlan &p, int *err);

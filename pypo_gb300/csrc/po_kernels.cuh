@@ -74,15 +74,30 @@ constexpr int kRecD = 18;       // x y z nx ny nz, J' 6, M' 6 (doubles)
 constexpr int kBboxThreads = 256;
 constexpr int kBboxBlocks = 152;
 
-// Illumination test of the mixed-precision kernels: n . R_hat >= -tol, a
-// few FP32 ulps of slack so that pairs tangent in exact arithmetic (n . d == 0,
-// which the reference keeps when its FP64 rounding gives +0) are kept. The
-// FP64 kernel instead repeats the reference's own rounding.
-constexpr float kTangentTol32 = 5e-7f;
+// Illumination test of the mixed-precision kernels: a pair with
+// n . R_hat >= kTangentBand is lit, one below -kTangentBand is not (the FP32
+// test's own error is below 4.2e-7). A pair inside the band is left out of
+// the FP32 sums and listed; a fixup kernel then decides it with the
+// reference's FP64 rounding, as the FP64 kernels decide every pair, and adds
+// its FP64 term if it is lit. The lit-tile proofs keep a margin of 1e-5.
+constexpr float kTangentBand = 1e-6f;
+
+// The list of pairs inside the band: (source, target) entries, their count
+// (zeroed before the main kernel) and the capacity; a count above the
+// capacity is reported as kErrBandOverflow by the fixup.
+struct BandList {
+    int2 *pairs;
+    unsigned *count;
+    unsigned cap;
+};
+constexpr unsigned kBandCap = 1u << 20;        // entries, calls on the library's pool
+constexpr unsigned kBandCapStatic = 1u << 14;  // entries, the allocation-free entry
+constexpr unsigned kFixupBlocks = 152;         // grid of the fixup kernels (grid-stride over the list)
 
 // Device error codes (written to the call's error word).
 constexpr int kErrWaitTimeout = 101;
 constexpr int kErrRngBound = 102;   // the device normal generator ran past its bound (never expected)
+constexpr int kErrBandOverflow = 103;   // more near-tangent pairs than the band list holds
 
 // Frame of the split representation: positions in turns (mm * kappa),
 // relative to origin o, hi parts on multiples of q.
@@ -132,6 +147,8 @@ void *pack_tgt_kernel();
 void *pack_src_d_kernel();
 void *epilogue_kernel();
 void *fp32_probe_kernel();
+void *band_fixup_kernel(int kind);
+void *adj_band_fixup_kernel(int kind, int t_sign, bool want_d, bool want_t);
 void *wait_selftest_kernel();
 void *adj_src_fp64_kernel(int kind, int t_sign);
 void *adj_tgt_fp64_kernel(int kind, int t_sign);
