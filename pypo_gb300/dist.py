@@ -14,6 +14,9 @@ target side are added with one all_reduce (the one real exchange step).
 A source shard is not a grid any more, so it goes as a point cloud
 (gmode -1) with the trapezoid weights folded into its area row.
 
+The *_dev variants keep everything on each rank's device: torch tensors in,
+NCCL collectives on device buffers, torch tensors out (no host round trip).
+
 `max_over_ranks` is the timing reduction used by bench.py.
 """
 import numpy as np
@@ -129,6 +132,93 @@ def adjoint_sharded(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0,
             dt = dt.cuda()
         dist.all_reduce(dt, op=dist.ReduceOp.SUM)
         out["dt"] = dt.cpu().numpy()
+    return out
+
+
+def _gather_cols(local, n, rank, world):
+    """All-gather a (rows, shard) tensor of contiguous column shards into
+    (rows, n), on local's device (the collective runs on that device)."""
+    import torch
+    import torch.distributed as dist
+    width = n // world + (1 if n % world else 0)
+    b, e = shard_range(n, rank, world)
+    buf = torch.zeros((local.shape[0], width), dtype=local.dtype, device=local.device)
+    buf[:, :e - b] = local
+    gathered = [torch.empty_like(buf) for _ in range(world)]
+    dist.all_gather(gathered, buf)
+    parts = []
+    for r in range(world):
+        rb, re = shard_range(n, r, world)
+        parts.append(gathered[r][:, :re - rb])
+    return torch.cat(parts, dim=1)
+
+
+def propagate_sharded_dev(mode, src7, cur, gmode, ncx, ncy, tgt7, k, epsilon=1.0, t_dir=-1.0, precision="mixed",
+                          m_zero=False, compute=None):
+    """Device-resident propagate_sharded: src7, cur, tgt7 are float64 torch
+    tensors on this rank's device, identical on every rank. `compute`
+    (default: pypo_gb300.engine.propagate_dev) maps the call on a target shard
+    (a contiguous 7-row tensor) to its (n_out, shard) tensor. Returns the full
+    (n_out, nt) output on every rank's device."""
+    import torch.distributed as dist
+    from . import engine
+    if compute is None:
+        def compute(*a):
+            return engine.propagate_dev(*a, precision=precision, m_zero=m_zero)
+    rank, world = dist.get_rank(), dist.get_world_size()
+    nt = tgt7.shape[1]
+    b, e = shard_range(nt, rank, world)
+    local = compute(mode, src7, cur, gmode, ncx, ncy, tgt7[:, b:e].contiguous(), k, epsilon, t_dir)
+    return _gather_cols(local, nt, rank, world)
+
+
+def as_point_cloud_dev(src7, gmode, ncx, ncy):
+    """as_point_cloud for a torch tensor, on its device."""
+    import torch
+    out = src7.clone()
+    n = out.shape[1]
+    if gmode >= 0:
+        i = torch.arange(n, device=out.device)
+        xu, yv = i // ncy, i % ncy
+        w = torch.ones(n, dtype=out.dtype, device=out.device)
+        w = torch.where((xu == 0) | (xu == ncx - 1), 0.5 * w, w)
+        if gmode != 1:
+            w = torch.where((yv == 0) | (yv == ncy - 1), 0.5 * w, w)
+        out[6] *= w
+    return out
+
+
+def adjoint_sharded_dev(mode, src7, cur, gmode, ncx, ncy, tgt7, k, cot, epsilon=1.0, t_dir=-1.0,
+                        precision="mixed", m_zero=False, compute=None):
+    """Device-resident adjoint_sharded: float64 torch tensors on this rank's
+    device, identical on every rank. `compute` (default: engine.adjoint_dev
+    into fresh device buffers) maps (mode, src7, cur, gmode, ncx, ncy, tgt7,
+    k, cot, epsilon, t_dir) on a source shard (a point cloud) to the dict
+    {"cur", "ds", "dt"} of device tensors. Returns the full gradients on every
+    rank's device ("dt" is None for the far field); the target side is one
+    all_reduce of the ranks' partial sums."""
+    import torch
+    import torch.distributed as dist
+    from . import engine
+    if compute is None:
+        def compute(md, s7, c, gm, nx, ny, t7, kk, ct, eps, t):
+            gc = torch.empty_like(c)
+            gs = torch.empty(s7.shape[1], dtype=torch.float64, device=s7.device)
+            gt = None if md == "FF" else torch.empty(t7.shape[1], dtype=torch.float64, device=t7.device)
+            engine.adjoint_dev(md, s7, c, gm, nx, ny, t7, kk, ct, eps, t, precision=precision, m_zero=m_zero,
+                               grad_cur=gc, grad_ds=gs, grad_dt=gt)
+            return {"cur": gc, "ds": gs, "dt": gt}
+    rank, world = dist.get_rank(), dist.get_world_size()
+    ns = src7.shape[1]
+    b, e = shard_range(ns, rank, world)
+    pts = as_point_cloud_dev(src7, gmode, ncx, ncy)
+    g = compute(mode, pts[:, b:e].contiguous(), cur[:, b:e].contiguous(), -1, 0, 0, tgt7, k, cot, epsilon, t_dir)
+    out = {"cur": _gather_cols(g["cur"], ns, rank, world), "ds": _gather_cols(g["ds"][None, :], ns, rank, world)[0],
+           "dt": None}
+    if mode != "FF":
+        dt = g["dt"].clone()
+        dist.all_reduce(dt, op=dist.ReduceOp.SUM)
+        out["dt"] = dt
     return out
 
 

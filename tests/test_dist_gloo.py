@@ -141,3 +141,60 @@ def test_sharded_adjoint_world2_gloo(tmp_path, oracle_mod, lib):
     for r in range(2):
         ok = np.load(tmp_path / f"adj_rank{r}.npy")
         assert ok.all(), f"rank {r}: {ok}"
+
+
+def _dev_worker(rank, world, port, result_dir):
+    """The device-resident variants on CPU tensors (gloo), with the oracle's
+    forward and FP64 adjoint as each rank's compute."""
+    import torch
+    import torch.distributed as dist
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from oracle import oracle as O
+    from pypo_gb300 import dist as D
+    from pypo_gb300 import engine, surfaces as SF
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    T = torch.from_numpy
+    rng = np.random.default_rng(9)
+    s7 = engine.generate_grid(SF.plane([5, 4], gmode=0, lims_a=[-1.0, 1.0]))
+    t7 = np.zeros((7, 23))
+    t7[0:2] = rng.uniform(-1, 1, (2, 23))
+    t7[2] = 2.5
+    t7[5] = -1.0
+    t7[6] = 1.0
+    cur = rng.standard_normal((12, s7.shape[1]))
+    cot = rng.standard_normal((12, 23))
+    ok = []
+    fwd = lambda m, a, c, g, x, y, t, k, e, d: T(O.run(m, a.numpy(), c.numpy(), g, x, y, t.numpy(), k, e, d,
+                                                        nthreads=1))
+    out = D.propagate_sharded_dev("EH", T(s7), T(cur), 0, 5, 4, T(t7), 4.0, compute=fwd)
+    ok.append(isinstance(out, torch.Tensor) and np.array_equal(out.numpy(),
+                                                                O.run("EH", s7, cur, 0, 5, 4, t7, 4.0, nthreads=1)))
+
+    def adj(m, a, c, g, x, y, t, k, ct, e, d):
+        r = O.adjoint(m, a.numpy(), c.numpy(), g, x, y, t.numpy(), k, ct.numpy(), e, d, nthreads=1)
+        return {n: T(v) for n, v in r.items()}
+    got = D.adjoint_sharded_dev("EH", T(s7), T(cur), 0, 5, 4, T(t7), 4.0, T(cot), compute=adj)
+    ref = O.adjoint("EH", s7, cur, 0, 5, 4, t7, 4.0, cot, nthreads=1)
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    for name in ("cur", "ds", "dt"):
+        ok.append(isinstance(got[name], torch.Tensor) and rel(got[name].numpy(), ref[name]) <= 1e-12)
+    pc = D.as_point_cloud_dev(T(s7), 0, 5, 4).numpy()
+    ok.append(np.array_equal(pc, D.as_point_cloud(s7, 0, 5, 4)))
+    np.save(os.path.join(result_dir, f"dev_rank{rank}.npy"), np.array(ok, dtype=bool))
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_device_resident_sharding_gloo(tmp_path, oracle_mod, lib, world):
+    """propagate_sharded_dev / adjoint_sharded_dev: tensors in and out, the
+    gather and the all_reduce on the tensors' device; uneven shards at world 3."""
+    import torch.multiprocessing as mp
+    port = _free_port()
+    mp.start_processes(_dev_worker, args=(world, port, str(tmp_path)), nprocs=world, join=True,
+                       start_method="spawn")
+    for r in range(world):
+        ok = np.load(tmp_path / f"dev_rank{r}.npy")
+        assert ok.all(), f"rank {r}: {ok}"
