@@ -346,21 +346,33 @@ __device__ __forceinline__ float2 adj_ff_ndr2(const float2 *r, const SrcC &s)
     return fma2(dup2(s.n[2]), r[20], fma2(dup2(s.n[1]), r[19], mul2(dup2(s.n[0]), r[18])));
 }
 
-template <int T, bool HAS_M, bool WANT_D, bool LIT>
+template <int T, bool HAS_M, bool WANT_D, bool LIT, bool WIDE>
 __device__ __forceinline__ void adj_ff_pair2(float2 *acc, const float2 *r, const SrcC &s, bool &band)
 {
-    const float2 Ph = fma2(dup2(s.sh[2]), r[2], fma2(dup2(s.sh[1]), r[1], mul2(dup2(s.sh[0]), r[0])));
-    const float2 Pl = fma2(dup2(s.sl[2]), r[20], fma2(dup2(s.sl[1]), r[19], fma2(dup2(s.sl[0]), r[18],
-                      fma2(dup2(s.sh[2]), r[5], fma2(dup2(s.sh[1]), r[4], mul2(dup2(s.sh[0]), r[3]))))));
-    float2 sn, cs, tq;
-    ff_phase_sincos2(Ph, Pl, sn, cs, tq);
+    // the phase of the source's offset w from its tile centre (the centre's
+    // phase is already in the cotangents): narrow tiles p = r.w in FP32
+    // (|w| <= kFFNarrow turns), reduced exactly to the nearest turn; wide
+    // tiles from the split offset, reduced in half turns with a parity
+    float2 sn, cs, tq = dup2(0.0f);
+    if (WIDE) {
+        const float2 Ph = fma2(dup2(s.sh[2]), r[2], fma2(dup2(s.sh[1]), r[1], mul2(dup2(s.sh[0]), r[0])));
+        const float2 Pl = fma2(dup2(s.sl[2]), r[20], fma2(dup2(s.sl[1]), r[19], fma2(dup2(s.sl[0]), r[18],
+                          fma2(dup2(s.sh[2]), r[5], fma2(dup2(s.sh[1]), r[4], mul2(dup2(s.sh[0]), r[3]))))));
+        ff_phase_sincos2(Ph, Pl, sn, cs, tq);
+    } else {
+        const float2 magic = dup2(12582912.0f), twopi = dup2(6.28318530717958648f);
+        const float2 P = fma2(dup2(s.sh[2]), r[20], fma2(dup2(s.sh[1]), r[19], mul2(dup2(s.sh[0]), r[18])));
+        const float2 ang = mul2(sub2(P, sub2(add2(P, magic), magic)), twopi);
+        __sincosf(ang.x, &sn.x, &cs.x);
+        __sincosf(ang.y, &sn.y, &cs.y);
+    }
     const float2 ndr = adj_ff_ndr2(r, s);
     float2 gc, gs;                                          // G = (gc, gs)
     if (LIT) {
-        gc = flip_parity(cs, tq);
-        gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
+        gc = WIDE ? flip_parity(cs, tq) : cs;
+        gs = WIDE ? flip_parity(T > 0 ? neg2(sn) : sn, tq) : (T > 0 ? neg2(sn) : sn);
     } else {
-        const float2 one = flip_parity(dup2(1.0f), tq);
+        const float2 one = WIDE ? flip_parity(dup2(1.0f), tq) : dup2(1.0f);
         band = band || (fabsf(ndr.x) < kTangentBand) || (fabsf(ndr.y) < kTangentBand);
         const float2 m = make_float2(ndr.x >= kTangentBand ? one.x : 0.0f, ndr.y >= kTangentBand ? one.y : 0.0f);
         gc = mul2(cs, m);
@@ -427,6 +439,31 @@ __global__ void po_adj_tgt_box_kernel(float2 *__restrict__ rec, long nt)
     }
 }
 
+// Far field: one stage's pair record of two directions (lanes), its
+// cotangents gS_J, gS_M (slots 6-17, (re, im) per axis) multiplied in place by
+// conj(e^{-t j k r.c}) for the CTA's tile centre c (hi xyz, lo xyz, turns).
+// With s = c + w, conj(G) g = conj(G_w) (conj(G_c) g), so the pair loop needs
+// only the offset's phase. r.c in split form: hi products exact (r hi on
+// 2^-11, c hi on the frame's quantum), the rest in one FP32 sum, reduced
+// exactly to half turns, as the forward's tile phase.
+template <int T>
+__device__ __forceinline__ void ff_rotate_cot(float4 *rec4, const float *c)
+{
+    float2 *r = reinterpret_cast<float2 *>(rec4);
+    const float2 Ph = fma2(dup2(c[2]), r[2], fma2(dup2(c[1]), r[1], mul2(dup2(c[0]), r[0])));
+    const float2 Pl = fma2(dup2(c[5]), r[20], fma2(dup2(c[4]), r[19], fma2(dup2(c[3]), r[18],
+                      fma2(dup2(c[2]), r[5], fma2(dup2(c[1]), r[4], mul2(dup2(c[0]), r[3]))))));
+    float2 sn, cs, tq;
+    ff_phase_sincos2(Ph, Pl, sn, cs, tq);
+    const float2 gc = flip_parity(cs, tq), gs = flip_parity(T > 0 ? neg2(sn) : sn, tq);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const float2 re = r[6 + 2 * q], im = r[7 + 2 * q];
+        r[6 + 2 * q] = fma2(gc, re, mul2(gs, im));
+        r[7 + 2 * q] = fma2(gc, im, mul2(neg2(gs), re));
+    }
+}
+
 // The rare path of a tile in which some pair fell inside the tangent band:
 // the thread's source is tested again against the tile's targets, with the
 // pair loop's operations, and each pair inside the band is listed for the
@@ -463,9 +500,10 @@ __device__ __forceinline__ void adj_band_scan(const float4 *tile, int cnt, long 
 }
 
 template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
-__global__ void __launch_bounds__(kThreadsA, kMinBlocksA2)
+__global__ void __launch_bounds__(kThreadsA, KIND == kKindFF ? kMinBlocksFF : kMinBlocksA2)
 po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
-                 double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err, int boxes, BandList bl)
+                 double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err, int boxes, BandList bl,
+                 const int *__restrict__ order)
 {
     static_assert(KIND != kKindFF || !WANT_T, "far-field targets do not move");
     constexpr int RT = adj2_rec(KIND, HAS_M, WANT_T);
@@ -475,20 +513,48 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
     float *lo = reinterpret_cast<float *>(stage + (size_t)kStages * kPairsA2 * RT);
     float2 *vbuf = reinterpret_cast<float2 *>(lo + kAccAdj * kThreadsA);   // [kFlush][kThreadsA]
 
-    const long si = (long)blockIdx.x * kThreadsA + threadIdx.x;
-    float4 q[kRec];
-#pragma unroll
-    for (int c = 0; c < kRec; ++c) q[c] = si < ns ? srcpk[(size_t)kRec * si + c] : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (si >= ns) q[0].z = 1e3f;   // idle lanes: keep R > 0 (zero currents)
     SrcC s;
-    s.sh[0] = q[0].x; s.sh[1] = q[0].y; s.sh[2] = q[0].z;
-    s.sl[0] = q[1].x; s.sl[1] = q[1].y; s.sl[2] = q[1].z;
-    s.n[0] = q[0].w; s.n[1] = q[1].w; s.n[2] = q[5].x;
-    const float jm[12] = {q[2].x, q[2].y, q[2].z, q[2].w, q[3].x, q[3].y, q[3].z, q[3].w, q[4].x, q[4].y, q[4].z, q[4].w};
+    long si;                 // the thread's source (its index in the caller's arrays)
+    [[maybe_unused]] bool wide = false;     // far field: the CTA's tile stores split offsets
+    [[maybe_unused]] float cen[6] = {};     // far field: the tile centre, hi xyz and lo xyz (turns)
+    if constexpr (KIND == kKindFF) {
+        // one CTA per far-field source tile (po_ff_pack_kernel's records, in
+        // Hilbert order): the offset from the tile centre, J', the normal, M'
+        constexpr int R4 = ff_rec4(HAS_M), T4 = ff_tile4(HAS_M);
+        static_assert(kThreadsA == kTile, "one far-field source tile per adjoint CTA");
+        const float *tf = reinterpret_cast<const float *>(srcpk + (size_t)blockIdx.x * T4);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        s.J[c] = jm[c];
-        s.M[c] = jm[6 + c];
+        for (int c = 0; c < 6; ++c) cen[c] = tf[c];
+        wide = tf[12] != 0.0f;
+        const float *rec = tf + kFFHead * 4 + (threadIdx.x >> 1) * R4 * 4 + (threadIdx.x & 1);   // slot k: rec[2k]
+        const long pos = (long)blockIdx.x * kThreadsA + threadIdx.x;
+        si = pos < ns ? (long)order[pos] : ns;   // padding: past the end, never written
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            s.sh[c] = rec[2 * c];
+            s.sl[c] = rec[2 * (12 + c)];
+            s.n[c] = rec[2 * (9 + c)];
+            s.J[2 * c] = rec[2 * (3 + c)];
+            s.J[2 * c + 1] = rec[2 * (6 + c)];
+            s.M[2 * c] = HAS_M ? rec[2 * (16 + c)] : 0.0f;
+            s.M[2 * c + 1] = HAS_M ? rec[2 * (19 + c)] : 0.0f;
+        }
+    } else {
+        si = (long)blockIdx.x * kThreadsA + threadIdx.x;
+        float4 q[kRec];
+#pragma unroll
+        for (int c = 0; c < kRec; ++c) q[c] = si < ns ? srcpk[(size_t)kRec * si + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (si >= ns) q[0].z = 1e3f;   // idle lanes: keep R > 0 (zero currents)
+        s.sh[0] = q[0].x; s.sh[1] = q[0].y; s.sh[2] = q[0].z;
+        s.sl[0] = q[1].x; s.sl[1] = q[1].y; s.sl[2] = q[1].z;
+        s.n[0] = q[0].w; s.n[1] = q[1].w; s.n[2] = q[5].x;
+        const float jm[12] = {q[2].x, q[2].y, q[2].z, q[2].w, q[3].x, q[3].y, q[3].z, q[3].w, q[4].x, q[4].y, q[4].z,
+                              q[4].w};
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            s.J[c] = jm[c];
+            s.M[c] = jm[6 + c];
+        }
     }
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
@@ -573,6 +639,11 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
         const float4 *tile = stage + (size_t)(it % kStages) * kPairsA2 * RT;
         const long pfirst = p0 + (long)it * kPairsA2;
         const int cnt = (int)min((long)kPairsA2, p1 - pfirst);
+        if constexpr (KIND == kKindFF) {
+            // the stage's cotangents times conj(e^{-t j k r.c}) for this CTA's tile centre c
+            if (threadIdx.x < cnt) ff_rotate_cot<T>(stage + (size_t)(it % kStages) * kPairsA2 * RT + threadIdx.x * RT, cen);
+            __syncthreads();
+        }
         float2 acc[kAccAdj];
 #pragma unroll
         for (int a = 0; a < kAccAdj; ++a) acc[a] = make_float2(0.f, 0.f);
@@ -595,10 +666,12 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
         }
         for (int fb = 0; fb < cnt; fb += kFlush) {
             const int fend = min(cnt, fb + kFlush);
-            if constexpr (kLitA) {
-                // far field, M = 0: two copies of the pair loop, with and without the test
-                auto pairs = [&](auto lit_c) {
-                    constexpr bool LIT = decltype(lit_c)::value;
+            if constexpr (KIND == kKindFF) {
+                // far field: one copy of the pair loop per case, all block-uniform.
+                // LIT: the tile is proven lit (M = 0), so the mask is left out.
+                // WIDE: the CTA's offsets are split, so the phase is too.
+                auto pairs = [&](auto lit_c, auto wide_c) {
+                    constexpr bool LIT = decltype(lit_c)::value, WIDE = decltype(wide_c)::value;
 #pragma unroll kUnrollA
                     for (int p = fb; p < fend; ++p) {
                         float2 rec[NL];
@@ -608,13 +681,15 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
                             rec[2 * c] = make_float2(v.x, v.y);
                             rec[2 * c + 1] = make_float2(v.z, v.w);
                         }
-                        adj_ff_pair2<T, HAS_M, WANT_D, LIT>(acc, rec, s, band);
+                        adj_ff_pair2<T, HAS_M, WANT_D, LIT, WIDE>(acc, rec, s, band);
                     }
                 };
-                if (lit)
-                    pairs(std::true_type{});
+                if (wide)
+                    pairs(std::false_type{}, std::true_type{});
+                else if (lit)
+                    pairs(std::bool_constant<kLitA>{}, std::false_type{});
                 else
-                    pairs(std::false_type{});
+                    pairs(std::false_type{}, std::false_type{});
             } else {
 #pragma unroll kUnrollA
                 for (int p = fb; p < fend; ++p) {
@@ -628,8 +703,7 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
                     float2 vt = make_float2(0.f, 0.f);
                     if (KIND == kKindNF)
                         adj_nf_pair2<T, HAS_M, WANT_D, WANT_T>(acc, vt, rec, s, band);
-                    else if (KIND == kKindScalar) adj_sc_pair2<T, WANT_D, WANT_T>(acc, vt, rec, s);
-                    else adj_ff_pair2<T, HAS_M, WANT_D, false>(acc, rec, s, band);
+                    else adj_sc_pair2<T, WANT_D, WANT_T>(acc, vt, rec, s);
                     if (WANT_T) vbuf[(p - fb) * kThreadsA + threadIdx.x] = vt;
                 }
             }

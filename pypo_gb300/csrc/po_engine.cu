@@ -643,7 +643,7 @@ int run_adjoint(const AdjArgs &a)
     Frame *frame = nullptr;
     float4 *srcpk = nullptr;
     if (!rc && ((rc = salloc(&bbox, (size_t)kBboxBlocks * 6, s, owned)) || (rc = salloc(&frame, 1, s, owned)) ||
-                (rc = salloc(&srcpk, (size_t)ns * kRec, s, owned)))) {
+                (!far && (rc = salloc(&srcpk, (size_t)ns * kRec, s, owned))))) {
         sfree(owned, s);
         return rc;
     }
@@ -655,8 +655,44 @@ int run_adjoint(const AdjArgs &a)
     int centred = far ? 0 : 1;
     void *frargs[] = {&bbox, &nbb, &kap, &centred, &frame};
     if (!rc) rc = launch(frame_kernel(), dim3(1), dim3(32), frargs, 0, s);
-    void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&mixed_scalar, &srcpk};
-    if (!rc) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
+    const int *ff_order = nullptr;   // far field: curve position -> source
+    if (far) {
+        // sources in Hilbert order, in the forward's tile records: one adjoint
+        // CTA per tile, whose centre's phase goes into the cotangents
+        const long n1 = std::max(ns, 1L);
+        const long ntile = (ns + kTile - 1) / kTile;
+        size_t sort_bytes = 0;
+        unsigned long long *keys = nullptr;
+        int *ord = nullptr;
+        void *sort_tmp = nullptr;
+        float4 *tiles = nullptr;
+        cudaError_t e = ff_sort(nullptr, &sort_bytes, nullptr, nullptr, nullptr, nullptr, n1, s);
+        if (e != cudaSuccess) rc = fail(2, std::string("sort size query: ") + err_str(e));
+        if (!rc && ((rc = salloc(&keys, 2 * (size_t)n1, s, owned)) || (rc = salloc(&ord, 2 * (size_t)n1, s, owned)) ||
+                    (rc = salloc(reinterpret_cast<unsigned char **>(&sort_tmp), std::max<size_t>(sort_bytes, 16), s,
+                                 owned)) ||
+                    (rc = salloc(&tiles, (size_t)ntile * ff_tile4(has_m), s, owned)))) {
+            sfree(owned, s);
+            return rc;
+        }
+        unsigned long long *k_in = keys, *k_out = keys + n1;
+        int *i_in = ord, *i_out = ord + n1;
+        void *kargs[] = {&ns, &src7, &frame, &k_in, &i_in};
+        if (!rc) rc = launch(ff_key_kernel(), dim3(nblk_s), dim3(256), kargs, 0, s);
+        if (!rc) {
+            e = ff_sort(sort_tmp, &sort_bytes, k_in, k_out, i_in, i_out, ns, s);
+            if (e != cudaSuccess) rc = fail(2, std::string("source sort: ") + err_str(e));
+            else note_launches(1);
+        }
+        ff_order = i_out;
+        void *fpargs[] = {&ns, &ff_order, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, &tiles};
+        if (!rc) rc = launch(ff_pack_kernel(has_m), dim3((unsigned)ntile), dim3(32), fpargs, 0, s);
+        srcpk = tiles;
+    } else {
+        void *psargs[] = {&ns, &src7, &cur, &gmode, &ncx, &ncy, &frame, &fac_re, &fac_im, (void *)&mixed_scalar,
+                          &srcpk};
+        if (!rc) rc = launch(pack_src_kernel(), dim3(nblk_s), dim3(256), psargs, 0, s);
+    }
     // Pair-packed adjoint: sources in registers, pairs of targets streamed.
     // Near field fused (currents, source and target displacement in one pass).
     const bool want_t = grad_dt != nullptr;
@@ -712,7 +748,7 @@ int run_adjoint(const AdjArgs &a)
     double *part = nullptr;
     if (!rc && (rc = salloc(&part, (size_t)split * kAccAdj * ns, s, owned))) { sfree(owned, s); return rc; }
     const float4 *srcc = srcpk, *trc2 = reinterpret_cast<const float4 *>(trec2);
-    void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err, &boxes, &band};
+    void *fargs[] = {&srcc, &ns, &trc2, &nt, &chunk, &part, &gt, &err, &boxes, &band, &ff_order};
     timing_mark(s, true);
     if (!rc) rc = launch(fk, dim3((unsigned)nsb, (unsigned)split), dim3(kThreadsA), fargs, smem2, s);
     timing_mark(s, false);

@@ -59,11 +59,18 @@ constexpr int kThreadsA = PO_THREADS_A;
 #define PO_PAIRS_A 32            // target pairs per stage of the pair-packed adjoint
 #endif
 #ifndef PO_MINB_A2
-#define PO_MINB_A2 2
+// Resident CTAs per SM asked of ptxas for the pair-packed adjoint: 3 holds the
+// fused near-field kernel at 150-165 registers with no spills (182 at 2), and
+// dish_eh's adjoint measured 208.6 -> 206.1 ms with it.
+#define PO_MINB_A2 3
 #endif
 constexpr int kMinBlocksA2 = PO_MINB_A2;
+#ifndef PO_MINB_FF
+#define PO_MINB_FF 5             // the far-field adjoint: 5 CTAs/SM hold it under 96 registers
+#endif
+constexpr int kMinBlocksFF = PO_MINB_FF;
 constexpr int kUnrollF = PO_UNROLL_F;
-constexpr int kUnrollA = PO_UNROLL_A;   // fused near-field adjoint: resident CTAs asked of ptxas
+constexpr int kUnrollA = PO_UNROLL_A;   // target pairs per iteration of the adjoint pair loop
 constexpr int kAccAdj = 13;
 
 // FP64 comparison kernel.
