@@ -21,9 +21,14 @@
 // vector per pair, Z = b x J - a x M: W.v = -v.Z (scalar triple product).
 //
 // Far field: the same kernel with the far-field pair (currents and source
-// displacement; far-field targets are directions and do not move). With
-// M = 0, a cotangent tile whose direction box proves every pair lit for the
-// CTA's source normals skips the illumination mask.
+// displacement; far-field targets are directions and do not move). A CTA
+// owns one tile of 128 sources in Hilbert order (the forward's tile records,
+// po_farfield.cu): e^{-t j k r.s} = e^{-t j k r.c} e^{-t j k r.(s - c)}, so
+// each stage's cotangents are multiplied once by conj(e^{-t j k r.c}) for
+// the CTA's centre c (ff_rotate_cot), and the pair loop takes only the
+// offset's phase: FP32 for a narrow tile, split for a wide one. With M = 0,
+// a cotangent tile whose direction box proves every pair lit for the CTA's
+// source normals skips the illumination mask.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <cstdint>
@@ -442,6 +447,8 @@ __global__ void po_adj_tgt_box_kernel(float2 *__restrict__ rec, long nt)
 // Far field: one stage's pair record of two directions (lanes), its
 // cotangents gS_J, gS_M (slots 6-17, (re, im) per axis) multiplied in place by
 // conj(e^{-t j k r.c}) for the CTA's tile centre c (hi xyz, lo xyz, turns).
+// One thread per record: spreading a record over four threads (each forming
+// the phase and rotating its share) measured 279.6 -> 297.0 ms on dish_ff.
 // With s = c + w, conj(G) g = conj(G_w) (conj(G_c) g), so the pair loop needs
 // only the offset's phase. r.c in split form: hi products exact (r hi on
 // 2^-11, c hi on the frame's quantum), the rest in one FP32 sum, reduced
@@ -500,7 +507,7 @@ __device__ __forceinline__ void adj_band_scan(const float4 *tile, int cnt, long 
 }
 
 template <int KIND, int T, bool HAS_M, bool WANT_D, bool WANT_T>
-__global__ void __launch_bounds__(kThreadsA, KIND == kKindFF ? kMinBlocksFF : kMinBlocksA2)
+__global__ void __launch_bounds__(kThreadsA, KIND == kKindFF ? kMinBlocksFF : (HAS_M ? kMinBlocksA2M : kMinBlocksA2))
 po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__restrict__ trec, long nt, long chunk,
                  double *__restrict__ part, double *__restrict__ gt, int *__restrict__ err, int boxes, BandList bl,
                  const int *__restrict__ order)
@@ -641,7 +648,8 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
         const int cnt = (int)min((long)kPairsA2, p1 - pfirst);
         if constexpr (KIND == kKindFF) {
             // the stage's cotangents times conj(e^{-t j k r.c}) for this CTA's tile centre c
-            if (threadIdx.x < cnt) ff_rotate_cot<T>(stage + (size_t)(it % kStages) * kPairsA2 * RT + threadIdx.x * RT, cen);
+            if (threadIdx.x < cnt)
+                ff_rotate_cot<T>(stage + (size_t)(it % kStages) * kPairsA2 * RT + threadIdx.x * RT, cen);
             __syncthreads();
         }
         float2 acc[kAccAdj];

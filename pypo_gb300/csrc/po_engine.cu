@@ -420,7 +420,7 @@ int mixed_prepare(const RunArgs &a, Scratch &sc, MixedPlan &p)
         (rc = sc.get(&p.tgtpk, (size_t)nt * 2)))
         return rc;
     if (!scalar) {
-        p.band.cap = sc.band_cap();
+        p.band.cap = sc.band_cap(ns, nt);
         if ((rc = sc.get(&p.band.pairs, p.band.cap)) || (rc = sc.get(&p.band.count, 1))) return rc;
     }
     if (p.far) {
@@ -717,7 +717,7 @@ int run_adjoint(const AdjArgs &a)
     if (want_t) PO_CK_RC(cudaMemsetAsync(gt, 0, sizeof(double) * nt, s));
     BandList band{nullptr, nullptr, 0};   // near-tangent pairs (not the scalar kind)
     if (!rc && kind != kKindScalar) {
-        band.cap = kBandCap;
+        band.cap = band_cap_for(ns, nt);
         if ((rc = salloc(&band.pairs, band.cap, s, owned)) || (rc = salloc(&band.count, 1, s, owned))) {
             sfree(owned, s);
             return rc;

@@ -81,8 +81,8 @@ public:
     virtual ~Scratch() = default;
     virtual int take(void **p, size_t bytes) = 0;
     virtual size_t room() const = 0;
-    // entries of the list of near-tangent pairs a call takes (BandList)
-    virtual unsigned band_cap() const { return kBandCap; }
+    // entries of the list of near-tangent pairs a call of ns x nt pairs takes (BandList)
+    virtual unsigned band_cap(long ns, long nt) const { return band_cap_for(ns, nt); }
     template <typename T>
     int get(T **p, size_t count)
     {

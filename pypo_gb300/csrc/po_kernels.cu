@@ -246,7 +246,7 @@ __device__ __forceinline__ bool tile_lit(const float4 *tile, const float *tb)
 // per-pair illumination test (M = 0 kernels). The far field has its own
 // kernel (po_farfield.cu).
 template <int KIND, int T, bool HAS_M, int TP>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
+__global__ void __launch_bounds__(kThreads, HAS_M ? kMinBlocksM : kMinBlocks)
 po_pk_kernel(const float4 *__restrict__ src, long ns, long chunk, const float4 *__restrict__ tgt, long nt,
              double *__restrict__ part, int *__restrict__ err, int boxes, BandList bl)
 {

@@ -30,7 +30,17 @@ constexpr int kKindScalar = 2;  // scalar Green's function
 constexpr int kThreads = PO_THREADS;   // threads per CTA
 constexpr int kTile = PO_TILE;         // sources per shared-memory stage
 constexpr int kMinBlocks = PO_MINB;    // resident CTAs per SM asked of ptxas
-constexpr int kStages = 3;             // TMA pipeline depth
+#ifndef PO_MINB_M
+// The near-field forward with magnetic currents: 5 CTAs/SM hold it at 90
+// registers (feed -> dish JM forward 0.673 -> 0.624 ms); asking the M = 0
+// kernel for 5 as well slows dish_eh's forward (68.4 -> 70.1 ms).
+#define PO_MINB_M 5
+#endif
+constexpr int kMinBlocksM = PO_MINB_M;
+#ifndef PO_STAGES
+#define PO_STAGES 3
+#endif
+constexpr int kStages = PO_STAGES;     // TMA pipeline depth
 constexpr int kRec = 6;         // float4 per packed source record (96 B)
 constexpr int kRecScalar = 2;   // float4 per packed scalar record (32 B)
 constexpr int kAcc = 12;        // accumulators per target (E, H re/im x y z)
@@ -65,6 +75,12 @@ constexpr int kThreadsA = PO_THREADS_A;
 #define PO_MINB_A2 3
 #endif
 constexpr int kMinBlocksA2 = PO_MINB_A2;
+#ifndef PO_MINB_A2M
+// The same with magnetic source currents: 2 (feed -> dish JM adjoint
+// 1.394 -> 1.348 ms against 3).
+#define PO_MINB_A2M 2
+#endif
+constexpr int kMinBlocksA2M = PO_MINB_A2M;
 #ifndef PO_MINB_FF
 #define PO_MINB_FF 5             // the far-field adjoint: 5 CTAs/SM hold it under 96 registers
 #endif
@@ -97,8 +113,16 @@ struct BandList {
     unsigned *count;
     unsigned cap;
 };
-constexpr unsigned kBandCap = 1u << 20;        // entries, calls on the library's pool
+constexpr unsigned kBandCap = 1u << 20;        // entries, calls on the library's pool: at least
+constexpr unsigned kBandCapMax = 1u << 24;     // ... and at most (one entry per 2^16 pairs between)
 constexpr unsigned kBandCapStatic = 1u << 14;  // entries, the allocation-free entry
+
+// Band-list entries of a call on the library's pool with ns x nt pairs.
+inline unsigned band_cap_for(long ns, long nt)
+{
+    const double want = (double)ns * (double)nt / 65536.0;
+    return want <= kBandCap ? kBandCap : (want >= kBandCapMax ? kBandCapMax : (unsigned)want);
+}
 constexpr unsigned kFixupBlocks = 152;         // grid of the fixup kernels (grid-stride over the list)
 
 // Device error codes (written to the call's error word).

@@ -88,7 +88,7 @@ public:
         return 0;
     }
     size_t room() const override { return kStaticScratchBytes - kOffScratch - used_; }
-    unsigned band_cap() const override { return po::kBandCapStatic; }
+    unsigned band_cap(long, long) const override { return po::kBandCapStatic; }
 
 private:
     unsigned char *base_;

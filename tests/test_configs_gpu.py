@@ -190,3 +190,45 @@ def test_cassegrain_full_size_stage_by_stage(cuda, lib, oracle_mod):
         e2, _ = errors(out[:, sub], oref, mode)
         assert e2 <= REL_L2_TOL, (sk, tk, e2)
         cur = out
+
+
+@pytest.mark.parametrize("name", ["dish_eh", "dish_ff"])
+def test_full_size_superposition(cuda, lib, name):
+    """At full size, a size-independent property of the integral: it is
+    linear in the currents, so out(J1 + c J2) = out(J1) + c out(J2) for a
+    complex c, to FP32 rounding of the sums; the adjoint's current gradient
+    is linear in the cotangent the same way."""
+    import torch
+    from pypo_gb300 import configs, engine
+    w = getattr(configs, name)()
+    dev = cuda
+    s7, t7 = (torch.tensor(w[k], device=dev) for k in ("s7", "t7"))
+    grid = (w["gmode"], w["ncx"], w["ncy"])
+    rng = np.random.default_rng(11)
+    j1 = torch.tensor(w["cur"], device=dev)
+    j2 = torch.tensor(rng.standard_normal(w["cur"].shape) * np.abs(w["cur"]).max(), device=dev)
+    j2[6:] = 0.0
+    c = complex(0.6, -1.3)
+
+    def cmul(x):   # c times a current block (rows: re xyz, im xyz per group)
+        y = torch.empty_like(x)
+        for g in range(2):
+            re, im = x[6 * g:6 * g + 3], x[6 * g + 3:6 * g + 6]
+            y[6 * g:6 * g + 3] = c.real * re - c.imag * im
+            y[6 * g + 3:6 * g + 6] = c.real * im + c.imag * re
+        return y
+    run = lambda j: engine.propagate_dev(w["mode"], s7, j, *grid, t7, w["k"], m_zero=True)
+    lhs = run(j1 + cmul(j2))
+    rhs = run(j1) + cmul(run(j2))
+    assert float(torch.linalg.norm(lhs - rhs) / torch.linalg.norm(rhs)) <= 2e-6
+    nt = t7.shape[1]
+    cot1 = torch.tensor(rng.standard_normal((12, nt)), device=dev)
+    cot2 = torch.tensor(rng.standard_normal((12, nt)), device=dev)
+
+    def grad(cot):
+        gc = torch.empty_like(j1)
+        engine.adjoint_dev(w["mode"], s7, j1, *grid, t7, w["k"], cot, m_zero=True, grad_cur=gc)
+        return gc
+    g = grad(cot1 + 0.7 * cot2)
+    ref = grad(cot1) + 0.7 * grad(cot2)
+    assert float(torch.linalg.norm(g - ref) / torch.linalg.norm(ref)) <= 2e-6
