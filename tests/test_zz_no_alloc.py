@@ -11,6 +11,8 @@ array inside the library. Checked here, through the C-ABI:
     with no change in device memory in use across the call;
   * a wait timeout set in its internal status word comes back through
     po_device_error, once, and is then cleared;
+  * captured in a CUDA graph, it replays to the same bits and reads its
+    inputs at replay time;
   * oversized problems are rejected with a message.
 This file is collected last so that a run stopping at the first failure has
 run every other test already; it also passes alone in a fresh process.
@@ -144,6 +146,39 @@ def test_static_timeout_reaches_po_device_error(cuda, lib):
     assert code.value == 101
     assert lib.po_device_error(ctypes.c_void_p(stream.cuda_stream), ctypes.byref(code)) == 0
     assert code.value == 0
+
+
+@pytest.mark.parametrize("name,scale", [("dish_eh", 0.1), ("dish_ff", 0.05)])
+def test_static_entry_replays_in_a_cuda_graph(cuda, lib, name, scale):
+    """The allocation-free entry inside a captured CUDA graph (near field, and
+    the far field with its radix sort): after one call outside capture (the
+    set-up), the captured call replays to the same bits, and a replay after
+    the currents were scaled in place gives the scaled field (the graph
+    reads its inputs at replay time)."""
+    import torch
+    from pypo_gb300 import configs
+    w = getattr(configs, name)(scale=scale)
+    s7, cur, t7 = (torch.tensor(w[k], device=cuda) for k in ("s7", "cur", "t7"))
+    out = torch.empty((12, t7.shape[1]), dtype=torch.float64, device=cuda)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        assert _static(lib, w["mode"], w, s7, cur, t7, out, status, True, side) == 0, lib.po_last_error()
+    torch.cuda.synchronize()
+    ref = out.clone()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        stream = torch.cuda.current_stream()
+        assert _static(lib, w["mode"], w, s7, cur, t7, out, status, True, stream) == 0, lib.po_last_error()
+    out.fill_(float("nan"))
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref) and int(status.item()) == 0
+    cur.mul_(2.0)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.allclose(out, 2.0 * ref, rtol=1e-6, atol=1e-6 * float(ref.abs().max()))
 
 
 def test_static_scratch_rejects_oversized_problems(cuda, lib):
