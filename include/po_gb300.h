@@ -349,8 +349,9 @@ int po_last_launches(void);
 /* Synchronises `stream`, then returns (and clears) the device error words in
  * *code: 0 when every kernel finished normally, 101 when a kernel gave up a
  * bounded wait for a tile copy, 103 when a call met more near-tangent
- * (source, target) pairs than its list holds (one entry per 65,536 pairs,
- * between 2^20 and 2^24; 16,384 for po_run_dev_static), 102 when the device normal generator overran its
+ * (source, target) pairs than its list holds (every pair of a call of up
+ * to 2^22 pairs, else one entry per 65,536 pairs, between 2^22 and 2^24;
+ * 16,384 for po_run_dev_static), 102 when the device normal generator overran its
  * bound; the results of such a call are invalid. It reads the
  * word of the allocating entries and the internal word of po_run_dev_static
  * (calls made with status == NULL); it allocates nothing. */

@@ -113,14 +113,19 @@ struct BandList {
     unsigned *count;
     unsigned cap;
 };
-constexpr unsigned kBandCap = 1u << 20;        // entries, calls on the library's pool: at least
+constexpr unsigned kBandCap = 1u << 22;        // entries, calls on the library's pool: every pair up
+                                               // to this many, else at least this many
 constexpr unsigned kBandCapMax = 1u << 24;     // ... and at most (one entry per 2^16 pairs between)
 constexpr unsigned kBandCapStatic = 1u << 14;  // entries, the allocation-free entry
 
-// Band-list entries of a call on the library's pool with ns x nt pairs.
+// Band-list entries of a call on the library's pool with ns x nt pairs: a
+// call of up to 2^22 pairs can list all of them (targets in the sources'
+// own plane put every pair in the band); larger calls one per 2^16 pairs.
 inline unsigned band_cap_for(long ns, long nt)
 {
-    const double want = (double)ns * (double)nt / 65536.0;
+    const double pairs = (double)ns * (double)nt;
+    if (pairs <= (double)kBandCap) return pairs < 1.0 ? 1u : (unsigned)pairs;
+    const double want = pairs / 65536.0;
     return want <= kBandCap ? kBandCap : (want >= kBandCapMax ? kBandCapMax : (unsigned)want);
 }
 constexpr unsigned kFixupBlocks = 152;         // grid of the fixup kernels (grid-stride over the list)

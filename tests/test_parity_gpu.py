@@ -186,3 +186,47 @@ def test_drop_in_float_abi(cuda, lib, name, modes):
             if mode == "EH":
                 e2, _ = errors(M.currents_block(got_d.stack()), ref, mode)
                 assert e2 <= REL_L2_TOL
+
+
+def test_coplanar_targets_every_pair_in_the_band(cuda, lib, oracle_mod):
+    """Targets in the sources' own plane: n . d == 0 for every pair, so every
+    pair is inside the tangent band (the reference counts them lit). The
+    allocating entries list all of them (a call of up to 2^22 pairs can),
+    and the fixups add every pair's FP64 term: forward and adjoint against
+    the oracle at FP64 level. The allocation-free entry's list holds 16,384
+    pairs, so with 18,000 it reports device error 103 through its status
+    word instead of a wrong sum."""
+    import ctypes
+    import torch
+    from pypo_gb300 import engine
+    rng = np.random.default_rng(41)
+    ns, nt = 150, 120
+    s7 = np.zeros((7, ns))
+    s7[0:2] = rng.uniform(-1, 1, (2, ns))
+    s7[5] = 1.0
+    s7[6] = rng.uniform(0.5, 1.5, ns) * 1e-3
+    t7 = np.zeros((7, nt))
+    t7[0:2] = rng.uniform(-1.3, 1.3, (2, nt))
+    t7[5] = 1.0
+    cur = rng.standard_normal((12, ns))
+    k = 2 * np.pi / 0.1
+    for mode in ("EH", "JM"):
+        got = engine.propagate(mode, s7, cur, -1, 0, 0, t7, k)
+        ref = oracle_mod.run(mode, s7, cur, -1, 0, 0, t7, k)
+        assert _rel(got, ref) <= 1e-12, (mode, _rel(got, ref))
+    cot = rng.standard_normal((12, nt))
+    gm = engine.adjoint("EH", s7, cur, -1, 0, 0, t7, k, cot)
+    go = oracle_mod.adjoint("EH", s7, cur, -1, 0, 0, t7, k, cot)
+    for name, want in go.items():
+        assert _rel(gm[name], want) <= 1e-10, (name, _rel(gm[name], want))
+    # the allocation-free entry: its list overflows, and it says so
+    d = {n: torch.tensor(a, device=cuda) for n, a in (("s7", s7), ("cur", cur), ("t7", t7))}
+    out = torch.empty((12, nt), dtype=torch.float64, device=cuda)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    stream = torch.cuda.current_stream()
+    rc = lib.po_run_dev_static(1, ns, d["s7"].data_ptr(), -1, 0, 0, d["cur"].data_ptr(), nt, d["t7"].data_ptr(),
+                               float(k), 1.0, -1.0, 0, out.data_ptr(), status.data_ptr(),
+                               ctypes.c_void_p(stream.cuda_stream))
+    assert rc == 0, lib.po_last_error()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 103
