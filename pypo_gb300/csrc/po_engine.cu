@@ -664,13 +664,12 @@ int run_adjoint(const AdjArgs &a)
         size_t sort_bytes = 0;
         unsigned long long *keys = nullptr;
         int *ord = nullptr;
-        void *sort_tmp = nullptr;
+        unsigned char *sort_tmp = nullptr;
         float4 *tiles = nullptr;
         cudaError_t e = ff_sort(nullptr, &sort_bytes, nullptr, nullptr, nullptr, nullptr, n1, s);
         if (e != cudaSuccess) rc = fail(2, std::string("sort size query: ") + err_str(e));
         if (!rc && ((rc = salloc(&keys, 2 * (size_t)n1, s, owned)) || (rc = salloc(&ord, 2 * (size_t)n1, s, owned)) ||
-                    (rc = salloc(reinterpret_cast<unsigned char **>(&sort_tmp), std::max<size_t>(sort_bytes, 16), s,
-                                 owned)) ||
+                    (rc = salloc(&sort_tmp, std::max<size_t>(sort_bytes, 16), s, owned)) ||
                     (rc = salloc(&tiles, (size_t)ntile * ff_tile4(has_m), s, owned)))) {
             sfree(owned, s);
             return rc;
