@@ -9,7 +9,8 @@ vector Gaussian feed (makeGaussBeam). Outputs go to golden_*.npz beside this
 script. Needs the reference sources (this container); the fixtures then
 travel without them.
 
-Usage: python tests/golden/make_golden.py [--only-calcjm | --only-eff | --only-fitgauss | --only-converge]
+Usage: python tests/golden/make_golden.py [--only-calcjm | --only-eff | --only-fitgauss | --only-converge |
+       --only-highkr]
 The reference checkout is read from $PYPO_REFERENCE (default /root/reference).
 """
 import json
@@ -288,10 +289,44 @@ def converge(ref):
     print("wrote converge", {k: v for k, v in out.items() if k.endswith(("__auto", "__on_target"))})
 
 
+def high_kr(ref):
+    """The reference's own CPU library at the benchmark's phase scale: a
+    paraboloid f 500 mm, D 200 mm (uv 41 x 40) at lambda 1 mm radiating a
+    tapered x-polarised current with phase noise (and a small random M) to
+    its focal plane (15 x 15 over +-5 mm; kR ~ 3.2e3 rad: EH, JM) and to a
+    15 x 15 far-field grid over +-1 deg (k r' up to 6e2 rad: FF), both time
+    directions."""
+    rng = np.random.default_rng(20261204)
+    src = SF.paraboloid(500.0, [41, 40], gmode=1, lims_a=[0, 100])
+    tgt = SF.translate(SF.plane([15, 15], gmode=0, lims_a=[-5, 5]), dz=500.0)
+    ff = SF.farfield([15, 15], [-1, 1], [-1, 1])
+    s7 = ref.grid(src)
+    r = np.hypot(s7[0], s7[1])
+    amp = np.exp(-0.5 * np.log(10) * (r / 100.0) ** 2)
+    ph = rng.normal(0.0, 0.05, r.size)
+    cur = 1e-3 * rng.standard_normal((12, r.size))
+    cur[0] += amp * np.cos(ph)
+    cur[3] += amp * np.sin(ph)
+    k = 2 * np.pi
+    data = {"src_json": dict_to_json(src), "tgt_json": dict_to_json(tgt), "ff_json": dict_to_json(ff), "k": k,
+            "epsilon": 1.0, "cur": cur}
+    for mode, t_dict in (("EH", tgt), ("JM", tgt), ("FF", ff)):
+        for t in (-1.0, 1.0):
+            out, sg, tg = ref.propagate(mode, src, t_dict, cur, k=k, epsilon=1.0, t_dir=t, nthreads=8)
+            data[f"out_{mode}_{'fwd' if t < 0 else 'bwd'}"] = out
+            data["ff_grid" if mode == "FF" else "tgt_grid"] = tg
+    data["src_grid"] = sg
+    np.savez_compressed(HERE / "golden_highkr.npz", **data)
+    print("wrote highkr")
+
+
 def main():
     if not O.REF_PATH.exists():
         subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
     ref = O.Reference()
+    if "--only-highkr" in sys.argv:
+        high_kr(ref)
+        return
     if "--only-calcjm" in sys.argv:
         calcjm(ref)
         return
@@ -308,6 +343,7 @@ def main():
     efficiencies(ref)
     fitgauss(ref)
     converge(ref)
+    high_kr(ref)
     rng = np.random.default_rng(20261203)
     k = 2 * np.pi / 0.7
     for name, src, tgt, modes in cases():

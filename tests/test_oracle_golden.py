@@ -57,3 +57,17 @@ def test_oracle_live_against_reference(oracle_mod):
         out, sg, tg = ref.propagate(mode, src, tgt, cc, k=3.1, epsilon=2.0, t_dir=-1.0, nthreads=2)
         got = oracle_mod.run(mode, sg, cc, 1, 9, 14, tg, 3.1, 2.0, -1.0, nthreads=3)
         np.testing.assert_allclose(got, out, rtol=0, atol=1e-12 * np.abs(out).max(), err_msg=mode)
+
+
+def test_oracle_matches_reference_at_high_kr(oracle_mod):
+    """The reference's own outputs at the benchmark's phase scale (kR ~ 3.2e3
+    rad near field, k r' up to 6e2 rad far field; golden_highkr.npz): the
+    oracle's FP64 sums agree to rounding."""
+    c = load_case("highkr")
+    src = c["src"]
+    for mode, tg in (("EH", "tgt_grid"), ("JM", "tgt_grid"), ("FF", "ff_grid")):
+        for tag, t in (("fwd", -1.0), ("bwd", 1.0)):
+            got = oracle_mod.run(mode, c["src_grid"], c["cur"], src["gmode"], *src["gridsize"], c[tg],
+                                 float(c["k"]), float(c["epsilon"]), t, nthreads=4)
+            ref = c[f"out_{mode}_{tag}"]
+            np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max(), err_msg=f"{mode} {tag}")
