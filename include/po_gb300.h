@@ -268,6 +268,7 @@ double po_last_extent(void);
  *         angle and y the azimuth (radians), as the reference's AoE grid
  *   out   po_n_out(mode)*nt doubles in bundle row order
  *   precision  0 mixed (FP32 bulk + split hi/lo phase), 1 plain FP64
+ *   ns, nt     0 .. 2^31 - 1 (device indices are 32-bit; larger is status 1)
  *
  * Whether M == 0 (which selects the kernels without magnetic terms) is
  * settled from the first 4096 magnetic values on the host when one of them

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -329,6 +330,8 @@ int validate(const RunArgs &a)
 {
     if (a.mode < 0 || a.mode > 5) return fail(1, "mode must be 0..5 (JM EH JMEH EHP FF scalar)");
     if (a.ns < 0 || a.nt < 0) return fail(1, "negative size");
+    if (a.ns > INT_MAX || a.nt > INT_MAX)
+        return fail(1, "at most 2^31 - 1 sources and targets per call (indices are 32-bit on the device)");
     if (a.ns > 0 && a.gmode >= 0 && (a.ncx < 1 || a.ncy < 1)) return fail(1, "bad source grid shape");
     if (a.ns > 0 && a.gmode >= 0 && (long)a.ncx * a.ncy != a.ns)
         return fail(1, "ncx * ncy must equal the number of source points");

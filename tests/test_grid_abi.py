@@ -93,6 +93,10 @@ def test_invalid_arguments_are_rejected_before_any_device_work(lib):
     rc = lib.po_run_d(1, 4, s7.ctypes.data, 0, 2, 2, cur.ctypes.data, 3, t7.ctypes.data, 1.0, 1.0, -1.0, 7,
                       out.ctypes.data)
     assert rc != 0 and b"precision" in lib.po_last_error()
+    # sizes past 32-bit device indices (the buffers are never read: the check comes first)
+    rc = lib.po_run_d(1, 1 << 31, s7.ctypes.data, -1, 0, 0, cur.ctypes.data, 3, t7.ctypes.data, 1.0, 1.0, -1.0, 0,
+                      out.ctypes.data)
+    assert rc == 1 and b"2^31 - 1" in lib.po_last_error()
     # empty target: nothing to do, success
     rc = lib.po_run_d(1, 4, s7.ctypes.data, 0, 2, 2, cur.ctypes.data, 0, t7.ctypes.data, 1.0, 1.0, -1.0, 0,
                       out.ctypes.data)
