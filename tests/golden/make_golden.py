@@ -293,7 +293,8 @@ def high_kr(ref):
     """The reference's own CPU library at the benchmark's phase scale: a
     paraboloid f 500 mm, D 200 mm (uv 41 x 40) at lambda 1 mm radiating a
     tapered x-polarised current with phase noise (and a small random M) to
-    its focal plane (15 x 15 over +-5 mm; kR ~ 3.2e3 rad: EH, JM) and to a
+    its focal plane (15 x 15 over +-5 mm; kR ~ 3.2e3 rad: EH, JM, EHP,
+    scalar) and to a
     15 x 15 far-field grid over +-1 deg (k r' up to 6e2 rad: FF), both time
     directions."""
     rng = np.random.default_rng(20261204)
@@ -310,9 +311,10 @@ def high_kr(ref):
     k = 2 * np.pi
     data = {"src_json": dict_to_json(src), "tgt_json": dict_to_json(tgt), "ff_json": dict_to_json(ff), "k": k,
             "epsilon": 1.0, "cur": cur}
-    for mode, t_dict in (("EH", tgt), ("JM", tgt), ("FF", ff)):
+    for mode, t_dict in (("EH", tgt), ("JM", tgt), ("EHP", tgt), ("scalar", tgt), ("FF", ff)):
         for t in (-1.0, 1.0):
-            out, sg, tg = ref.propagate(mode, src, t_dict, cur, k=k, epsilon=1.0, t_dir=t, nthreads=8)
+            c = cur[:2] if mode == "scalar" else cur
+            out, sg, tg = ref.propagate(mode, src, t_dict, c, k=k, epsilon=1.0, t_dir=t, nthreads=8)
             data[f"out_{mode}_{'fwd' if t < 0 else 'bwd'}"] = out
             data["ff_grid" if mode == "FF" else "tgt_grid"] = tg
     data["src_grid"] = sg

@@ -61,13 +61,15 @@ def test_oracle_live_against_reference(oracle_mod):
 
 def test_oracle_matches_reference_at_high_kr(oracle_mod):
     """The reference's own outputs at the benchmark's phase scale (kR ~ 3.2e3
-    rad near field, k r' up to 6e2 rad far field; golden_highkr.npz): the
-    oracle's FP64 sums agree to rounding."""
+    rad near field: EH, JM, EHP, scalar; k r' up to 6e2 rad far field: FF;
+    golden_highkr.npz): the oracle's FP64 sums agree to rounding."""
     c = load_case("highkr")
     src = c["src"]
-    for mode, tg in (("EH", "tgt_grid"), ("JM", "tgt_grid"), ("FF", "ff_grid")):
+    for mode, tg in (("EH", "tgt_grid"), ("JM", "tgt_grid"), ("EHP", "tgt_grid"), ("scalar", "tgt_grid"),
+                     ("FF", "ff_grid")):
+        cur = c["cur"][:2] if mode == "scalar" else c["cur"]
         for tag, t in (("fwd", -1.0), ("bwd", 1.0)):
-            got = oracle_mod.run(mode, c["src_grid"], c["cur"], src["gmode"], *src["gridsize"], c[tg],
+            got = oracle_mod.run(mode, c["src_grid"], cur, src["gmode"], *src["gridsize"], c[tg],
                                  float(c["k"]), float(c["epsilon"]), t, nthreads=4)
             ref = c[f"out_{mode}_{tag}"]
             np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max(), err_msg=f"{mode} {tag}")

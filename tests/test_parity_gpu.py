@@ -234,18 +234,20 @@ def test_coplanar_targets_every_pair_in_the_band(cuda, lib, oracle_mod):
 
 def test_high_kr_against_reference_outputs(cuda, lib):
     """The reference's own FP64 outputs at the benchmark's phase scale
-    (golden_highkr.npz: kR ~ 3.2e3 rad to the focal plane, EH and JM; the far
-    field, FF; both time directions): the mixed path within the bar, the
-    FP64 path to 1e-10."""
+    (golden_highkr.npz: kR ~ 3.2e3 rad to the focal plane, EH, JM, EHP and
+    scalar; the far field, FF; both time directions): the mixed path within
+    the bar, the FP64 path to 1e-10."""
     from pypo_gb300 import engine
     c = load_case("highkr")
     src = c["src"]
     grid = (int(src["gmode"]), *[int(v) for v in src["gridsize"]])
-    for mode, tg in (("EH", "tgt_grid"), ("JM", "tgt_grid"), ("FF", "ff_grid")):
+    for mode, tg in (("EH", "tgt_grid"), ("JM", "tgt_grid"), ("EHP", "tgt_grid"), ("scalar", "tgt_grid"),
+                     ("FF", "ff_grid")):
+        cur = c["cur"][:2] if mode == "scalar" else c["cur"]
         for tag, t in (("fwd", -1.0), ("bwd", 1.0)):
             ref = c[f"out_{mode}_{tag}"]
-            got = engine.propagate(mode, c["src_grid"], c["cur"], *grid, c[tg], float(c["k"]), 1.0, t)
+            got = engine.propagate(mode, c["src_grid"], cur, *grid, c[tg], float(c["k"]), 1.0, t)
             e, p = errors(got, ref, mode)
             assert e <= REL_L2_TOL and p <= PHASE_TOL, (mode, tag, e, p)
-            d = engine.propagate(mode, c["src_grid"], c["cur"], *grid, c[tg], float(c["k"]), 1.0, t, "fp64")
+            d = engine.propagate(mode, c["src_grid"], cur, *grid, c[tg], float(c["k"]), 1.0, t, "fp64")
             np.testing.assert_allclose(d, ref, rtol=0, atol=FP64_TOL * np.abs(ref).max(), err_msg=f"{mode} {tag}")
