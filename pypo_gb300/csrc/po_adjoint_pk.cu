@@ -52,8 +52,13 @@ __host__ __device__ constexpr int adj2_rec(int kind, bool has_m, bool want_t)
 }
 
 constexpr int kPairsA2 = PO_PAIRS_A;   // target pairs per shared-memory stage
-constexpr int kFlush = 16;     // target pairs per transpose of the target-side values
-static_assert(kThreadsA == 128 && kFlush == 16, "the transpose maps 128 threads onto 16 pairs x 8 segments");
+#ifndef PO_FLUSH_A
+#define PO_FLUSH_A 16
+#endif
+constexpr int kFlush = PO_FLUSH_A;   // target pairs per transpose of the target-side values
+constexpr int kSegs = kThreadsA / kFlush;   // threads summing one target pair
+static_assert(kThreadsA == 128 && (kFlush == 16 || kFlush == 32),
+              "the transpose maps 128 threads onto 16 pairs x 8 segments or 32 pairs x 4");
 
 __global__ void po_adj_pack_tgt2_kernel(long nt, const double *__restrict__ tgt7, const double *__restrict__ gam,
                                         const Frame *__restrict__ frp, int far, int rec4, float *__restrict__ out)
@@ -717,21 +722,24 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
             }
             if (WANT_T) {
                 // Sum the CTA's sources for each target pair of this flush: thread
-                // (pl, k) adds 16 sources of pair pl (rotated reads: no bank
-                // conflicts), then the 8 segments combine by shuffles.
+                // (pl, k) adds kThreadsA / kSegs sources of pair pl (rotated reads:
+                // the 8 threads of a shared-memory phase hit distinct banks), then
+                // the kSegs segments combine by shuffles.
                 __syncthreads();
-                const int pl = threadIdx.x >> 3, k = threadIdx.x & 7;
+                constexpr int kPer = kThreadsA / kSegs / 2;   // float4 (two sources each) per thread
+                const int pl = threadIdx.x / kSegs, k = threadIdx.x % kSegs;
+                const int rot = kSegs == 8 ? k : 4 * (pl & 1) + k;
                 float2 sum = make_float2(0.f, 0.f);
                 if (pl < fend - fb) {
                     const float4 *row = reinterpret_cast<const float4 *>(vbuf + pl * kThreadsA);
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const float4 v = row[8 * k + ((j + k) & 7)];
+                    for (int j = 0; j < kPer; ++j) {
+                        const float4 v = row[kPer * k + ((j + rot) & (kPer - 1))];
                         sum = add2(sum, add2(make_float2(v.x, v.y), make_float2(v.z, v.w)));
                     }
                 }
 #pragma unroll
-                for (int m = 1; m < 8; m <<= 1) {
+                for (int m = 1; m < kSegs; m <<= 1) {
                     sum.x += __shfl_xor_sync(0xffffffffu, sum.x, m);
                     sum.y += __shfl_xor_sync(0xffffffffu, sum.y, m);
                 }
