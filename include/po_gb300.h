@@ -256,6 +256,13 @@ int po_fmin(int n, const double *x0, double xtol, double ftol, long maxiter, lon
  * and reads it back with the call's results. */
 double po_last_extent(void);
 
+/* Number of near-tangent (source, target) pairs (|n . R_hat| < 1e-6) that
+ * this thread's last mixed-precision host-buffer call (po_run_d,
+ * po_adjoint_d) left out of its FP32 sums and decided, and summed if lit, in
+ * FP64 with the reference's rounding; 0 after any other call. A count above
+ * the call's list capacity came with device error 103. */
+unsigned long long po_last_band_pairs(void);
+
 /* ---- explicit-grid, double-precision entry (host buffers) ---------------
  * New; the reference has no equivalent (its C-ABI regenerates grids inside
  * every call, Kernelsf.cu:1643-1644, so it cannot take perturbed surfaces or

@@ -14,7 +14,7 @@ LIB_PATH = pathlib.Path(__file__).resolve().parent / "libpo_gb300.so"
 EXPORTS = ("po_last_error", "po_n_out", "po_last_launches", "po_generate_grid", "po_generate_grid_dev",
            "po_correlated_error", "po_correlated_error_dev", "po_gauss_beam_dev", "po_calc_jm_dev",
            "po_efficiency_sums_dev", "po_fit_gauss_abs_dev", "po_generate_gauss_dev", "po_fmin", "po_run_d",
-           "po_run_dev", "po_run_dev_static", "po_last_extent", "po_adjoint_dev", "po_adjoint_d", "po_device_error", "po_wait_selftest", "po_scratch_in_use", "po_timing_enable", "po_timing_collect", "po_fp32_probe",
+           "po_run_dev", "po_run_dev_static", "po_last_extent", "po_last_band_pairs", "po_adjoint_dev", "po_adjoint_d", "po_device_error", "po_wait_selftest", "po_scratch_in_use", "po_timing_enable", "po_timing_collect", "po_fp32_probe",
            "callKernelf_JM", "callKernelf_EH", "callKernelf_JMEH", "callKernelf_EHP",
            "callKernelf_FF", "callKernelf_scalar", "callRTKernel")
 
@@ -77,6 +77,8 @@ def load():
                              c_double, c_double, c_double, c_int, c_void_p]
     lib.po_last_extent.restype = c_double
     lib.po_last_extent.argtypes = []
+    lib.po_last_band_pairs.restype = ctypes.c_ulonglong
+    lib.po_last_band_pairs.argtypes = []
     lib.po_run_dev.restype = c_int
     lib.po_run_dev.argtypes = [c_int, c_long, c_void_p, c_int, c_int, c_int, c_void_p, c_long, c_void_p,
                                c_double, c_double, c_double, c_int, c_int, c_void_p, c_void_p]

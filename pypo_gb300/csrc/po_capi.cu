@@ -21,6 +21,7 @@ cudaStream_t g_streams[64] = {};
 // Frame half-extent (wavelengths) of this thread's last mixed-precision
 // host-buffer call; 0 after any other call.
 thread_local double t_extent = 0.0;
+thread_local unsigned long long t_band = 0;
 
 // Private non-blocking stream of the host-buffer entry points, one per device.
 // The message of a device error code of the kernels (kErr* in po_kernels.cuh).
@@ -110,23 +111,32 @@ int m_is_zero(const double *h_cur, const double *d_cur, long ns, cudaStream_t s,
         if ((rc = po::scratch_alloc(reinterpret_cast<void **>(&ptr), (bytes), s))) goto done; \
     } while (0)
 
-// Host slot for the frame's half-extent read back by a host-buffer call. It
-// is page-locked so that the copy stays asynchronous: a device-to-host copy
-// into pageable memory makes the host wait for all of the call's kernels
-// before it can queue the output copies. Pageable (the caller's slot) if
-// pinning fails. One small page-locked block per calling thread, kept.
-double *extent_slot(double *pageable)
+// Host slots read back by a host-buffer call: the frame's half-extent and
+// the number of near-tangent pairs. They are page-locked so that the copies
+// stay asynchronous: a device-to-host copy into pageable memory makes the
+// host wait for all of the call's kernels before it can queue the output
+// copies. Pageable (the caller's slots) if pinning fails. One small
+// page-locked block per calling thread, kept.
+struct HostSlots {
+    double extent;
+    unsigned band;
+};
+
+HostSlots *host_slots(HostSlots *pageable)
 {
-    thread_local double *pinned = nullptr;
+    thread_local HostSlots *pinned = nullptr;
     thread_local bool tried = false;
     if (!tried) {
         tried = true;
-        if (cudaMallocHost(&pinned, sizeof(double)) != cudaSuccess) {
+        if (cudaMallocHost(&pinned, sizeof(HostSlots)) != cudaSuccess) {
             pinned = nullptr;
             (void)cudaGetLastError();
         }
     }
-    return pinned ? pinned : pageable;
+    HostSlots *h = pinned ? pinned : pageable;
+    h->extent = 0.0;
+    h->band = 0;
+    return h;
 }
 
 // Host buffers in, host buffers out; synchronous.
@@ -135,6 +145,7 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
 {
     po::clear_error();
     t_extent = 0.0;
+    t_band = 0;
     {
         po::RunArgs v;
         v.mode = mode;
@@ -160,7 +171,8 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
     if (int rc = lib_stream(&s)) return rc;
     double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_out = nullptr;
     int rc = 0, code = 0;
-    double extent = 0.0;
+    HostSlots local{};
+    HostSlots *hs = host_slots(&local);
     po::RunArgs a;
     PO_SCRATCH(d_src, sizeof(double) * 7 * std::max(ns, 1L));
     PO_SCRATCH(d_cur, sizeof(double) * ncur * std::max(ns, 1L));
@@ -190,15 +202,18 @@ int run_host(int mode, long ns, const double *src7, int gmode, int ncx, int ncy,
         if ((rc = m_is_zero(cur, d_cur, ns, s, mz))) goto done;
         a.m_zero = mz;
     }
-    a.extent_host = extent_slot(&extent);
-    *a.extent_host = 0.0;
+    a.extent_host = &hs->extent;
+    a.band_host = &hs->band;
     a.out = d_out;
     a.stream = s;
     rc = po::run_device(a);
     if (rc) goto done;
     CK(cudaMemcpyAsync(out, d_out, sizeof(double) * nout * nt, cudaMemcpyDeviceToHost, s));
     rc = po::read_device_error(s, &code);   // the call's one synchronisation
-    if (!rc && precision == 0) t_extent = *a.extent_host;
+    if (!rc && precision == 0) {
+        t_extent = hs->extent;
+        t_band = hs->band;
+    }
     if (!rc && code) rc = fail(4, device_error_text(code));
 done:
     if (d_src) cudaFreeAsync(d_src, s);
@@ -420,7 +435,7 @@ namespace {
 int adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
                 const double *tgt7, double k, double epsilon, double t_direction, int precision, int flags,
                 const double *cot, double *grad_cur, double *grad_ds, double *grad_dt, cudaStream_t stream,
-                double *extent_host)
+                HostSlots *slots)
 {
     po::AdjArgs a;
     a.mode = mode;
@@ -443,7 +458,8 @@ int adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, int n
     a.grad_ds = grad_ds;
     a.grad_dt = grad_dt;
     a.stream = stream;
-    a.extent_host = extent_host;
+    a.extent_host = slots ? &slots->extent : nullptr;
+    a.band_host = slots ? &slots->band : nullptr;
     if (!grad_cur && !grad_ds && !grad_dt) return fail(1, "no gradient requested");
     return po::run_adjoint(a);
 }
@@ -460,6 +476,7 @@ int po_adjoint_dev(int mode, long ns, const double *src7, int gmode, int ncx, in
 }
 
 double po_last_extent(void) { return t_extent; }
+unsigned long long po_last_band_pairs(void) { return t_band; }
 
 int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int ncy, const double *cur, long nt,
                  const double *tgt7, double k, double epsilon, double t_direction, int precision, const double *cot,
@@ -467,6 +484,7 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
 {
     po::clear_error();
     t_extent = 0.0;
+    t_band = 0;
     if (mode < 0 || mode > 5) return fail(1, "mode must be 0..5");
     if (ns < 0 || nt < 0) return fail(1, "negative size");
     const int nout = po::n_out(mode);
@@ -475,9 +493,8 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_cot = nullptr;
     double *d_gc = nullptr, *d_gs = nullptr, *d_gt = nullptr;
     int rc = 0, code = 0;
-    double extent = 0.0;
-    double *ext = extent_slot(&extent);
-    *ext = 0.0;
+    HostSlots local{};
+    HostSlots *hs = host_slots(&local);
     const size_t ns1 = std::max(ns, 1L), nt1 = std::max(nt, 1L);
     const int ncur = mode == po::kScalar ? 2 : 12;
     PO_SCRATCH(d_src, sizeof(double) * 7 * ns1);
@@ -499,7 +516,7 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
         bool mz = false;
         if (ns > 0 && mode != po::kScalar && (rc = m_is_zero(cur, d_cur, ns, s, mz))) goto done;
         rc = adjoint_dev(mode, ns, d_src, gmode, ncx, ncy, d_cur, nt, d_tgt, k, epsilon, t_direction, precision,
-                         mz ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s, ext);
+                         mz ? 1 : 0, d_cot, d_gc, d_gs, d_gt, s, hs);
     }
     if (rc) goto done;
     if (grad_cur && ns > 0)
@@ -507,7 +524,10 @@ int po_adjoint_d(int mode, long ns, const double *src7, int gmode, int ncx, int 
     if (grad_ds && ns > 0) CK(cudaMemcpyAsync(grad_ds, d_gs, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
     if (grad_dt && nt > 0) CK(cudaMemcpyAsync(grad_dt, d_gt, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
     rc = po::read_device_error(s, &code);   // the call's one synchronisation
-    if (!rc && precision == 0) t_extent = *ext;
+    if (!rc && precision == 0) {
+        t_extent = hs->extent;
+        t_band = hs->band;
+    }
     if (!rc && code) rc = fail(4, device_error_text(code));
 done:
     for (double *p : {d_src, d_cur, d_tgt, d_cot, d_gc, d_gs, d_gt})

@@ -526,6 +526,8 @@ int mixed_launch(const RunArgs &a, MixedPlan &p, int *err)
     if (!rc) rc = launch(epilogue_kernel(), dim3(nblk_t), dim3(256), eargs, 0, s);
     if (!rc && a.extent_host) PO_CK_RC(cudaMemcpyAsync(a.extent_host, &p.frame->m, sizeof(double),
                                                        cudaMemcpyDeviceToHost, s));
+    if (!rc && a.band_host && p.band.count)
+        PO_CK_RC(cudaMemcpyAsync(a.band_host, p.band.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     return rc;
 }
 
@@ -594,6 +596,7 @@ int run_adjoint(const AdjArgs &a)
         fa.mode = kEH;
         fa.out = eh;
         fa.extent_host = nullptr;
+        fa.band_host = nullptr;
         rc = run_device(fa);
         const double c_l = (double)2.99792458e8f, mu0 = (double)1.2566370614e-6f;
         double zi = 1.0 / std::sqrt(mu0 / (a.epsilon * (1.0 / (mu0 * c_l * c_l))));
@@ -774,6 +777,8 @@ int run_adjoint(const AdjArgs &a)
     }
     if (!rc && a.extent_host) PO_CK_RC(cudaMemcpyAsync(a.extent_host, &frame->m, sizeof(double),
                                                        cudaMemcpyDeviceToHost, s));
+    if (!rc && a.band_host && band.count)
+        PO_CK_RC(cudaMemcpyAsync(a.band_host, band.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     sfree(owned, s);
     return rc;
 }

@@ -26,6 +26,8 @@ struct RunArgs {
     cudaStream_t stream = nullptr;
     double *extent_host = nullptr; // mixed path: host slot for the frame's half-extent (wavelengths),
                                    // written by a copy queued on `stream`
+    unsigned *band_host = nullptr; // mixed path: host slot for the number of near-tangent pairs the
+                                   // call met (decided in FP64), written the same way
 };
 
 // Adjoint of one propagation: cotangents of the outputs in, gradients with

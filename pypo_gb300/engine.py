@@ -127,6 +127,12 @@ def last_extent():
     return float(load().po_last_extent())
 
 
+def last_band_pairs():
+    """Near-tangent (source, target) pairs of this thread's last mixed-precision
+    host-buffer call, decided and summed in FP64 (po_last_band_pairs)."""
+    return int(load().po_last_band_pairs())
+
+
 def _extent_warning(m, precision):
     """Warn when a mixed-precision call's frame half-extent m is beyond the
     measured range of the path."""

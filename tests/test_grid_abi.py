@@ -19,7 +19,8 @@ def declared_functions():
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     text = re.sub(r"^\s*typedef\b[^;]*;", "", text, flags=re.M)   # function-pointer types are not entry points
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?(?:(?:unsigned|signed|long|short)\s+)*\w+(?:\s+|\s*\*\s*)(\w+)\s*\(",
+                                 text, flags=re.M)))
 
 
 def test_library_exports_every_declared_symbol(lib):

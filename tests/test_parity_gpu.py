@@ -71,6 +71,10 @@ def test_tangent_pairs(cuda, lib, oracle_mod):
     assert 0 < touched.sum() < 0.2 * t.shape[1]
     ref = c["out_EH_fwd"]
     got = _run(c, "EH", -1.0, "mixed")
+    # every exactly tangent pair (36) is inside the band, and few others are
+    n_tangent = int((np.abs(nd) <= 1e-12 * np.sqrt((d ** 2).sum(0))).sum())
+    from pypo_gb300 import engine
+    assert n_tangent == 36 and n_tangent <= engine.last_band_pairs() <= 4 * n_tangent
     for sel in (slice(None), touched):
         e, p = errors(got[:, sel], ref[:, sel], "EH")
         assert e <= REL_L2_TOL and p <= PHASE_TOL, (e, p)
@@ -212,10 +216,12 @@ def test_coplanar_targets_every_pair_in_the_band(cuda, lib, oracle_mod):
     k = 2 * np.pi / 0.1
     for mode in ("EH", "JM"):
         got = engine.propagate(mode, s7, cur, -1, 0, 0, t7, k)
+        assert engine.last_band_pairs() == ns * nt
         ref = oracle_mod.run(mode, s7, cur, -1, 0, 0, t7, k)
         assert _rel(got, ref) <= 1e-12, (mode, _rel(got, ref))
     cot = rng.standard_normal((12, nt))
     gm = engine.adjoint("EH", s7, cur, -1, 0, 0, t7, k, cot)
+    assert engine.last_band_pairs() == ns * nt
     go = oracle_mod.adjoint("EH", s7, cur, -1, 0, 0, t7, k, cot)
     for name, want in go.items():
         assert _rel(gm[name], want) <= 1e-10, (name, _rel(gm[name], want))
@@ -251,3 +257,13 @@ def test_high_kr_against_reference_outputs(cuda, lib):
             assert e <= REL_L2_TOL and p <= PHASE_TOL, (mode, tag, e, p)
             d = engine.propagate(mode, c["src_grid"], cur, *grid, c[tg], float(c["k"]), 1.0, t, "fp64")
             np.testing.assert_allclose(d, ref, rtol=0, atol=FP64_TOL * np.abs(ref).max(), err_msg=f"{mode} {tag}")
+
+
+def test_no_band_pairs_on_the_dish_workloads(cuda, lib):
+    """The dish workloads face their targets: no pair comes near tangency,
+    so nothing is left to the FP64 fixup (and the near field's tiles are all
+    proven lit)."""
+    from pypo_gb300 import configs, engine
+    for w in (configs.dish_eh(scale=0.2), configs.dish_ff(scale=0.1)):
+        engine.propagate(w["mode"], w["s7"], w["cur"], w["gmode"], w["ncx"], w["ncy"], w["t7"], w["k"])
+        assert engine.last_band_pairs() == 0, w["name"]
