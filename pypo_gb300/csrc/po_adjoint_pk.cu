@@ -586,7 +586,7 @@ po_adj_pk_kernel(const float4 *__restrict__ srcpk, long ns, const float4 *__rest
     // Far field, M = 0: the CTA's box of source normals for the lit-tile
     // proof (a tile's directions r_hat against it: min n.r_hat >= 1e-5, the
     // least of n.r over the two boxes being the sum of the least corner
-    // products per axis; the test is n.r_hat >= -5e-7). Only there: the
+    // products per axis; the per-pair test: lit when n.r_hat >= 1e-6). Only there: the
     // near-field adjoint needs n_s.R for its displacement gradient anyway,
     // and a second copy of the loop is not worth its cost with M.
     constexpr bool kLitA = KIND == kKindFF && !HAS_M;

@@ -435,7 +435,7 @@ po_ff_kernel(const float4 *__restrict__ src, long ntiles, long chunk, const floa
         if (kLitPath && boxes) {
             // every pair lit when the least n . r over the tile's box of
             // normals and the CTA's box of directions is at least 1e-5 (the
-            // per-pair test is n . r >= -5e-7): the least of n r over n in
+            // per-pair test is lit when n . r >= 1e-6): the least of n r over n in
             // [a, b], r in [c, d] is the least of the four corner products
             float L = 0.0f;
 #pragma unroll

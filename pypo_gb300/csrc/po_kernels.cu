@@ -219,7 +219,8 @@ __device__ __forceinline__ void sc_pair2(float2 *acc, const float2 *tc, const fl
 // the unused slot 21 of its first four pair records, so it arrives in
 // shared memory with the tile's copy: n.(t - s) >= min over the boxes of
 // n.t - max n.s, required above a margin of 1e-5 (|t|_1 + |s|_1) for the
-// FP32 rounding of both sides (the test is n.d + 5e-7 R >= 0). The least of
+// FP32 rounding of both sides (a pair is lit for the per-pair test when
+// n.d >= 1e-6 R, kTangentBand). The least of
 // n t over n in [a, b], t in [c, d] is the least of the four corner products.
 template <int REC>
 __device__ __forceinline__ bool tile_lit(const float4 *tile, const float *tb)

@@ -3,14 +3,14 @@ po_src_box_kernel and the CTA target box of po_pk_kernel), restated in numpy
 FP32 on the CPU: whenever the proof says a tile is lit for a block of
 targets, every (source, target) pair of the two passes the kernel's own
 per-pair test, computed the kernel's way (hi/lo split positions in turns,
-FP32 differences, n.d + 5e-7 R >= 0). Seeded random scenes, among them ones
+FP32 differences; lit when n.d >= 1e-6 R, the tangent band's edge). Seeded random scenes, among them ones
 whose targets graze the sources' tangent planes, where the margins matter.
 """
 import numpy as np
 import pytest
 
 F = np.float32
-TOL = F(5e-7)
+BAND = F(1e-6)   # kTangentBand: lit at n.d >= BAND R, deferred to FP64 inside +-BAND R
 
 
 def split(x, q):
@@ -49,7 +49,7 @@ def pair_test(sh, sl, n, th, tl):
     d = (dh + dl).astype(F)
     R = np.sqrt((d.astype(np.float64) ** 2).sum(-1)).astype(F)
     nd = (n[:, None, 2] * d[..., 2] + (n[:, None, 1] * d[..., 1] + n[:, None, 0] * d[..., 0])).astype(F)
-    return (TOL * R + nd) >= 0
+    return nd >= BAND * R
 
 
 def scene(seed):
