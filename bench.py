@@ -466,6 +466,30 @@ def run_ours(args):
     e2e = w["pairs"] * args.steps / e2e_s / 1e9 * world
     h2d = 2 * (7 + 12) * ns * 8 + 2 * 7 * nt * 8 + nout * nt * 8
     d2h = nout * nt * 8 + 13 * ns * 8 + (0 if far else nt * 8)
+
+    # ---- the forward as a PyPO user calls it: BindGPU.PyPO_GPUf with the
+    # reference's arguments (reflDicts, runPODict, a currents object) through
+    # the float drop-in ABI callKernelf_*, which generates both grids inside
+    # the call; the result comes back as PyPO field objects
+    drop_in = None
+    if w.get("src") is not None and w.get("tgt") is not None:
+        from pypo_gb300 import BindGPU, PyPOTypes as PT
+        shape = tuple(int(v) for v in w["src"]["gridsize"])
+        comps = [(w["cur"][6 * g + a] + 1j * w["cur"][6 * g + 3 + a]).reshape(shape) for g in range(2)
+                 for a in range(3)]
+        sc = PT.currents(*comps)
+        sc.setMeta("src", float(k))
+        rdict = {"mode": mode, "exp": "fwd", "epsilon": 1.0, "k": float(k), "nThreads": 256, "s_current": sc}
+        BindGPU.PyPO_GPUf(w["src"], w["tgt"], dict(rdict))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            BindGPU.PyPO_GPUf(w["src"], w["tgt"], dict(rdict))
+        drop_s = (time.perf_counter() - t0) / args.steps
+        drop_in = {"value": w["pairs"] / drop_s / 1e9, "unit": "Gpairs/s", "ms_per_call": drop_s * 1e3,
+                   "path": "BindGPU.PyPO_GPUf -> callKernelf_" + mode + " (the reference's float ABI, both grids "
+                           "generated inside the call, results as PyPO field objects), forward only: the "
+                           "reference has no adjoint"}
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -599,6 +623,7 @@ def run_ours(args):
                          "sample": f"{ncpu} random targets x {ns} sources, forward {cpu_tf:.1f} s + adjoint "
                                    f"{cpu_ta:.1f} s, FP64 oracle (the reference's algorithm)"},
         "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "drop_in_forward": drop_in,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
     }
