@@ -110,8 +110,9 @@ const char *po_last_error(void);
  * Same signatures as reference src/CUDA/InterfaceCUDA.h:31-64 (ctypes
  * argtypes src/PyPO/BindGPU.py:34-74), called from BindGPU.PyPO_GPUf
  * (src/PyPO/BindGPU.py:83-224). Like the reference they generate the source
- * and target grids from the reflparamsf into cs / ct (here in FP64, then
- * stored as float), and fill res. nBlocks / nThreads are accepted and
+ * and target grids from the reflparamsf into cs / ct (here in FP64 on the
+ * device, then stored as float; the reference generates them on the host),
+ * and fill res. nBlocks / nThreads are accepted and
  * ignored: the engine picks its own tiling. Computation is mixed precision
  * (FP32 bulk, split hi/lo separation and phase). The reference returns void;
  * these return the status (ctypes restype None ignores it).

@@ -254,60 +254,102 @@ void widen(const reflparamsf &f, Widened &w)
     w.r.rms_seed = f.rms_seed;
 }
 
-int make_grid(const reflparamsf &pf, std::vector<double> &g7, reflcontainerf *cf)
-{
-    if (!pf.n_cells || !pf.lxu || !pf.lyv) return fail(1, "reflparamsf has null arrays");
-    const long n = (long)pf.n_cells[0] * pf.n_cells[1];
-    if (n <= 0) return fail(1, "empty grid");
-    Widened w;
-    widen(pf, w);
-    g7.assign(7 * n, 0.0);
-    reflcontainer c;
-    c.size = (int)n;
-    c.x = g7.data();
-    c.y = c.x + n;
-    c.z = c.y + n;
-    c.nx = c.z + n;
-    c.ny = c.nx + n;
-    c.nz = c.ny + n;
-    c.area = c.nz + n;
-    if (po_grid_fill(w.r, &c, true, true)) return fail(1, "grid generation failed (bad gmode or sizes)");
-    if (cf && cf->x) {
-        float *dst[7] = {cf->x, cf->y, cf->z, cf->nx, cf->ny, cf->nz, cf->area};
-        for (int r = 0; r < 7; ++r)
-            if (dst[r])
-                for (long i = 0; i < n; ++i) dst[r][i] = (float)g7[r * n + i];
-    }
-    return 0;
-}
-
-// Shared body of the callKernelf_* drop-ins: FP64 grids, widened inputs,
-// mixed-precision run, float outputs into the caller's bundle rows.
+// Shared body of the callKernelf_* drop-ins. Both grids are generated in
+// FP64 on the device from the widened reflparams (the reference generates
+// them on the host); the currents are widened on the host and copied once;
+// the mixed-precision run is followed by one synchronisation. The FP64 grids
+// come back into the caller's float containers cs / ct, and the outputs into
+// its float bundle rows.
 int drop_in(int mode, float *const *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
             reflcontainerf *ct, float *const *inp, float k, float epsilon, float t)
 {
     po::clear_error();
-    std::vector<double> s7, t7;
-    if (int rc = make_grid(source, s7, cs)) return rc;
-    if (int rc = make_grid(target, t7, ct)) return rc;
+    t_extent = 0.0;
+    t_band = 0;
+    if (!source.n_cells || !source.lxu || !source.lyv || !target.n_cells || !target.lxu || !target.lyv)
+        return fail(1, "reflparamsf has null arrays");
     const long ns = (long)source.n_cells[0] * source.n_cells[1];
     const long nt = (long)target.n_cells[0] * target.n_cells[1];
-    const int ncur = mode == po::kScalar ? 2 : 12;
-    std::vector<double> cur((size_t)ncur * ns);
-    for (int r = 0; r < ncur; ++r) {
-        if (!inp[r]) return fail(1, "null current array");
-        for (long i = 0; i < ns; ++i) cur[r * ns + i] = inp[r][i];
-    }
+    if (ns <= 0 || nt <= 0) return fail(1, "empty grid");
     const int nout = po::n_out(mode);
-    std::vector<double> out((size_t)nout * nt);
-    int rc = run_host(mode, ns, s7.data(), source.gmode, source.n_cells[0], source.n_cells[1], cur.data(), nt,
-                      t7.data(), (double)k, (double)epsilon, (double)t, 0, out.data());
-    if (rc) return rc;
-    for (int r = 0; r < nout; ++r) {
+    if (nout < 0) return fail(1, "mode must be 0..5 (JM EH JMEH EHP FF scalar)");
+    const int ncur = mode == po::kScalar ? 2 : 12;
+    for (int r = 0; r < ncur; ++r)
+        if (!inp[r]) return fail(1, "null current array");
+    for (int r = 0; r < nout; ++r)
         if (!res[r]) return fail(1, "null result array");
-        for (long i = 0; i < nt; ++i) res[r][i] = (float)out[r * nt + i];
+    Widened ws, wt;
+    widen(source, ws);
+    widen(target, wt);
+    std::vector<double> cur((size_t)ncur * ns), out((size_t)nout * nt), grid((size_t)7 * std::max(ns, nt));
+    for (int r = 0; r < ncur; ++r)
+        for (long i = 0; i < ns; ++i) cur[r * ns + i] = inp[r][i];
+    cudaStream_t s = nullptr;
+    if (int rc = lib_stream(&s)) return rc;
+    double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_out = nullptr;
+    int rc = 0, code = 0;
+    HostSlots local{};
+    HostSlots *hs = host_slots(&local);
+    po::RunArgs a;
+    PO_SCRATCH(d_src, sizeof(double) * 7 * ns);
+    PO_SCRATCH(d_cur, sizeof(double) * ncur * ns);
+    PO_SCRATCH(d_tgt, sizeof(double) * 7 * nt);
+    PO_SCRATCH(d_out, sizeof(double) * nout * nt);
+    if ((rc = po::generate_grid_dev(ws.r, d_src, true, true, s)) ||
+        (rc = po::generate_grid_dev(wt.r, d_tgt, true, true, s)))
+        goto done;
+    CK(cudaMemcpyAsync(d_cur, cur.data(), sizeof(double) * ncur * ns, cudaMemcpyHostToDevice, s));
+    a.mode = mode;
+    a.ns = ns;
+    a.src7 = d_src;
+    a.gmode = source.gmode;
+    a.ncx = source.n_cells[0];
+    a.ncy = source.n_cells[1];
+    a.cur = d_cur;
+    a.nt = nt;
+    a.tgt7 = d_tgt;
+    a.k = (double)k;
+    a.epsilon = (double)epsilon;
+    a.t_dir = (double)t;
+    a.precision = 0;
+    a.m_zero = false;
+    if (mode != po::kScalar) {
+        bool mz = false;
+        if ((rc = m_is_zero(cur.data(), d_cur, ns, s, mz))) goto done;
+        a.m_zero = mz;
     }
-    return 0;
+    a.extent_host = &hs->extent;
+    a.band_host = &hs->band;
+    a.out = d_out;
+    a.stream = s;
+    rc = po::run_device(a);
+    if (rc) goto done;
+    CK(cudaMemcpyAsync(out.data(), d_out, sizeof(double) * nout * nt, cudaMemcpyDeviceToHost, s));
+    rc = po::read_device_error(s, &code);   // the kernels' one synchronisation
+    if (!rc && code) rc = fail(4, device_error_text(code));
+    if (rc) goto done;
+    t_extent = hs->extent;
+    t_band = hs->band;
+    for (int r = 0; r < nout; ++r)
+        for (long i = 0; i < nt; ++i) res[r][i] = (float)out[r * nt + i];
+    // the grids, as the reference leaves them in cs and ct
+    for (int w = 0; w < 2; ++w) {
+        reflcontainerf *cf = w == 0 ? cs : ct;
+        if (!cf || !cf->x) continue;
+        const long n = w == 0 ? ns : nt;
+        CK(cudaMemcpy(grid.data(), w == 0 ? d_src : d_tgt, sizeof(double) * 7 * n, cudaMemcpyDeviceToHost));
+        float *dst[7] = {cf->x, cf->y, cf->z, cf->nx, cf->ny, cf->nz, cf->area};
+        for (int r = 0; r < 7; ++r)
+            if (dst[r])
+                for (long i = 0; i < n; ++i) dst[r][i] = (float)grid[r * n + i];
+    }
+done:
+    if (d_src) cudaFreeAsync(d_src, s);
+    if (d_cur) cudaFreeAsync(d_cur, s);
+    if (d_tgt) cudaFreeAsync(d_tgt, s);
+    if (d_out) cudaFreeAsync(d_out, s);
+    if (s && rc) cudaStreamSynchronize(s);
+    return rc;
 }
 
 }  // namespace

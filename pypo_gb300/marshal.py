@@ -63,6 +63,7 @@ def alloc_container(n, ctype=ctypes.c_double):
     st.size = n
     for i, name in enumerate(("x", "y", "z", "nx", "ny", "nz", "area")):
         setattr(st, name, _ptr(block[i], ctype))
+    st._block = block
     return st, block
 
 
@@ -73,16 +74,20 @@ def fill_container(block, ctype=ctypes.c_double):
     st.size = block.shape[1]
     for i, name in enumerate(("x", "y", "z", "nx", "ny", "nz", "area")):
         setattr(st, name, _ptr(block[i], ctype))
+    st._block = block
     return st, block
 
 
 def bundle(cls, block, ctype):
-    """Point a bundle struct's members, in field order, at the rows of `block`."""
+    """Point a bundle struct's members, in field order, at the rows of `block`.
+    The struct holds a reference to `block`, so a temporary block stays
+    alive as long as the struct does."""
     st = cls()
     names = [f[0] for f in cls._fields_]
     assert block.shape[0] == len(names)
     for i, name in enumerate(names):
         setattr(st, name, _ptr(block[i], ctype))
+    st._block = block
     return st
 
 

@@ -155,3 +155,15 @@ def test_adjoint_output_buffers_are_checked_before_any_device_work(lib):
                 {"dt": np.zeros((3, 1))}, {"cur": np.zeros((4, 12)).T}):
         with pytest.raises(POError, match="out\\["):
             engine.adjoint("EH", s7, cur, -1, 0, 0, t7, 1.0, cot, out=bad)
+
+
+def test_bundles_keep_their_blocks_alive():
+    """A bundle made from a temporary block keeps it alive: its pointers stay valid."""
+    import gc
+    import ctypes
+    from pypo_gb300 import Structs as S, marshal as M
+    st = M.bundle(S.c2Bundlef, np.arange(12 * 5, dtype=np.float32).reshape(12, 5) + 1.0, ctypes.c_float)
+    junk = [np.zeros((12, 5), dtype=np.float32) for _ in range(50)]   # would reuse a freed block
+    gc.collect()
+    assert st.r1x[0] == 1.0 and st.i2z[4] == 60.0
+    del junk

@@ -267,3 +267,31 @@ def test_no_band_pairs_on_the_dish_workloads(cuda, lib):
     for w in (configs.dish_eh(scale=0.2), configs.dish_ff(scale=0.1)):
         engine.propagate(w["mode"], w["s7"], w["cur"], w["gmode"], w["ncx"], w["ncy"], w["t7"], w["k"])
         assert engine.last_band_pairs() == 0, w["name"]
+
+
+def test_drop_in_fills_the_grid_containers(cuda, lib):
+    """callKernelf_* through the reference's call shape leaves the source and
+    target grids in cs / ct, as the reference does: generated in FP64 (on the
+    device here) and stored as float, equal to the reference's own grids
+    (golden) to float rounding; and the result matches the golden output."""
+    import ctypes
+    from pypo_gb300 import Structs as S, marshal as M
+    c = load_case("paruv_to_plane")
+    src, tgt = c["src"], c["tgt"]
+    f = ctypes.c_float
+    csp, _k1 = M.fill_reflparams(src, f)
+    ctp, _k2 = M.fill_reflparams(tgt, f)
+    gs, gt = int(np.prod(src["gridsize"])), int(np.prod(tgt["gridsize"]))
+    cs, sblock = M.alloc_container(gs, f)
+    ct, tblock = M.alloc_container(gt, f)
+    cur32 = np.ascontiguousarray(c["cur"], dtype=np.float32)   # kept alive: the bundle points into it
+    cin = M.bundle(S.c2Bundlef, cur32, f)
+    out = np.zeros((12, gt), dtype=np.float32)
+    res = M.bundle(S.c2Bundlef, out, f)
+    rc = lib.callKernelf_EH(ctypes.byref(res), csp, ctp, ctypes.byref(cs), ctypes.byref(ct), ctypes.byref(cin),
+                            f(float(c["k"])), f(float(c["epsilon"])), f(-1.0), 1, 256)
+    assert rc == 0, lib.po_last_error()
+    for block, ref in ((sblock, c["src_grid"]), (tblock, c["tgt_grid"])):
+        np.testing.assert_allclose(block, ref, rtol=0, atol=1e-6 * np.abs(ref).max())
+    e, p = errors(out.astype(np.float64), c["out_EH_fwd"], "EH")
+    assert e <= 1e-5 and p <= 1e-4, (e, p)
