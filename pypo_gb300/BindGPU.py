@@ -39,12 +39,12 @@ def _t_direction(runPODict):
     return -1.0 if runPODict.get("exp", "fwd") == "fwd" else 1.0
 
 
-def _source_values(runPODict, gs):
+def _source_values(runPODict, gs, ctype=ctypes.c_double):
     if runPODict["mode"] == "scalar":
         sf = runPODict["s_scalarfield"]
         S_ = np.asarray(sf.S).ravel()
-        return np.stack([S_.real, S_.imag])
-    return M.currents_block([runPODict["s_current"][i] for i in range(6)], ctypes.c_double)
+        return np.stack([S_.real, S_.imag]).astype(M._NP[ctype])
+    return M.currents_block([runPODict["s_current"][i] for i in range(6)], ctype)
 
 
 def _unpack(mode, block, shape):
@@ -76,7 +76,7 @@ def PyPO_GPUf(source, target, runPODict):
     gt = int(np.prod(target["gridsize"]))
     cs, _sblock = M.alloc_container(gs, f)
     ct, _tblock = M.alloc_container(gt, f)
-    vals = _source_values(runPODict, gs).astype(np.float32)
+    vals = _source_values(runPODict, gs, f)
     in_cls = S.arrC1f if mode == "scalar" else S.c2Bundlef
     cin = M.bundle(in_cls, vals, f)
     out = np.zeros((S.N_OUT[mode], gt), dtype=np.float32)

@@ -256,10 +256,11 @@ void widen(const reflparamsf &f, Widened &w)
 
 // Shared body of the callKernelf_* drop-ins. Both grids are generated in
 // FP64 on the device from the widened reflparams (the reference generates
-// them on the host); the currents are widened on the host and copied once;
-// the mixed-precision run is followed by one synchronisation. The FP64 grids
-// come back into the caller's float containers cs / ct, and the outputs into
-// its float bundle rows.
+// them on the host); the float currents are copied as they are and widened
+// on the device; after the mixed-precision run and the call's one
+// synchronisation of its kernels, the outputs and the two grids are narrowed
+// to float on the device and copied into the caller's bundle rows and
+// containers cs / ct, as the reference leaves them.
 int drop_in(int mode, float *const *res, reflparamsf source, reflparamsf target, reflcontainerf *cs,
             reflcontainerf *ct, float *const *inp, float k, float epsilon, float t)
 {
@@ -281,24 +282,31 @@ int drop_in(int mode, float *const *res, reflparamsf source, reflparamsf target,
     Widened ws, wt;
     widen(source, ws);
     widen(target, wt);
-    std::vector<double> cur((size_t)ncur * ns), out((size_t)nout * nt), grid((size_t)7 * std::max(ns, nt));
-    for (int r = 0; r < ncur; ++r)
-        for (long i = 0; i < ns; ++i) cur[r * ns + i] = inp[r][i];
     cudaStream_t s = nullptr;
     if (int rc = lib_stream(&s)) return rc;
     double *d_src = nullptr, *d_cur = nullptr, *d_tgt = nullptr, *d_out = nullptr;
+    float *d_f = nullptr;   // float staging: the currents in, then the outputs and grids out
+    const long nf = std::max({(long)ncur * ns, (long)nout * nt, 7L * std::max(ns, nt)});
     int rc = 0, code = 0;
     HostSlots local{};
     HostSlots *hs = host_slots(&local);
     po::RunArgs a;
+    const unsigned cblk = 608;   // 152 SMs x 4, grid-stride
     PO_SCRATCH(d_src, sizeof(double) * 7 * ns);
     PO_SCRATCH(d_cur, sizeof(double) * ncur * ns);
     PO_SCRATCH(d_tgt, sizeof(double) * 7 * nt);
     PO_SCRATCH(d_out, sizeof(double) * nout * nt);
+    PO_SCRATCH(d_f, sizeof(float) * nf);
     if ((rc = po::generate_grid_dev(ws.r, d_src, true, true, s)) ||
         (rc = po::generate_grid_dev(wt.r, d_tgt, true, true, s)))
         goto done;
-    CK(cudaMemcpyAsync(d_cur, cur.data(), sizeof(double) * ncur * ns, cudaMemcpyHostToDevice, s));
+    for (int r = 0; r < ncur; ++r)
+        CK(cudaMemcpyAsync(d_f + (size_t)r * ns, inp[r], sizeof(float) * ns, cudaMemcpyHostToDevice, s));
+    {
+        long n = (long)ncur * ns;
+        void *args[] = {&d_f, &d_cur, &n};
+        CK(cudaLaunchKernel(po::f2d_kernel(), dim3(cblk), dim3(256), args, 0, s));
+    }
     a.mode = mode;
     a.ns = ns;
     a.src7 = d_src;
@@ -315,7 +323,7 @@ int drop_in(int mode, float *const *res, reflparamsf source, reflparamsf target,
     a.m_zero = false;
     if (mode != po::kScalar) {
         bool mz = false;
-        if ((rc = m_is_zero(cur.data(), d_cur, ns, s, mz))) goto done;
+        if ((rc = device_m_is_zero(d_cur, ns, s, mz))) goto done;
         a.m_zero = mz;
     }
     a.extent_host = &hs->extent;
@@ -324,30 +332,38 @@ int drop_in(int mode, float *const *res, reflparamsf source, reflparamsf target,
     a.stream = s;
     rc = po::run_device(a);
     if (rc) goto done;
-    CK(cudaMemcpyAsync(out.data(), d_out, sizeof(double) * nout * nt, cudaMemcpyDeviceToHost, s));
+    {
+        long n = (long)nout * nt;
+        void *args[] = {&d_out, &d_f, &n};
+        CK(cudaLaunchKernel(po::d2f_kernel(), dim3(cblk), dim3(256), args, 0, s));
+    }
+    for (int r = 0; r < nout; ++r)
+        CK(cudaMemcpyAsync(res[r], d_f + (size_t)r * nt, sizeof(float) * nt, cudaMemcpyDeviceToHost, s));
     rc = po::read_device_error(s, &code);   // the kernels' one synchronisation
     if (!rc && code) rc = fail(4, device_error_text(code));
     if (rc) goto done;
     t_extent = hs->extent;
     t_band = hs->band;
-    for (int r = 0; r < nout; ++r)
-        for (long i = 0; i < nt; ++i) res[r][i] = (float)out[r * nt + i];
     // the grids, as the reference leaves them in cs and ct
     for (int w = 0; w < 2; ++w) {
         reflcontainerf *cf = w == 0 ? cs : ct;
         if (!cf || !cf->x) continue;
-        const long n = w == 0 ? ns : nt;
-        CK(cudaMemcpy(grid.data(), w == 0 ? d_src : d_tgt, sizeof(double) * 7 * n, cudaMemcpyDeviceToHost));
+        long n = 7L * (w == 0 ? ns : nt);
+        double *g = w == 0 ? d_src : d_tgt;
+        void *args[] = {&g, &d_f, &n};
+        CK(cudaLaunchKernel(po::d2f_kernel(), dim3(cblk), dim3(256), args, 0, s));
         float *dst[7] = {cf->x, cf->y, cf->z, cf->nx, cf->ny, cf->nz, cf->area};
+        const long np = n / 7;
         for (int r = 0; r < 7; ++r)
-            if (dst[r])
-                for (long i = 0; i < n; ++i) dst[r][i] = (float)grid[r * n + i];
+            if (dst[r]) CK(cudaMemcpyAsync(dst[r], d_f + (size_t)r * np, sizeof(float) * np, cudaMemcpyDeviceToHost, s));
     }
+    CK(cudaStreamSynchronize(s));
 done:
     if (d_src) cudaFreeAsync(d_src, s);
     if (d_cur) cudaFreeAsync(d_cur, s);
     if (d_tgt) cudaFreeAsync(d_tgt, s);
     if (d_out) cudaFreeAsync(d_out, s);
+    if (d_f) cudaFreeAsync(d_f, s);
     if (s && rc) cudaStreamSynchronize(s);
     return rc;
 }

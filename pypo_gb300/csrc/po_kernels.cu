@@ -954,7 +954,22 @@ void *frame_kernel() { return reinterpret_cast<void *>(&po_frame_kernel); }
 void *pack_src_kernel() { return reinterpret_cast<void *>(&po_pack_src_kernel); }
 void *pack_tgt_kernel() { return reinterpret_cast<void *>(&po_pack_tgt_kernel); }
 void *pack_src_d_kernel() { return reinterpret_cast<void *>(&po_pack_src_d_kernel); }
+// Precision conversions of the float drop-in ABI's buffers (n elements).
+__global__ void po_f2d_kernel(const float *__restrict__ in, double *__restrict__ out, long n)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+__global__ void po_d2f_kernel(const double *__restrict__ in, float *__restrict__ out, long n)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
 void *epilogue_kernel() { return reinterpret_cast<void *>(&po_epilogue_kernel); }
+void *f2d_kernel() { return reinterpret_cast<void *>(&po_f2d_kernel); }
+void *d2f_kernel() { return reinterpret_cast<void *>(&po_d2f_kernel); }
 void *fp32_probe_kernel() { return reinterpret_cast<void *>(&po_fp32_probe_kernel); }
 void *wait_selftest_kernel() { return reinterpret_cast<void *>(&po_wait_selftest_kernel); }
 void *band_fixup_kernel(int kind)

@@ -182,6 +182,8 @@ void *pack_src_kernel();
 void *pack_tgt_kernel();
 void *pack_src_d_kernel();
 void *epilogue_kernel();
+void *f2d_kernel();   // float -> double, grid-stride over n
+void *d2f_kernel();   // double -> float
 void *fp32_probe_kernel();
 void *band_fixup_kernel(int kind);
 void *adj_band_fixup_kernel(int kind, int t_sign, bool want_d, bool want_t);

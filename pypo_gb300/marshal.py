@@ -92,12 +92,16 @@ def bundle(cls, block, ctype):
 
 
 def currents_block(cur, ctype=ctypes.c_double):
-    """(12, n) block in c2Bundle order from a (6, ...) complex array-like (Jx..Mz)."""
+    """(12, n) block in c2Bundle order from a (6, ...) complex array-like
+    (Jx..Mz), written straight into the ctype's precision."""
     c = [np.asarray(a).ravel() for a in cur]
-    rows = []
-    for grp in (c[0:3], c[3:6]):
-        rows += [np.real(a) for a in grp] + [np.imag(a) for a in grp]
-    return np.ascontiguousarray(np.stack(rows), dtype=_NP[ctype])
+    out = np.empty((12, c[0].size), dtype=_NP[ctype])
+    for g in range(2):
+        for a in range(3):
+            z = c[3 * g + a]
+            out[6 * g + a] = np.real(z)
+            out[6 * g + 3 + a] = np.imag(z)
+    return out
 
 
 def block_to_complex(block, n_complex):
@@ -106,5 +110,8 @@ def block_to_complex(block, n_complex):
     for b in range(n_complex):
         re = block[6 * b:6 * b + 3]
         im = block[6 * b + 3:6 * b + 6]
-        out.append(re.astype(np.float64) + 1j * im.astype(np.float64))
+        z = np.empty(re.shape, dtype=np.complex128)
+        z.real = re
+        z.imag = im
+        out.append(z)
     return np.concatenate(out, axis=0)
