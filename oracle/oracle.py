@@ -28,11 +28,13 @@ _lib = None
 
 
 def build(quiet=True):
-    """Compile oracle/po_oracle.c with gcc (plain C, no arch flags)."""
+    """Compile oracle/po_oracle.c with gcc (plain C, no arch flags; -O3 as
+    oracle/build_ref.sh builds the reference's own library, and no FP
+    contraction, so the sums are the reference's to the bit)."""
     import subprocess
     src = HERE / "po_oracle.c"
     tmp = str(LIB_PATH) + ".tmp"
-    cmd = ["gcc", "-O2", "-ffp-contract=off", "-std=c11", "-shared", "-fPIC", "-pthread", str(src), "-o", tmp, "-lm"]
+    cmd = ["gcc", "-O3", "-ffp-contract=off", "-std=c11", "-shared", "-fPIC", "-pthread", str(src), "-o", tmp, "-lm"]
     subprocess.run(cmd, check=True, capture_output=quiet)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
