@@ -232,3 +232,26 @@ def test_full_size_superposition(cuda, lib, name):
     g = grad(cot1 + 0.7 * cot2)
     ref = grad(cot1) + 0.7 * grad(cot2)
     assert float(torch.linalg.norm(g - ref) / torch.linalg.norm(ref)) <= 2e-6
+
+
+@pytest.mark.parametrize("mode", ["JMEH", "EHP"])
+def test_dish_eh_other_modes_full_size_sampled(cuda, lib, mode):
+    """The dish_eh configuration at full size in the other near-field modes:
+    JMEH (PEC currents and fields in one call) and EHP (the reflected field
+    from the normalised Poynting vector, nonlinear in E and H). Against the
+    plain FP64 GPU sum on a 1 % target sample."""
+    import torch
+    from pypo_gb300 import configs, engine
+    w = configs.dish_eh()
+    dev = cuda
+    s7, cur = (torch.tensor(w[k], device=dev) for k in ("s7", "cur"))
+    t7n = w["t7"].copy()
+    t7n[3:6] = [[0.0], [0.0], [-1.0]]   # the focal plane's normal faces the dish (JM, EHP use it)
+    t7 = torch.tensor(t7n, device=dev)
+    grid = (w["gmode"], w["ncx"], w["ncy"])
+    got = engine.propagate_dev(mode, s7, cur, *grid, t7, w["k"], m_zero=True).cpu().numpy()
+    idx = np.sort(np.random.default_rng(13).choice(t7n.shape[1], size=t7n.shape[1] // 100, replace=False))
+    ts = torch.tensor(np.ascontiguousarray(t7n[:, idx]), device=dev)
+    ref = engine.propagate_dev(mode, s7, cur, *grid, ts, w["k"], precision="fp64").cpu().numpy()
+    e, p = errors(got[:, idx], ref, mode)
+    assert e <= REL_L2_TOL and p <= PHASE_TOL, (mode, e, p)
