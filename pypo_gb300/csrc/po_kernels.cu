@@ -23,12 +23,18 @@
 //   * (M = 0) a tile whose box of normals and positions proves every pair
 //     lit for the CTA's targets runs without the per-pair illumination test
 //     (tile_lit; the boxes travel in the records' spare slot 21);
+//   * the per-pair test counts a pair lit when n . d >= 1e-6 R and unlit
+//     below -1e-6 R; a pair in between is left out, its tile flagged, and the
+//     rare path after the tile's fold lists it (nf_band_scan) for
+//     po_band_fixup_kernel, which decides it with the reference's FP64
+//     rounding and adds its FP64 term;
 //   * a source chunk (blockIdx.y) writes its totals as doubles; the epilogue
 //     kernel adds the chunks in a fixed order and applies the mode's physics
 //     (PEC current, EHP reflection, far-field projection) in FP64.
 //
 // The plain FP64 direct sum (po_fp64_kernel) is the comparison path: same
-// formulas, double everywhere, no splitting.
+// formulas, double everywhere, no splitting. The far field's forward kernel
+// is in po_farfield.cu.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <cstdint>
